@@ -1,0 +1,202 @@
+/*
+ * pnepma.h -- C ABI of the GB300 PN-moment transport solve (forward k-ratio functional and
+ * its adjoint gradient).
+ *
+ * The reference exposes this path as Julia methods with no foreign-function layer; the entry
+ * points below are what a Julia shim binds with ccall to replace them (the binding is shown in
+ * INTEGRATION.md):
+ *
+ *   pn_create            <- ForwardPNProblem{N,T}(...) / AdjointPNProblem(frwd)
+ *                           pn_solver/pn_problem.jl:72-136 (matrices, boundary source, tables)
+ *   pn_forward           <- calc_intensities(problem, m, x_rays, detector_position)
+ *                           pn_solver/pn_intensities.jl:325-351
+ *   pn_adjoint           <- the pullback of the Zygote.@adjoint of calc_intensities
+ *                           pn_solver/pn_intensities.jl:353-413 (returns rho_bar, NOA_bar, ACS_bar;
+ *                           the material pullbacks of :406-409 stay with the caller)
+ *   pn_generation_field  <- calc_x_ray_generation_field, pn_solver/pn_intensities.jl:189-212
+ *   pn_step              <- step_pn!(problem, rho, u, du, E, dE), pn_solver/pn_intensities.jl:16-30
+ *                           (StaRMAP.step_pde!, starmap/src/solver.jl:171-196)
+ *
+ * Conventions
+ *   - Units are the reference's calculation units: cm, g, eV (pn_solver/units.jl).
+ *   - Class order is eee, eeo, eoe, eoo, oee, oeo, ooe, ooo (starmap/src/even_odd_classification.jl:19);
+ *     class c has parity bits (ox, oy, oz) = (c>>2 & 1, c>>1 & 1, c & 1).
+ *   - A class grid has M_d points along an axis where it is even, M_d + 1 (two ghost points)
+ *     where it is odd, and 1 along a singleton axis (n_points[d] == 1).
+ *   - Per-cell vectors are stored as the reference's Array{MVector} arrays are laid out in memory:
+ *     the vector index fastest, then x, then y, then z.  Classes are concatenated in class order.
+ *   - All functions return a pn_status; none aborts or throws across the ABI.  After an error,
+ *     pn_last_error(handle) describes it.
+ *   - A handle is used by one thread at a time; distinct handles may be used concurrently.
+ *     The caller owns every host buffer; the library owns device memory.
+ */
+#ifndef PNEPMA_H
+#define PNEPMA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PN_ABI_VERSION 1
+
+typedef enum pn_status {
+  PN_OK = 0,
+  PN_ERR_INVALID = -1,       /* malformed descriptor or argument */
+  PN_ERR_UNSUPPORTED = -2,   /* P_N order or layout not compiled into this build */
+  PN_ERR_CFL = -3,           /* energy step above the stability estimate (only with PN_FLAG_CHECK_CFL) */
+  PN_ERR_NO_MEMORY = -4,     /* device allocation failed or memory budget exceeded */
+  PN_ERR_DIVERGED = -5,      /* a non-finite value appeared in the solution */
+  PN_ERR_TIMEOUT = -6,       /* a bounded device-side wait ran out */
+  PN_ERR_CUDA = -7,          /* CUDA runtime error */
+  PN_ERR_STATE = -8,         /* call out of order (e.g. adjoint before forward) */
+  PN_ERR_NO_DEVICE = -9      /* no CUDA device is available */
+} pn_status;
+
+typedef enum pn_precision {
+  PN_FP64 = 0,   /* "plain" method: state, stencil and accumulators in FP64 */
+  PN_FP32 = 1    /* state and stencil in FP32, intensity/gradient accumulators in FP64 */
+} pn_precision;
+
+enum pn_flags {
+  PN_FLAG_CHECK_FINITE = 1,  /* report PN_ERR_DIVERGED when the intensities are not finite */
+  PN_FLAG_CHECK_CFL = 2      /* reject descriptors whose energy step exceeds cfl_limit */
+};
+
+/*
+ * Problem descriptor.  Everything the solve needs except the material fields.  The caller
+ * evaluates the physical data (stopping power, transport coefficients, ionisation cross-sections,
+ * beam) at the energies of the march and passes them as tables, exactly as the reference's
+ * update_problem! would evaluate them (pn_solver/pn_problem.jl:157-249).
+ *
+ * Energy march: dE = (E_initial - E_cutoff) / n_steps; forward step i (1-based) goes from E_{i-1}
+ * to E_i with coefficients at E_{i-1} - dE/2 (pn_intensities.jl:341-349).  Adjoint iteration
+ * j = 0..n_steps-1 handles tape state n_steps - j at energy Ea_j (Ea_0 = E_cutoff, Ea_{j+1} =
+ * Ea_j + dE); iteration j == n_steps is the final accumulation at the initial state
+ * (pn_intensities.jl:391-404).
+ */
+typedef struct pn_desc {
+  int32_t abi_version;       /* PN_ABI_VERSION */
+  int32_t order;             /* P_N order N */
+  int32_t n_points[3];       /* M per axis; 1 marks a singleton axis */
+  int32_t n_elements;        /* n_e */
+  int32_t n_xrays;           /* n_r */
+  int32_t n_steps;
+  int32_t precision;         /* pn_precision */
+  int32_t checkpoint_stride; /* adjoint tape: 0 keeps every state, K > 0 keeps every K-th and recomputes */
+  int32_t flags;             /* pn_flags */
+  int32_t reserved;
+  double  h[3];              /* grid steps (1.0 on a singleton axis) */
+  double  delta_e;           /* dE */
+  double  dvol;              /* h_x h_y h_z */
+  double  cfl_limit;         /* largest admissible dE when PN_FLAG_CHECK_CFL is set */
+  const int32_t* xray_element;   /* [n_r] element index (0-based) emitting each line */
+
+  /* advection blocks A_d[c], dense n_c x n_switch(c,d), row-major, for d = x,y,z and c = 0..7 in
+     that nesting; blocks of classes with no moments are empty.  The sparsity must match the
+     closed form of pn_solver/pn_matrices.jl:146-152 for this order (checked at pn_create). */
+  const double* advection;
+  /* boundary blocks for classes odd in d, same nesting, dense n_c x n_switch(c,d):
+     forward L*A (pn_matrices.jl:277-284) and adjoint -L'*A (pn_matrices.jl:286-293) */
+  const double* boundary_fwd;
+  const double* boundary_adj;
+  /* beam source on the right x face (gx_temp[eo][2,:,:], pn_problem.jl:192-203) for the classes
+     odd in x (oee, oeo, ooe, ooo in that order): [class][z][y][moment] */
+  const double* beam_face;
+
+  /* forward march, step i = 0..n_steps-1 (coefficients at E_i - dE/2 with E_0 = E_initial) */
+  const double* fwd_s;       /* [step][e]      s_e                          (update_coefficients!) */
+  const double* fwd_c;       /* [step][e][l]   c_{e,l} = -s_e' - (tc_l - tc_0), l = 0..N      */
+  const double* fwd_bc;      /* [step]         (Phi(E+dE) - Phi(E)) / dE   (update_boundary_condition!) */
+  const double* fwd_sigma;   /* [n_steps+1][r] sigma_r(E_i), i = 0..n_steps */
+  const double* fwd_weight;  /* [n_steps+1]    int_fac of each accumulation */
+
+  /* adjoint march, iteration j = 0..n_steps */
+  const double* adj_int_s;   /* [j][e]    forward s_e(Ea_j) */
+  const double* adj_int_c;   /* [j][e][l] forward c_{e,l}(Ea_j) */
+  const double* adj_int_bc;  /* [j]       forward beam weight at Ea_j */
+  const double* adj_sigma;   /* [j][r]    sigma_r(Ea_j) */
+  const double* adj_weight;  /* [j]       int_fac */
+  const double* adj_src_sigma; /* [j][r]  sigma_r(Ea_j + dE/2), j < n_steps */
+  const double* adj_s;       /* [j][e]    s_e(Ea_j + dE/2), j < n_steps */
+  const double* adj_c;       /* [j][e][l] adjoint c_{e,l} = -(tc_l - tc_0) at Ea_j + dE/2 */
+} pn_desc;
+
+/* Sizes the caller must allocate, derived from a descriptor. */
+typedef struct pn_sizes {
+  int32_t n_moments[8];      /* moments per class */
+  int32_t shape[8][3];       /* class grid (nx, ny, nz) including ghost points */
+  int64_t n_rho;             /* doubles in a rho / rho_bar buffer (all 8 classes, n_e per point) */
+  int64_t n_eee_cells;       /* cells of the eee grid */
+  int64_t n_noa;             /* n_eee_cells * n_e */
+  int64_t n_acs;             /* n_eee_cells * n_r */
+  int64_t n_state;           /* doubles of a full state (all 8 classes, moments per point) */
+  int64_t n_beam_face;       /* doubles expected in beam_face */
+  int64_t n_advection;       /* doubles expected in advection */
+  int64_t n_boundary;        /* doubles expected in boundary_fwd (and boundary_adj) */
+  int64_t device_bytes;      /* device memory pn_create will allocate */
+} pn_sizes;
+
+typedef struct pn_handle pn_handle;
+
+/* Fill *sizes for a descriptor (no device work).  Replaces nothing in the reference; it lets a
+   shim allocate the buffers the reference would have allocated itself. */
+int pn_query_sizes(const pn_desc* desc, pn_sizes* sizes);
+
+/* Validate the descriptor, copy its tables to the device and allocate the state and tape.
+   Replaces the construction of ForwardPNProblem / AdjointPNProblem (pn_problem.jl:72-136). */
+int pn_create(const pn_desc* desc, pn_handle** out);
+
+/* Forward march and intensities.  rho: [n_rho] component densities on all 8 class grids
+   (component_densities(m, gspec), pn_material_utils.jl:74-83); noa: [n_eee_cells][n_e] number of
+   atoms (x_ray_intensities.jl:43-55); acs: [n_eee_cells][n_r] absorption factors
+   (x_ray_intensities.jl:115-128); intensities: [n_r] out.  Keeps the forward tape on the device
+   for a following pn_adjoint.  Replaces calc_intensities (pn_intensities.jl:325-351). */
+int pn_forward(pn_handle* h, const double* rho, const double* noa, const double* acs,
+               double* intensities);
+
+/* Adjoint march for cotangent intensities_bar [n_r] after pn_forward on the same handle.
+   Outputs (overwritten): rho_bar [n_rho] (zero on ghost points and inactive classes),
+   noa_bar [n_eee_cells][n_e], acs_bar [n_eee_cells][n_r].  Replaces the body of
+   calc_intensities_pullback up to the material pullbacks (pn_intensities.jl:381-405). */
+int pn_adjoint(pn_handle* h, const double* intensities_bar, double* rho_bar, double* noa_bar,
+               double* acs_bar);
+
+/* Same as pn_forward / pn_adjoint with device pointers (device-resident inputs and outputs),
+   ordered on the CUDA stream `stream` (a cudaStream_t, NULL for the legacy default stream). */
+int pn_forward_device(pn_handle* h, const double* rho, const double* noa, const double* acs,
+                      double* intensities, void* stream);
+int pn_adjoint_device(pn_handle* h, const double* intensities_bar, double* rho_bar,
+                      double* noa_bar, double* acs_bar, void* stream);
+
+/* x-ray generation field: out [n_eee_cells][n_r] = sum over steps of u_eee[cell,0] dE sigma_r w
+   (pn_intensities.jl:189-212 with integrate_step_and_add_x_ray_generation!,
+   x_ray_intensities.jl:226-234). */
+int pn_generation_field(pn_handle* h, const double* rho, double* field);
+
+/* One forward energy step of the state held by the handle, in place (step_pn!,
+   pn_intensities.jl:16-22): uses the coefficients of forward step `step` (0-based).
+   pn_set_state / pn_get_state move the state in the reference's layout: [n_state] doubles,
+   classes concatenated, moments fastest.  Ghost points are updated as the reference updates
+   them, except points that are ghosts along two or more axes and the classes odd in a singleton
+   axis: no stencil reads those, and they are returned as zero. */
+int pn_set_state(pn_handle* h, const double* rho, const double* state);
+int pn_step(pn_handle* h, int32_t step);
+int pn_get_state(pn_handle* h, double* state);
+
+void pn_destroy(pn_handle* h);
+
+/* Human-readable description of the last error on this handle (or of the last failed
+   pn_create / pn_query_sizes in this thread when h is NULL).  Never NULL. */
+const char* pn_last_error(const pn_handle* h);
+
+/* ABI version and the compiled P_N orders (bit N set when order N is available). */
+int32_t pn_abi_version(void);
+int64_t pn_compiled_orders(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PNEPMA_H */

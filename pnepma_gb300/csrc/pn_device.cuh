@@ -1,0 +1,493 @@
+// pn_device.cuh -- device kernels of the PN-moment energy march (sm_103a).
+//
+// One launch advances the classes of one parity by one StaRMAP sub-step (starmap/src/solver.jl:
+// 171-196): for every target cell it
+//   1. (face cells only) evaluates the ghost values of the neighbouring class that the cell's
+//      stencil reads, from the cell's own old values and the neighbour's interior value
+//      (apply_boundary_source!/zero!, starmap/src/boundary_conditions.jl:67-102), and stores them;
+//   2. forms du = sum_d A_d (u_r - u_l) / h_d over the active axes with the generated sparse
+//      stencils (kernel!/matmuldiff!, starmap/src/solver_core.jl:59-69,108-137);
+//   3. applies du = ((Q - du) - C u) / S * phi1(-C/S dt) with S = sum_e rho_e s_e and
+//      C_l = sum_e rho_e c_{e,l} formed on the fly from the per-step tables (weighted_sum!,
+//      pn_solver/pn_problem.jl:213-249; right_hand_side!, solver_core.jl:92-106) and
+//   4. writes u + dt du (update!, solver.jl:149-168).
+// A ghost value that lies outside the grid along exactly one axis is read by exactly one target
+// cell -- the cell at that face of the switched class -- so the thread that owns that cell
+// computes it, with no other thread reading or writing it during the launch.  Ghosts along two or
+// more axes are read by no stencil and are not maintained.
+//
+// The adjoint density kernel (integrate_adjoint_densities!, pn_solver/pn_intensities.jl:129-164)
+// evaluates du of a tape state for every class (plain right-hand side, no exponential factor) and
+// accumulates rho_bar[e] += sum_m lambda_m (s_e du_m + c_{e,l(m)} u_m) dvol dE w, plus the eee
+// pullbacks of the intensity integral (integrate_step_and_add_pullback!,
+// pn_solver/x_ray_intensities.jl:193-223).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "generated/pn_stencils.cuh"
+
+namespace pn {
+
+constexpr int MAXE = 4;     // elements per solve
+constexpr int MAXR = 8;     // x-ray lines per solve
+constexpr int MAXSEG = 16;  // work segments per launch
+constexpr int BLOCK = 128;  // threads per block
+
+struct Geom {
+  int n[3];        // points per axis (ghosts included)
+  int px;          // x pitch in elements
+  int nm;          // moments
+  int pad;
+  long long ms;    // moment stride in elements (px * ny * nz)
+};
+
+// A contiguous range of blocks working on one target class: either an inner box (cells whose
+// stencil needs no ghost) tiled tile_x x (128 / tile_x), or a list of face cells.
+struct Seg {
+  int cls;
+  int kind;        // 0 = box, 1 = face list
+  int block0;
+  int nblocks;
+  int lo[3];
+  int ext[3];
+  int tiles_x, tiles_y;
+  int tile_x;
+  int n_face;
+  const int* faces;  // packed i | j << 11 | k << 22
+};
+
+__host__ __device__ inline int pack_cell(int i, int j, int k) { return i | (j << 11) | (k << 22); }
+
+template <class T, int N>
+struct SubArgs {
+  Geom g[8];
+  T* rd[8];                   // read pointer per class (from-classes, own old values, ghosts)
+  T* wr[8];                   // write pointer per class (targets)
+  const T* rho[8];            // [e][z][y][x] with the class geometry
+  const double* bmat[3][8];   // boundary blocks n_f x n_t (row-major)
+  const double* beam[8];      // right-x-face source [z][y][m] (classes odd in x)
+  int act[3];                 // active axes
+  int ne, nr;
+  int nseg;
+  int adjoint_source;         // add Q on eee moment 0
+  T dt;
+  double bc;                  // beam energy weight of this step (forward source)
+  double scale_g;             // multiplier of the beam source (power of two)
+  T s[MAXE];
+  T c[MAXE][N + 1];
+  // adjoint source on eee moment 0: Q = -sum_r sigma_r ACS NOA ibar_r
+  const double* acs;          // [cell][r], eee cells
+  const double* noa;          // [cell][e]
+  const double* ibar;         // [r] (device)
+  int xel[MAXR];
+  double sig_src[MAXR];
+  // intensity partial sums of the new eee moment 0 (forward, even sub-step)
+  const double* wint;         // [cell][r] = ACS * NOA
+  double* partial;            // [block][r]
+  Seg seg[MAXSEG];
+  T tab[Ord<N>::n_tab];       // advection nnz values divided by the grid step
+};
+
+template <class T, int N>
+struct IntArgs {
+  Geom g[8];
+  T* u[8];                    // tape state (ghosts rewritten)
+  const T* lam[8];            // adjoint state
+  const T* rho[8];
+  double* rbar[8];            // rho_bar per class [e][z][y][x]
+  const double* bmat[3][8];   // forward boundary blocks
+  const double* beam[8];
+  int act[3];
+  int ne, nr;
+  int nseg;
+  double bc;
+  double scale_g;
+  double wfac;                // dvol * dE * w
+  T s[MAXE];
+  T c[MAXE][N + 1];
+  const double* acs;
+  const double* noa;
+  const double* ibar;
+  double* acs_bar;
+  double* noa_bar;
+  int xel[MAXR];
+  double coef[MAXR];          // dE * dvol * sigma_r * w   (times ibar_r in the kernel)
+  Seg seg[MAXSEG];
+  T tab[Ord<N>::n_tab];
+};
+
+// --------------------------------------------------------------------------------------------
+// small helpers
+// --------------------------------------------------------------------------------------------
+__device__ __forceinline__ double phi1(double c) {
+  // expm1div (solver_core.jl:38-44): the same threshold, Taylor form and (exp(c) - 1) / c
+  if (fabs(c) <= 0.0002) return 1.0 + 0.5 * c + 1.0 / 6.0 * (c * c);
+  return (exp(c) - 1.0) / c;
+}
+
+__device__ __forceinline__ float phi1(float c) {
+  // FP32: exp(c) - 1 cancels for small |c|; expm1f keeps full relative accuracy
+  if (fabsf(c) <= 1e-3f) return 1.0f + c * (0.5f + c * (1.0f / 6.0f));
+  return expm1f(c) / c;
+}
+
+template <class T>
+__device__ __forceinline__ T recip(T x) { return T(1) / x; }
+
+__device__ __forceinline__ bool locate(const Seg* seg, int nseg, int b, int tid, int& s, int& i, int& j,
+                                       int& k) {
+  s = 0;
+  while (s + 1 < nseg && b >= seg[s + 1].block0) ++s;
+  const Seg& g = seg[s];
+  const int lb = b - g.block0;
+  if (g.kind == 0) {
+    const int ty = BLOCK / g.tile_x;
+    const int bx = lb % g.tiles_x;
+    const int rest = lb / g.tiles_x;
+    const int by = rest % g.tiles_y;
+    const int bz = rest / g.tiles_y;
+    const int li = bx * g.tile_x + tid % g.tile_x;
+    const int lj = by * ty + tid / g.tile_x;
+    if (li >= g.ext[0] || lj >= g.ext[1] || bz >= g.ext[2]) return false;
+    i = g.lo[0] + li;
+    j = g.lo[1] + lj;
+    k = g.lo[2] + bz;
+    return true;
+  }
+  const int f = lb * BLOCK + tid;
+  if (f >= g.n_face) return false;
+  const int p = g.faces[f];
+  i = p & 2047;
+  j = (p >> 11) & 2047;
+  k = (p >> 22) & 1023;
+  return true;
+}
+
+__device__ __forceinline__ long long lin(const Geom& g, int i, int j, int k) {
+  return ((long long)k * g.n[1] + j) * g.px + i;
+}
+
+__device__ __forceinline__ long long eee_cell(const Geom& g, int i, int j, int k) {
+  return ((long long)k * g.n[1] + j) * g.n[0] + i;
+}
+
+// Ghost of class F = switch(C, d) next to target cell (i,j,k) of class C (C even along d, cell on
+// a face along d).  Writes the ghost into F's storage.  `left` selects the face at index 0.
+template <class T, int N, int C, int D>
+__device__ __forceinline__ void ghost_fill(T* const* rd, const Geom* g, const double* const (*bmat)[8],
+                                           const double* const* beam, double bc_scaled, bool source,
+                                           int i, int j, int k, bool left) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nt = Ord<N>::n(C);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nt == 0 || nf == 0) {
+    return;
+  } else {
+    const Geom& gt = g[C];
+    const Geom& gf = g[F];
+    const T* ut = rd[C] + lin(gt, i, j, k);
+    T v[nt];
+#pragma unroll
+    for (int m = 0; m < nt; ++m) v[m] = ut[m * gt.ms];
+    int c[3] = {i, j, k};
+    int cg[3] = {i, j, k};
+    int ci[3] = {i, j, k};
+    if (left) {
+      cg[D] = 0;
+      ci[D] = 1;
+    } else {
+      cg[D] = c[D] + 1;
+      ci[D] = c[D];
+    }
+    T* fg = rd[F] + lin(gf, cg[0], cg[1], cg[2]);
+    const T* fi = rd[F] + lin(gf, ci[0], ci[1], ci[2]);
+    const double* B = bmat[D][F];
+    const bool src = source && D == 0 && !left;
+    const double* bm = src ? beam[F] + ((long long)k * gf.n[1] + j) * nf : nullptr;
+#pragma unroll 1
+    for (int r = 0; r < nf; ++r) {
+      T bv = T(0);
+#pragma unroll
+      for (int q = 0; q < nt; ++q) bv = fma(T(B[r * nt + q]), v[q], bv);
+      const T gval = src ? T(bm[r] * bc_scaled) : T(0);
+      const T interior = fi[r * gf.ms];
+      const T gh = left ? T(2) * (gval - bv) - interior : T(2) * (bv + gval) - interior;
+      fg[r * gf.ms] = gh;
+    }
+  }
+}
+
+template <class T, int N, int C>
+__device__ __forceinline__ void ghosts_for_cell(T* const* rd, const Geom* g, const int* act,
+                                                const double* const (*bmat)[8], const double* const* beam,
+                                                double bc_scaled, bool source, int i, int j, int k) {
+  const int c3[3] = {i, j, k};
+  if (act[0] && !((C >> 2) & 1)) {
+    if (c3[0] == 0) ghost_fill<T, N, C, 0>(rd, g, bmat, beam, bc_scaled, source, i, j, k, true);
+    if (c3[0] == g[C].n[0] - 1) ghost_fill<T, N, C, 0>(rd, g, bmat, beam, bc_scaled, source, i, j, k, false);
+  }
+  if (act[1] && !((C >> 1) & 1)) {
+    if (c3[1] == 0) ghost_fill<T, N, C, 1>(rd, g, bmat, beam, bc_scaled, source, i, j, k, true);
+    if (c3[1] == g[C].n[1] - 1) ghost_fill<T, N, C, 1>(rd, g, bmat, beam, bc_scaled, source, i, j, k, false);
+  }
+  if (act[2] && !(C & 1)) {
+    if (c3[2] == 0) ghost_fill<T, N, C, 2>(rd, g, bmat, beam, bc_scaled, source, i, j, k, true);
+    if (c3[2] == g[C].n[2] - 1) ghost_fill<T, N, C, 2>(rd, g, bmat, beam, bc_scaled, source, i, j, k, false);
+  }
+}
+
+// acc[m] += sum over active axes of A_d[C] (f_r - f_l) / h_d  (sign flipped for the adjoint)
+template <class T, int N, int C, int D, bool NEG, class Tab>
+__device__ __forceinline__ void stencil_axis(T* acc, T* const* rd, const Geom* g, int i, int j, int k,
+                                             const Tab& tab) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nf == 0 || Ord<N>::n(C) == 0) {
+    return;
+  } else {
+    const Geom& gf = g[F];
+    int r3[3] = {i, j, k};
+    int l3[3] = {i, j, k};
+    if ((C >> (2 - D)) & 1) {  // odd target: even neighbour at i (right) and i - 1 (left)
+      l3[D] -= 1;
+    } else {                   // even target: odd neighbour at i + 1 (right) and i (left)
+      r3[D] += 1;
+    }
+    const T* fr = rd[F] + lin(gf, r3[0], r3[1], r3[2]);
+    const T* fl = rd[F] + lin(gf, l3[0], l3[1], l3[2]);
+    const long long ms = gf.ms;
+    auto diff = [&](int q) -> T {
+      const T a = fr[q * ms];
+      const T b = fl[q * ms];
+      return NEG ? (b - a) : (a - b);
+    };
+    constexpr int off = Ord<N>::off(C, D);
+    auto coef = [&](int kk, double) -> T { return tab[off + kk]; };
+    Adv<N, C, D>::template apply<T>(acc, diff, coef);
+  }
+}
+
+// --------------------------------------------------------------------------------------------
+// sub-step kernel
+// --------------------------------------------------------------------------------------------
+template <class T, int N, int C, bool ADJ>
+__device__ __forceinline__ void substep_cell(const SubArgs<T, N>& a, int i, int j, int k, bool face,
+                                             double* part) {
+  constexpr int n = Ord<N>::n(C);
+  if constexpr (n == 0) {
+    return;
+  } else {
+    T* const* rd = a.rd;
+    if (face) ghosts_for_cell<T, N, C>(const_cast<T* const*>(rd), a.g, a.act, a.bmat, a.beam,
+                                       a.bc * a.scale_g, !ADJ, i, j, k);
+    T acc[n];
+#pragma unroll
+    for (int m = 0; m < n; ++m) acc[m] = T(0);
+    if (a.act[0]) stencil_axis<T, N, C, 0, ADJ>(acc, rd, a.g, i, j, k, a.tab);
+    if (a.act[1]) stencil_axis<T, N, C, 1, ADJ>(acc, rd, a.g, i, j, k, a.tab);
+    if (a.act[2]) stencil_axis<T, N, C, 2, ADJ>(acc, rd, a.g, i, j, k, a.tab);
+
+    const Geom& gt = a.g[C];
+    const long long p = lin(gt, i, j, k);
+    const T* rho = a.rho[C] + p;
+    T rr[MAXE];
+    T S = T(0);
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+      rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
+      S = fma(rr[e], a.s[e], S);
+    }
+    const T invS = recip(S);
+    constexpr unsigned mask = Ord<N>::deg_mask(C);
+    T Cl[N + 1];
+    T ph[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) {
+      if ((mask >> l) & 1u) {
+        T cc = T(0);
+#pragma unroll
+        for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
+        Cl[l] = cc;
+        ph[l] = phi1(-cc * invS * a.dt);
+      } else {
+        Cl[l] = T(0);
+        ph[l] = T(1);
+      }
+    }
+    const T* uo = a.rd[C] + p;
+    T* un = a.wr[C] + p;
+    T q0 = T(0);
+    if constexpr (ADJ && C == 0) {
+      if (a.adjoint_source) {
+        const long long ce = eee_cell(gt, i, j, k);
+        double q = 0.0;
+        for (int r = 0; r < a.nr; ++r)
+          q = q - a.sig_src[r] * a.acs[ce * a.nr + r] * a.noa[ce * a.ne + a.xel[r]] * a.ibar[r];
+        q0 = T(q);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const int l = degree_of<N, C>(m);
+      const T u = uo[m * gt.ms];
+      const T q = (m == 0) ? q0 : T(0);
+      const T num = (q - acc[m]) - Cl[l] * u;
+      const T du = num * invS * ph[l];
+      const T unew = u + a.dt * du;
+      un[m * gt.ms] = unew;
+      if constexpr (C == 0 && !ADJ) {
+        if (m == 0 && part != nullptr) {
+          const long long ce = eee_cell(gt, i, j, k);
+#pragma unroll
+          for (int r = 0; r < MAXR; ++r)
+            if (r < a.nr) part[r] += a.wint[ce * a.nr + r] * double(unew);
+        }
+      }
+    }
+  }
+}
+
+template <class T, int N, bool ADJ>
+__global__ void __launch_bounds__(BLOCK) substep_kernel(const __grid_constant__ SubArgs<T, N> a) {
+  int s, i, j, k;
+  const bool ok = locate(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k);
+  const int cls = a.seg[s].cls;
+  const bool face = a.seg[s].kind == 1;
+  double part[MAXR];
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
+  double* pp = (a.partial != nullptr) ? part : nullptr;
+  if (ok) {
+    switch (cls) {
+      case 0: substep_cell<T, N, 0, ADJ>(a, i, j, k, face, pp); break;
+      case 1: substep_cell<T, N, 1, ADJ>(a, i, j, k, face, pp); break;
+      case 2: substep_cell<T, N, 2, ADJ>(a, i, j, k, face, pp); break;
+      case 3: substep_cell<T, N, 3, ADJ>(a, i, j, k, face, pp); break;
+      case 4: substep_cell<T, N, 4, ADJ>(a, i, j, k, face, pp); break;
+      case 5: substep_cell<T, N, 5, ADJ>(a, i, j, k, face, pp); break;
+      case 6: substep_cell<T, N, 6, ADJ>(a, i, j, k, face, pp); break;
+      default: substep_cell<T, N, 7, ADJ>(a, i, j, k, face, pp); break;
+    }
+  }
+  if (a.partial != nullptr) {
+    // block sum of the intensity partials, fixed order -> deterministic
+    __shared__ double red[BLOCK / 32][MAXR];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+      if (r < a.nr) {
+        double v = part[r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][r] = v;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < a.nr) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+      a.partial[(long long)blockIdx.x * a.nr + threadIdx.x] = v;
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------------
+// adjoint density kernel
+// --------------------------------------------------------------------------------------------
+template <class T, int N, int C>
+__device__ __forceinline__ void integrate_cell(const IntArgs<T, N>& a, int i, int j, int k, bool face) {
+  constexpr int n = Ord<N>::n(C);
+  if constexpr (n == 0) {
+    return;
+  } else {
+    if (face) ghosts_for_cell<T, N, C>(a.u, a.g, a.act, a.bmat, a.beam, a.bc * a.scale_g, true, i, j, k);
+    T acc[n];
+#pragma unroll
+    for (int m = 0; m < n; ++m) acc[m] = T(0);
+    if (a.act[0]) stencil_axis<T, N, C, 0, false>(acc, a.u, a.g, i, j, k, a.tab);
+    if (a.act[1]) stencil_axis<T, N, C, 1, false>(acc, a.u, a.g, i, j, k, a.tab);
+    if (a.act[2]) stencil_axis<T, N, C, 2, false>(acc, a.u, a.g, i, j, k, a.tab);
+    const Geom& gt = a.g[C];
+    const long long p = lin(gt, i, j, k);
+    const T* rho = a.rho[C] + p;
+    T rr[MAXE];
+    T S = T(0);
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+      rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
+      S = fma(rr[e], a.s[e], S);
+    }
+    const T invS = recip(S);
+    constexpr unsigned mask = Ord<N>::deg_mask(C);
+    T Cl[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) {
+      T cc = T(0);
+      if ((mask >> l) & 1u) {
+#pragma unroll
+        for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
+      }
+      Cl[l] = cc;
+    }
+    const T* uu = a.u[C] + p;
+    const T* la = a.lam[C] + p;
+    // P = sum_m lam_m du_m ; R_l = sum_{m: l(m) = l} lam_m u_m
+    T P = T(0);
+    T R[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) R[l] = T(0);
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const int l = degree_of<N, C>(m);
+      const T u = uu[m * gt.ms];
+      const T lm = la[m * gt.ms];
+      const T du = (-acc[m] - Cl[l] * u) * invS;
+      P = fma(lm, du, P);
+      R[l] = fma(lm, u, R[l]);
+    }
+    double* rb = a.rbar[C] + p;
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+      if (e < a.ne) {
+        double v = double(a.s[e]) * double(P);
+#pragma unroll
+        for (int l = 0; l <= N; ++l)
+          if ((mask >> l) & 1u) v += double(a.c[e][l]) * double(R[l]);
+        rb[e * gt.ms] += v * a.wfac;
+      }
+    }
+    if constexpr (C == 0) {
+      const long long ce = eee_cell(gt, i, j, k);
+      const double u0 = double(uu[0]);
+      for (int r = 0; r < a.nr; ++r) {
+        const double cr = a.coef[r] * a.ibar[r];
+        const int el = a.xel[r];
+        a.acs_bar[ce * a.nr + r] += a.noa[ce * a.ne + el] * u0 * cr;
+        a.noa_bar[ce * a.ne + el] += a.acs[ce * a.nr + r] * u0 * cr;
+      }
+    }
+  }
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ IntArgs<T, N> a) {
+  int s, i, j, k;
+  if (!locate(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k)) return;
+  const int cls = a.seg[s].cls;
+  const bool face = a.seg[s].kind == 1;
+  switch (cls) {
+    case 0: integrate_cell<T, N, 0>(a, i, j, k, face); break;
+    case 1: integrate_cell<T, N, 1>(a, i, j, k, face); break;
+    case 2: integrate_cell<T, N, 2>(a, i, j, k, face); break;
+    case 3: integrate_cell<T, N, 3>(a, i, j, k, face); break;
+    case 4: integrate_cell<T, N, 4>(a, i, j, k, face); break;
+    case 5: integrate_cell<T, N, 5>(a, i, j, k, face); break;
+    case 6: integrate_cell<T, N, 6>(a, i, j, k, face); break;
+    default: integrate_cell<T, N, 7>(a, i, j, k, face); break;
+  }
+}
+
+}  // namespace pn
