@@ -84,7 +84,9 @@ typedef struct pn_desc {
   int32_t n_xrays;           /* n_r */
   int32_t n_steps;
   int32_t precision;         /* pn_precision */
-  int32_t checkpoint_stride; /* adjoint tape: 0 keeps every state, K > 0 keeps every K-th and recomputes */
+  int32_t checkpoint_stride; /* adjoint tape: K >= 1 keeps every K-th state and recomputes the rest
+                                (1 keeps all); 0 keeps all while that fits in 2 GiB, else every
+                                ceil(sqrt(n_steps))-th */
   int32_t flags;             /* pn_flags */
   int32_t reserved;
   double  h[3];              /* grid steps (1.0 on a singleton axis) */
@@ -184,6 +186,17 @@ int pn_generation_field(pn_handle* h, const double* rho, double* field);
 int pn_set_state(pn_handle* h, const double* rho, const double* state);
 int pn_step(pn_handle* h, int32_t step);
 int pn_get_state(pn_handle* h, double* state);
+
+/* Facts about a created handle (diagnostics; no counterpart in the reference). */
+typedef struct pn_handle_info {
+  int32_t checkpoint_stride;   /* stride in use (1 = every state kept) */
+  int32_t precision;
+  int64_t device_bytes;        /* device memory held by the handle */
+  int64_t forward_kernels;     /* kernel launches of one pn_forward(_device) call */
+  int64_t adjoint_kernels;     /* kernel launches of one pn_adjoint(_device) call */
+} pn_handle_info;
+
+int pn_query_handle(const pn_handle* h, pn_handle_info* info);
 
 void pn_destroy(pn_handle* h);
 

@@ -21,7 +21,13 @@ STATUS = {
     -5: "PN_ERR_DIVERGED", -6: "PN_ERR_TIMEOUT", -7: "PN_ERR_CUDA", -8: "PN_ERR_STATE", -9: "PN_ERR_NO_DEVICE",
 }
 
-EXPORTS = ("pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
+class PnHandleInfo(ctypes.Structure):
+    _fields_ = [("checkpoint_stride", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("device_bytes", ctypes.c_int64), ("forward_kernels", ctypes.c_int64),
+                ("adjoint_kernels", ctypes.c_int64)]
+
+
+EXPORTS = ("pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
            "pn_abi_version", "pn_compiled_orders")
 
@@ -54,6 +60,8 @@ def lib():
         L.pn_set_state.argtypes = [P, P, P]
         L.pn_step.argtypes = [P, ctypes.c_int32]
         L.pn_get_state.argtypes = [P, P]
+        L.pn_query_handle.argtypes = [P, ctypes.POINTER(PnHandleInfo)]
+        L.pn_query_handle.restype = ctypes.c_int
         L.pn_destroy.argtypes = [P]
         L.pn_destroy.restype = None
         L.pn_last_error.argtypes = [P]
@@ -103,6 +111,11 @@ class Handle:
     def _check(self, rc):
         if rc:
             raise PnError(rc, lib().pn_last_error(self._h).decode())
+
+    def info(self) -> PnHandleInfo:
+        out = PnHandleInfo()
+        self._check(lib().pn_query_handle(self._h, ctypes.byref(out)))
+        return out
 
     def close(self):
         if getattr(self, "_h", None):

@@ -88,7 +88,7 @@ int pn_query_sizes(const pn_desc* desc, pn_sizes* sizes) {
     const long long esize = desc->precision == PN_FP32 ? 4 : 8;
     const long long slot = L.slot_elems * esize;
     int K = desc->checkpoint_stride;
-    if (K <= 0) K = ((long long)(L.ns + 1) * slot <= (4LL << 30)) ? 1 : (int)std::ceil(std::sqrt((double)L.ns));
+    if (K <= 0) K = ((long long)(L.ns + 1) * slot <= (2LL << 30)) ? 1 : (int)std::ceil(std::sqrt((double)L.ns));
     if (K > L.ns) K = L.ns;
     const long long nck = L.ns / K + 1 + ((L.ns % K) ? 1 : 0);
     const long long nwork = K - 1 > 2 ? K - 1 : 2;
@@ -175,6 +175,12 @@ int pn_step(pn_handle* h, int32_t step) {
 int pn_get_state(pn_handle* h, double* state) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
   PN_GUARD(h->s->get_state(state))
+}
+
+int pn_query_handle(const pn_handle* h, pn_handle_info* info) {
+  if (!h || !h->s || !info) return fail("handle or info is NULL", PN_ERR_INVALID);
+  h->s->info(info);
+  return PN_OK;
 }
 
 void pn_destroy(pn_handle* h) {

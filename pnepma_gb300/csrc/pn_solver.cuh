@@ -93,6 +93,7 @@ class Solver : public SolverBase {
   int* xel_d = nullptr;
   int* faces_d = nullptr;
   double* stage_d = nullptr;     // caller-layout staging, max(n_rho, n_state) doubles
+  double* out_mul_d = nullptr;   // factor that undoes the FP32 scaling of the adjoint outputs
   int* flag_d = nullptr;
   const double* bmat_f[3][8] = {{nullptr}};
   const double* bmat_a[3][8] = {{nullptr}};
@@ -116,6 +117,24 @@ class Solver : public SolverBase {
   }
 
   long long device_bytes() const override { return bytes; }
+
+  long long n_launch = 0;            // kernel launches recorded since the counter was reset
+  long long fwd_kernels = 0, adj_kernels = 0;
+
+  int n_active() const {
+    int n = 0;
+    for (int c = 0; c < 8; ++c) n += L.active[c] ? 1 : 0;
+    return n;
+  }
+
+  void info(pn_handle_info* out) const override {
+    out->checkpoint_stride = K;
+    out->precision = sizeof(T) == 4 ? PN_FP32 : PN_FP64;
+    out->device_bytes = bytes;
+    // graph kernels + per-call layout kernels
+    out->forward_kernels = fwd_kernels + n_active() + (L.nr ? 1 : 0);
+    out->adjoint_kernels = adj_kernels + n_active() + 1 + (L.nr ? 2 : 1);
+  }
 
   template <class U>
   int alloc(U*& p, long long n) {
@@ -222,7 +241,7 @@ class Solver : public SolverBase {
     K = d->checkpoint_stride;
     if (K < 0) { err = "checkpoint_stride must be >= 0"; return PN_ERR_INVALID; }
     if (K == 0) {
-      const long long budget = 4LL << 30;
+      const long long budget = 2LL << 30;
       K = ((long long)(ns + 1) * slot_bytes <= budget) ? 1 : std::max(2, (int)std::ceil(std::sqrt((double)ns)));
     }
     if (K > ns) K = ns;
@@ -267,6 +286,7 @@ class Solver : public SolverBase {
     if ((rc = alloc(xel_d, std::max(nr, 1)))) return rc;
     if ((rc = alloc(stage_d, std::max(L.n_rho, L.n_state)))) return rc;
     if ((rc = alloc(flag_d, 1))) return rc;
+    if ((rc = alloc(out_mul_d, 1))) return rc;
     PN_CUDA(cudaMemsetAsync(slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems, stream));
     PN_CUDA(cudaMemsetAsync(sstate, 0, sizeof(T) * (size_t)L.slot_elems, stream));
     PN_CUDA(cudaMemsetAsync(rho_d, 0, sizeof(T) * (size_t)L.rho_elems, stream));
@@ -291,6 +311,8 @@ class Solver : public SolverBase {
     }
     if ((rc = build_segments())) return rc;
     PN_CUDA(cudaStreamSynchronize(stream));
+    if ((rc = capture(g_fwd, true))) return rc;
+    if ((rc = capture(g_adj, false))) return rc;
     return PN_OK;
   }
 
@@ -434,6 +456,7 @@ class Solver : public SolverBase {
     else
       substep_kernel<T, N, false><<<nb, BLOCK, 0, stream>>>(a);
     PN_CUDA(cudaGetLastError());
+    ++n_launch;
     return PN_OK;
   }
 
@@ -475,6 +498,7 @@ class Solver : public SolverBase {
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
     integrate_kernel<T, N><<<nblk_all, BLOCK, 0, stream>>>(a);
     PN_CUDA(cudaGetLastError());
+    ++n_launch;
     return PN_OK;
   }
 
@@ -519,6 +543,7 @@ class Solver : public SolverBase {
       final_intensity_kernel<<<1, 32, 0, stream>>>(integral_d, sigma_d, weight_d, I_d, L.ns + 1, L.nr, dE, dvol,
                                                    1.0 / scale_g);
       PN_CUDA(cudaGetLastError());
+      n_launch += 2;
     }
     return PN_OK;
   }
@@ -552,6 +577,7 @@ class Solver : public SolverBase {
 
   int capture(cudaGraphExec_t& exec, bool fwd) {
     cudaGraph_t graph = nullptr;
+    n_launch = 0;
     PN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = fwd ? record_forward() : record_adjoint();
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
@@ -565,6 +591,7 @@ class Solver : public SolverBase {
     }
     e = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
+    (fwd ? fwd_kernels : adj_kernels) = n_launch;
     if (e != cudaSuccess) {
       err = std::string("graph instantiate: ") + cudaGetErrorString(e);
       return PN_ERR_CUDA;
@@ -626,29 +653,23 @@ class Solver : public SolverBase {
     if ((L.nr && !ibar) || !rho_bar || !noa_bar || (L.nr && !acs_bar)) { err = "NULL buffer"; return PN_ERR_INVALID; }
     if (!g_adj && (rc = capture(g_adj, false))) return rc;
     cudaStream_t s = st ? st : stream;
-    // scale of the cotangent (FP32 only): keep the adjoint source near unity
-    double sc_i = 1.0;
-    double ib[MAXR] = {0};
+    double* mul_d = out_mul_d;
     if (L.nr) {
-      if (dev)
-        PN_CUDA(cudaMemcpyAsync(ib, ibar, sizeof(double) * L.nr, cudaMemcpyDeviceToHost, s));
-      else
-        std::memcpy(ib, ibar, sizeof(double) * L.nr);
-      if (dev) PN_CUDA(cudaStreamSynchronize(s));
-      if (sizeof(T) == 4) {
-        double m = 0.0, smax = 0.0;
-        for (int r = 0; r < L.nr; ++r) m = std::max(m, std::fabs(ib[r]));
-        for (double v : adj_src_sigma) smax = std::max(smax, std::fabs(v));
-        // the cotangent enters with sigma * ACS * NOA; ACS <= 1, NOA ~ 1e23
-        const double q = m * smax * 1e23;
-        if (q > 0.0 && std::isfinite(q)) sc_i = std::ldexp(1.0, -(int)std::lround(std::log2(q)));
+      const double* src = ibar;
+      if (!dev) {
+        PN_CUDA(cudaMemcpyAsync(stage_d, ibar, sizeof(double) * L.nr, cudaMemcpyHostToDevice, s));
+        src = stage_d;
       }
-      for (int r = 0; r < L.nr; ++r) ib[r] *= sc_i;
-      PN_CUDA(cudaMemcpyAsync(ibar_d, ib, sizeof(double) * L.nr, cudaMemcpyHostToDevice, s));
+      double smax = 0.0;
+      for (double v : adj_src_sigma) smax = std::max(smax, std::fabs(v));
+      // the cotangent enters the adjoint source with sigma * ACS * NOA (ACS <= 1, NOA ~ 1e23)
+      prep_ibar_kernel<<<1, 32, 0, s>>>(src, ibar_d, mul_d, L.nr, smax * 1e23, sizeof(T) == 4 ? 1 : 0, scale_g);
+      PN_CUDA(cudaGetLastError());
+    } else {
+      const double one = 1.0 / scale_g;
+      PN_CUDA(cudaMemcpyAsync(mul_d, &one, sizeof(double), cudaMemcpyHostToDevice, s));
     }
-    scale_i = sc_i;
     PN_CUDA(cudaGraphLaunch(g_adj, s));
-    const double inv = 1.0 / (scale_g * scale_i);
     // rho_bar to the caller layout (zeros on ghost points and inactive classes)
     PN_CUDA(cudaMemsetAsync(stage_d, 0, sizeof(double) * (size_t)L.n_rho, s));
     for (int c = 0; c < 8; ++c) {
@@ -656,12 +677,12 @@ class Solver : public SolverBase {
       const long long n = L.npts[c] * L.ne;
       pack_points_kernel<double><<<grid_for(n), 256, 0, s>>>(rbar_d + L.rho_off[c], stage_d + L.off_rho[c],
                                                               L.shape[c][0], L.shape[c][1], L.shape[c][2], L.px[c],
-                                                              L.ne, L.ms[c], inv, 0, 0, 0, 0, 0, 0, 0);
+                                                              L.ne, L.ms[c], 1.0, 0, 0, 0, 0, 0, 0, 0, mul_d);
       PN_CUDA(cudaGetLastError());
     }
     const long long ncell = L.n_eee_cells;
-    scale_kernel<<<grid_for(ncell * L.ne), 256, 0, s>>>(noa_bar_d, ncell * L.ne, inv);
-    if (L.nr) scale_kernel<<<grid_for(ncell * L.nr), 256, 0, s>>>(acs_bar_d, ncell * L.nr, inv);
+    scale_kernel<<<grid_for(ncell * L.ne), 256, 0, s>>>(noa_bar_d, ncell * L.ne, 1.0, mul_d);
+    if (L.nr) scale_kernel<<<grid_for(ncell * L.nr), 256, 0, s>>>(acs_bar_d, ncell * L.nr, 1.0, mul_d);
     PN_CUDA(cudaGetLastError());
     const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     PN_CUDA(cudaMemcpyAsync(rho_bar, stage_d, sizeof(double) * (size_t)L.n_rho, kind, s));
@@ -737,7 +758,7 @@ class Solver : public SolverBase {
                                                              L.shape[c][0], L.shape[c][1], L.shape[c][2], L.px[c],
                                                              L.nm[c], L.ms[c], 1.0 / scale_g, 1, class_bit(c, 0),
                                                              class_bit(c, 1), class_bit(c, 2), L.act[0], L.act[1],
-                                                             L.act[2]);
+                                                             L.act[2], nullptr);
       PN_CUDA(cudaGetLastError());
     }
     PN_CUDA(cudaMemcpyAsync(state, stage_d, sizeof(double) * (size_t)L.n_state, cudaMemcpyDeviceToHost, stream));

@@ -22,6 +22,7 @@ class SolverBase {
   virtual int step(int i) = 0;
   virtual int get_state(double* state) = 0;
   virtual long long device_bytes() const = 0;
+  virtual void info(pn_handle_info* out) const = 0;
   std::string err;
 };
 

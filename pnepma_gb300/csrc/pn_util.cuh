@@ -26,7 +26,8 @@ static __global__ void unpack_points_kernel(const double* __restrict__ src, T* _
 template <class T>
 static __global__ void pack_points_kernel(const T* __restrict__ src, double* __restrict__ dst, int nx, int ny, int nz,
                                    int px, int nv, long long ms, double mul, int zero_multi_ghost,
-                                   int ox, int oy, int oz, int ax, int ay, int az) {
+                                   int ox, int oy, int oz, int ax, int ay, int az, const double* __restrict__ mulp) {
+  if (mulp) mul *= mulp[0];
   const long long np = (long long)nx * ny * nz;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < np * nv;
        q += (long long)gridDim.x * blockDim.x) {
@@ -95,10 +96,27 @@ static __global__ void generation_kernel(const T* __restrict__ u0, double* __res
   }
 }
 
-// scale a double buffer in place
-static __global__ void scale_kernel(double* __restrict__ x, long long n, double mul) {
+// scale a double buffer in place by mul * (*mulp)
+static __global__ void scale_kernel(double* __restrict__ x, long long n, double mul, const double* __restrict__ mulp) {
+  const double f = mulp ? mul * mulp[0] : mul;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
-    x[q] *= mul;
+    x[q] *= f;
+}
+
+// Copy the cotangent to the device buffer the adjoint graph reads, scaled by a power of two that
+// keeps the FP32 adjoint source near unity (FP64: no scaling), and store the factor that undoes
+// the scaling of the outputs: out_mul[0] = 1 / (scale_g * scale_i).
+static __global__ void prep_ibar_kernel(const double* __restrict__ ibar_in, double* __restrict__ ibar_d,
+                                        double* __restrict__ out_mul, int nr, double src_mag, int fp32,
+                                        double scale_g) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double m = 0.0;
+  for (int r = 0; r < nr; ++r) m = fmax(m, fabs(ibar_in[r]));
+  double sc = 1.0;
+  const double q = m * src_mag;
+  if (fp32 && q > 0.0 && isfinite(q)) sc = ldexp(1.0, -(int)llrint(log2(q)));
+  for (int r = 0; r < nr; ++r) ibar_d[r] = ibar_in[r] * sc;
+  out_mul[0] = 1.0 / (scale_g * sc);
 }
 
 // true when every value is finite (flag stays 1)

@@ -324,15 +324,21 @@ def _matmul_ordered(L: np.ndarray, A: np.ndarray) -> np.ndarray:
     return out
 
 
+@lru_cache(maxsize=None)
+def _boundary_block_cached(N: int, c: int, dim: int, adjoint: bool) -> bytes:
+    L = boundary_L(N, c, dim)
+    A = advection_block(N, c, dim)
+    B = -_matmul_ordered(L.T.copy(), A) if adjoint else _matmul_ordered(L, A)
+    return B.tobytes()
+
+
 def boundary_block(N: int, c: int, dim: int, adjoint: bool = False) -> np.ndarray:
     """``L @ A`` (forward) or ``-L^T @ A`` (adjoint) for a class odd in ``dim``."""
     if not odd_in(c, dim):
         raise ValueError("boundary blocks exist only for classes odd in the boundary axis")
-    L = boundary_L(N, c, dim)
-    A = advection_block(N, c, dim)
-    if adjoint:
-        return -_matmul_ordered(L.T.copy(), A)
-    return _matmul_ordered(L, A)
+    ms = class_moments(N)
+    B = np.frombuffer(_boundary_block_cached(N, c, dim, bool(adjoint)), dtype=np.float64)
+    return B.reshape(len(ms[c]), len(ms[switch(c, dim)])).copy()
 
 
 def boundary_blocks(N: int, adjoint: bool = False) -> list[list[np.ndarray | None]]:
@@ -398,8 +404,20 @@ def vmf_pdf(direction: np.ndarray, mu_dir, kappa: float) -> np.ndarray:
     return kappa / (2 * math.pi * (-math.expm1(-2 * kappa))) * np.exp(kappa * (dot - 1.0))
 
 
-def beam_moments(moments, mu_dir, kappa: float, n_theta: int = 400, n_phi: int = 800) -> np.ndarray:
+def beam_moments(moments, mu_dir, kappa: float, n_theta: int = 200, n_phi: int = 400) -> np.ndarray:
     """``-int Y_m(Omega) vMF(Omega) dOmega`` for each moment (``beam_moments``, pn_matrices.jl:331-338)."""
+    key = (tuple(tuple(m) for m in moments), tuple(float(v) for v in mu_dir), float(kappa), n_theta, n_phi)
+    hit = _BEAM_CACHE.get(key)
+    if hit is None:
+        hit = _beam_moments(moments, mu_dir, kappa, n_theta, n_phi)
+        _BEAM_CACHE[key] = hit
+    return hit.copy()
+
+
+_BEAM_CACHE: dict = {}
+
+
+def _beam_moments(moments, mu_dir, kappa, n_theta, n_phi):
     if not moments:
         return np.zeros(0)
     N = max(l for (l, _k) in moments)

@@ -41,12 +41,17 @@ class Solve:
     label: str = ""
 
     def inputs(self):
-        """(rho, noa, acs) in the C-ABI layout."""
+        """(rho, noa, acs) in the C-ABI layout (memoised on the material: solves that share a
+        material, lines, detector and beam depth share the arrays)."""
         m = self.material
-        rho = m.rho_flat()
-        noa = m.number_of_atoms().reshape(-1, m.n_e)
-        acs = m.absorption(self.x_rays, self.detector, self.problem.beam_position.mean).reshape(-1, len(self.x_rays))
-        return rho, np.ascontiguousarray(noa), np.ascontiguousarray(acs)
+        key = (tuple(self.x_rays), tuple(self.detector), float(self.problem.beam_position.mean[0]))
+        memo = m.__dict__.setdefault("_inputs_memo", {})
+        if key not in memo:
+            rho = m.rho_flat()
+            noa = m.number_of_atoms().reshape(-1, m.n_e)
+            acs = m.absorption(self.x_rays, self.detector, self.problem.beam_position.mean).reshape(-1, len(self.x_rays))
+            memo[key] = (rho, np.ascontiguousarray(noa), np.ascontiguousarray(acs))
+        return memo[key]
 
 
 def min_stopping(material: BoxedMassFraction, problem: ForwardPNProblem, E: float) -> float:
@@ -137,11 +142,16 @@ def config2(seed: int = 2, precision=PN_FP64, stabilise=True, n_positions=20, en
     frac = smooth_fractions(rng, gspec, 3)
     ys = np.linspace(-1 * UM, 1 * UM, n_positions + 2)[1:-1] if n_positions > 1 else [0.0]
     out = []
+    mat = None
     for E in energies:
         for y in ys:
-            out.append(make_solve(11, gspec, ["Fe", "Cr", "Ni"], frac, E, beam_y=float(y), beam_sigma=50 * NM,
-                                  n_steps=n_steps, detector=(100 * NM, 0.0, 0.0), precision=precision,
-                                  stabilise=stabilise, label=f"cfg2 E={E} y={y:.3e}"))
+            s = make_solve(11, gspec, ["Fe", "Cr", "Ni"], frac, E, beam_y=float(y), beam_sigma=50 * NM,
+                           n_steps=n_steps, detector=(100 * NM, 0.0, 0.0), precision=precision,
+                           stabilise=stabilise, label=f"cfg2 E={E} y={y:.3e}")
+            if mat is None:
+                mat = s.material
+            s.material = mat
+            out.append(s)
     return out
 
 
