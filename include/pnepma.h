@@ -187,6 +187,23 @@ int pn_set_state(pn_handle* h, const double* rho, const double* state);
 int pn_step(pn_handle* h, int32_t step);
 int pn_get_state(pn_handle* h, double* state);
 
+/* Forward intensity march that allocates nothing (no counterpart in the reference).
+   For callers that cannot allocate device memory while they solve -- their GPU memory is owned by
+   another allocator that has reserved it, or they run a latency-bound loop where cudaMalloc /
+   cudaFree would synchronise the device.  Same result as pn_forward (FP64 descriptors only), but
+   rho, noa, acs and intensities are device pointers owned by the caller, the work is ordered on
+   `stream` (a cudaStream_t, NULL = legacy default stream) without synchronising, and every
+   scratch buffer comes from one library-owned device array of PN_NOALLOC_SCRATCH_BYTES per GPU,
+   held by every GPU that loads the library until the process exits.  Problems whose scratch does
+   not fit are rejected with PN_ERR_NO_MEMORY (message from pn_last_error(NULL)).  The first call
+   on a device looks up the array's device address (cudaGetSymbolAddress) and should come before
+   any stream capture.  All calls share the array: calls whose work overlaps on the GPU race and
+   must be serialised by the caller.  The descriptor's host tables may be reused once the call
+   returns. */
+#define PN_NOALLOC_SCRATCH_BYTES (64u << 20)
+int pn_forward_noalloc(const pn_desc* desc, const double* rho, const double* noa, const double* acs,
+                       double* intensities, void* stream);
+
 /* Facts about a created handle (diagnostics; no counterpart in the reference). */
 typedef struct pn_handle_info {
   int32_t checkpoint_stride;   /* stride in use (1 = every state kept) */

@@ -62,6 +62,11 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     objs.append(o)
     if force or _stale(o, deps + [capi]):
         jobs.append((capi, o, [], extra))
+    noalloc = os.path.join(CSRC, "pn_noalloc.cu")
+    o = os.path.join(OUT, "pn_noalloc.o")
+    objs.append(o)
+    if force or _stale(o, deps + [noalloc]):
+        jobs.append((noalloc, o, [], extra))
     order_src = os.path.join(CSRC, "pn_order.cu")
     for N in codegen.ORDERS:
         o = os.path.join(OUT, f"pn_order_{N}.o")

@@ -27,7 +27,7 @@ class PnHandleInfo(ctypes.Structure):
                 ("adjoint_kernels", ctypes.c_int64)]
 
 
-EXPORTS = ("pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
+EXPORTS = ("pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
            "pn_abi_version", "pn_compiled_orders")
 
@@ -60,6 +60,8 @@ def lib():
         L.pn_set_state.argtypes = [P, P, P]
         L.pn_step.argtypes = [P, ctypes.c_int32]
         L.pn_get_state.argtypes = [P, P]
+        L.pn_forward_noalloc.argtypes = [ctypes.POINTER(PnDesc), P, P, P, P, P]
+        L.pn_forward_noalloc.restype = ctypes.c_int
         L.pn_query_handle.argtypes = [P, ctypes.POINTER(PnHandleInfo)]
         L.pn_query_handle.restype = ctypes.c_int
         L.pn_destroy.argtypes = [P]

@@ -44,6 +44,10 @@ struct pn_handle {
 
 static thread_local std::string g_last_error;
 
+namespace pn {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace pn
+
 static int fail(const std::string& msg, int code) {
   g_last_error = msg;
   return code;
