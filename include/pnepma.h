@@ -217,8 +217,44 @@ int pn_query_handle(const pn_handle* h, pn_handle_info* info);
 
 void pn_destroy(pn_handle* h);
 
-/* Human-readable description of the last error on this handle (or of the last failed
-   pn_create / pn_query_sizes in this thread when h is NULL).  Never NULL. */
+/*
+ * Batched solves (no counterpart in the reference, whose scripts call calc_intensities once per
+ * beam position and energy, scripts/2d_full_reconstruction_test.jl:104-149).  Many descriptors,
+ * possibly of different orders, grids, element counts and step counts, marched together: one
+ * kernel launch per sub-step covers every solve of one order.  All descriptors must share one
+ * precision; the coupling blocks must be the closed form of pn_matrices.jl:146-152.  Inputs and
+ * outputs are arrays (one entry per solve, in descriptor order) of device pointers with the same
+ * layouts as pn_forward / pn_adjoint; work is ordered on `stream` without synchronising.
+ */
+typedef struct pn_batch pn_batch;
+
+typedef struct pn_batch_options {
+  int64_t memory_budget;      /* bytes of device memory for the tapes; 0 = half of the free memory */
+  int32_t checkpoint_stride;  /* 0 = smallest stride whose tapes fit the budget; K >= 1 forces K */
+  int32_t reserved;
+} pn_batch_options;
+
+typedef struct pn_batch_info {
+  int32_t n_solves;
+  int32_t n_groups;           /* one per distinct order */
+  int32_t checkpoint_stride;  /* largest stride in use */
+  int32_t reserved;
+  int64_t device_bytes;
+  int64_t forward_kernels;    /* kernel launches of one pn_batch_forward */
+  int64_t adjoint_kernels;    /* kernel launches of one pn_batch_adjoint */
+} pn_batch_info;
+
+int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_options* options, pn_batch** out);
+int pn_batch_forward(pn_batch* b, const double* const* rho, const double* const* noa,
+                     const double* const* acs, double* const* intensities, void* stream);
+int pn_batch_adjoint(pn_batch* b, const double* const* intensities_bar, double* const* rho_bar,
+                     double* const* noa_bar, double* const* acs_bar, void* stream);
+int pn_batch_query(const pn_batch* b, pn_batch_info* info);
+void pn_batch_destroy(pn_batch* b);
+
+/* Human-readable description of the last error on this handle (or, when h is NULL, of the last
+   failed call in this thread that has no handle: pn_create, pn_query_sizes, pn_batch_*,
+   pn_forward_noalloc).  Never NULL. */
 const char* pn_last_error(const pn_handle* h);
 
 /* ABI version and the compiled P_N orders (bit N set when order N is available). */

@@ -62,6 +62,11 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     objs.append(o)
     if force or _stale(o, deps + [capi]):
         jobs.append((capi, o, [], extra))
+    batch = os.path.join(CSRC, "pn_batch.cu")
+    o = os.path.join(OUT, "pn_batch.o")
+    objs.append(o)
+    if force or _stale(o, deps + [batch]):
+        jobs.append((batch, o, [], extra))
     noalloc = os.path.join(CSRC, "pn_noalloc.cu")
     o = os.path.join(OUT, "pn_noalloc.o")
     objs.append(o)

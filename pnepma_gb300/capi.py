@@ -27,7 +27,20 @@ class PnHandleInfo(ctypes.Structure):
                 ("adjoint_kernels", ctypes.c_int64)]
 
 
-EXPORTS = ("pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
+class PnBatchOptions(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_int64), ("checkpoint_stride", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class PnBatchInfo(ctypes.Structure):
+    _fields_ = [("n_solves", ctypes.c_int32), ("n_groups", ctypes.c_int32),
+                ("checkpoint_stride", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("device_bytes", ctypes.c_int64), ("forward_kernels", ctypes.c_int64),
+                ("adjoint_kernels", ctypes.c_int64)]
+
+
+EXPORTS = ("pn_batch_create", "pn_batch_forward", "pn_batch_adjoint", "pn_batch_query", "pn_batch_destroy",
+           "pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
            "pn_abi_version", "pn_compiled_orders")
 
@@ -60,6 +73,16 @@ def lib():
         L.pn_set_state.argtypes = [P, P, P]
         L.pn_step.argtypes = [P, ctypes.c_int32]
         L.pn_get_state.argtypes = [P, P]
+        L.pn_batch_create.argtypes = [P, ctypes.c_int32, ctypes.POINTER(PnBatchOptions), ctypes.POINTER(P)]
+        L.pn_batch_create.restype = ctypes.c_int
+        L.pn_batch_forward.argtypes = [P, P, P, P, P, P]
+        L.pn_batch_forward.restype = ctypes.c_int
+        L.pn_batch_adjoint.argtypes = [P, P, P, P, P, P]
+        L.pn_batch_adjoint.restype = ctypes.c_int
+        L.pn_batch_query.argtypes = [P, ctypes.POINTER(PnBatchInfo)]
+        L.pn_batch_query.restype = ctypes.c_int
+        L.pn_batch_destroy.argtypes = [P]
+        L.pn_batch_destroy.restype = None
         L.pn_forward_noalloc.argtypes = [ctypes.POINTER(PnDesc), P, P, P, P, P]
         L.pn_forward_noalloc.restype = ctypes.c_int
         L.pn_query_handle.argtypes = [P, ctypes.POINTER(PnHandleInfo)]
@@ -178,3 +201,58 @@ class Handle:
     def _check_len(a, n, name):
         if a.size != n:
             raise ValueError(f"{name} has {a.size} values, expected {n}")
+
+
+def _ptr_array(ptrs):
+    arr = (ctypes.c_void_p * len(ptrs))()
+    for i, p in enumerate(ptrs):
+        arr[i] = int(p)
+    return arr
+
+
+class Batch:
+    """Owns one ``pn_batch``: many solves marched together (device-pointer interface)."""
+
+    def __init__(self, descs, keepalive=None, memory_budget: int = 0, checkpoint_stride: int = 0):
+        self.descs = list(descs)
+        self._keep = keepalive
+        self.sizes = [query_sizes(d) for d in self.descs]
+        arr = (ctypes.c_void_p * len(self.descs))()
+        for i, d in enumerate(self.descs):
+            arr[i] = ctypes.addressof(d)
+        self._arr = arr
+        opt = PnBatchOptions(int(memory_budget), int(checkpoint_stride), 0)
+        b = ctypes.c_void_p()
+        rc = lib().pn_batch_create(arr, len(self.descs), ctypes.byref(opt), ctypes.byref(b))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        self._b = b
+
+    def _check(self, rc):
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+
+    def info(self) -> PnBatchInfo:
+        out = PnBatchInfo()
+        self._check(lib().pn_batch_query(self._b, ctypes.byref(out)))
+        return out
+
+    def forward(self, rho, noa, acs, intensities, stream=0):
+        """Lists of device pointers (ints), one per solve."""
+        self._check(lib().pn_batch_forward(self._b, _ptr_array(rho), _ptr_array(noa), _ptr_array(acs),
+                                           _ptr_array(intensities), _ptr(stream)))
+
+    def adjoint(self, ibar, rho_bar, noa_bar, acs_bar, stream=0):
+        self._check(lib().pn_batch_adjoint(self._b, _ptr_array(ibar), _ptr_array(rho_bar), _ptr_array(noa_bar),
+                                           _ptr_array(acs_bar), _ptr(stream)))
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().pn_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

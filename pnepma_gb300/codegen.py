@@ -95,6 +95,14 @@ def emit(orders=ORDERS) -> str:
                 for j, rows in block_structure(N, c, d):
                     for (i, _v) in rows:
                         rc.append(f"{{{i}, {j}}}")
+        vals = []
+        for c in range(N_CLASSES):
+            for d in range(3):
+                for j, rows in block_structure(N, c, d):
+                    for (i, v) in rows:
+                        vals.append(_lit(v))
+        w(f"  // closed-form value of every table entry, in table order")
+        w(f"  static constexpr double val[{max(1, len(vals))}] = {{{', '.join(vals) if vals else '0.0'}}};")
         w(f"  // (row, column) of every table entry, in table order")
         w(f"  static constexpr short rc[{max(1, len(rc))}][2] = {{{', '.join(rc) if rc else '{0, 0}'}}};")
         w(f"  static __host__ __device__ constexpr int off(int c, int d) {{ return " +

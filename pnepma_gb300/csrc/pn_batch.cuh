@@ -1,0 +1,940 @@
+// pn_batch.cuh -- many uneven solves of one P_N order marched together: one launch per sub-step
+// covers the active cells of every solve of the group.
+//
+// Scheduling.  Solves are sorted by their number of energy steps (longest first) and aligned at
+// the end of their forward march.  A state is named by j = n_steps - (forward step): j = n_steps
+// is the zero initial state, j = 0 the last forward state.  Forward launch t (t = 1..max_steps)
+// produces state j = max_steps - t of every solve with n_steps > j; adjoint iteration a uses state
+// j = a of every solve with n_steps > a (and the zero state, with the final accumulation, for the
+// solves with n_steps == a).  So the solves active in any launch are a prefix of the sorted
+// list, and the tile list of each launch is a prefix of one fixed, solve-major tile list.
+//
+// Checkpoints.  With stride K, state j is kept when j % K == 0; the adjoint walks segments
+// [mK, (m+1)K) and first recomputes states mK+1 .. (m+1)K-1 from state (m+1)K (or from the zero
+// state).  Because the schedule is aligned in j, every solve checkpoints and recomputes at the
+// same launches.  K = 1 keeps every state.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "pn_batch_base.h"
+#include "pn_solver.cuh"
+
+namespace pn {
+
+template <class T>
+struct BInst {
+  Geom g[8];
+  long long dev_off[8];
+  long long slot_elems;
+  T* slots;               // [0] zero state, [1 .. n_ck] checkpoints, then work slots
+  T* lam;
+  int n_ck;
+  int ns, ne, nr, N1;
+  int act[3];
+  int active[8];
+  T inv_h[3];
+  T dE;
+  double dEd, dvol, scale_g;
+  const T* rho[8];
+  double* rbar[8];
+  const double* bmat_f[3][8];
+  const double* bmat_a[3][8];
+  const double* beam[8];
+  double* acs;            // [cell][r] device copies of the inputs
+  double* noa;            // [cell][e]
+  double* wint;           // [cell][r]
+  double* acs_bar;
+  double* noa_bar;
+  double* ibar;           // scaled cotangent [r]
+  double* out_mul;        // factor undoing the scaling of the adjoint outputs
+  double* I;              // [r] intensities of the last forward
+  double* integral;       // [ns + 1][r]
+  int xel[MAXR];
+  // per-step tables
+  const T* fwd_s;         // [ns][ne]
+  const T* fwd_c;         // [ns][ne][N1]
+  const double* fwd_bc;   // [ns]
+  const double* fwd_sigma;   // [ns + 1][r]
+  const double* fwd_weight;  // [ns + 1]
+  const T* adj_s;         // [ns][ne]
+  const T* adj_c;         // [ns][ne][N1]
+  const double* adj_src;  // [ns][r]
+  const T* int_s;         // [ns + 1][ne]
+  const T* int_c;         // [ns + 1][ne][N1]
+  const double* int_bc;   // [ns + 1]
+  const double* int_coef; // [ns + 1][r]  dE dvol sigma w
+  const double* int_wfac; // [ns + 1]     dvol dE w
+  double src_mag;         // largest adjoint cross-section x 1e23 (scaling of the cotangent)
+  // caller layout of rho / rho_bar
+  int shape[8][3];
+  long long off_rho[8];
+  long long n_rho;
+  long long n_eee;
+  long long rho_off[8];
+  int px[8];
+  // work segments per list (0: parity-0 targets, 1: parity-1 targets, 2: all classes)
+  int tile0[3];
+  int nseg[3];
+  Seg seg[3][MAXSEG];
+};
+
+struct BTile {
+  int inst;
+  int seg;
+  int lb;   // block index local to the segment
+  int pad;
+};
+
+enum { BM_FORWARD = 0, BM_RECOMPUTE = 1, BM_ADJOINT = 2 };
+
+template <class T>
+struct BLaunch {
+  const BInst<T>* inst;
+  const BTile* tiles;
+  int list;
+  int mode;
+  int j;        // forward / recompute: state produced; adjoint / integrate: iteration
+  int sub;      // 1, 2, 3
+  int K;
+  double* partial;   // forward even sub-step: [tile][r] of this launch
+};
+
+// per-block arguments in shared memory, same member names as SubArgs / IntArgs
+template <class T, int N>
+struct BSub {
+  Geom g[8];
+  T* rd[8];
+  T* wr[8];
+  const T* rho[8];
+  const double* bmat[3][8];
+  const double* beam[8];
+  int act[3];
+  int ne, nr;
+  int adjoint_source;
+  T dt;
+  double bc, scale_g;
+  T s[MAXE];
+  T c[MAXE][N + 1];
+  const double* acs;
+  const double* noa;
+  const double* ibar;
+  int xel[MAXR];
+  double sig_src[MAXR];
+  const double* wint;
+  T inv_h[3];
+};
+
+template <class T, int N>
+struct BInt {
+  Geom g[8];
+  T* u[8];
+  const T* lam[8];
+  const T* rho[8];
+  double* rbar[8];
+  const double* bmat[3][8];
+  const double* beam[8];
+  int act[3];
+  int ne, nr;
+  double bc, scale_g, wfac;
+  T s[MAXE];
+  T c[MAXE][N + 1];
+  const double* acs;
+  const double* noa;
+  const double* ibar;
+  double* acs_bar;
+  double* noa_bar;
+  int xel[MAXR];
+  double coef[MAXR];
+  T inv_h[3];
+};
+
+template <class T>
+__device__ __forceinline__ T* bslot(const BInst<T>& I, int j, int K, bool segment, int m) {
+  if (j >= I.ns) return I.slots;
+  if (j % K == 0) return I.slots + (long long)(1 + j / K) * I.slot_elems;
+  const int w = segment ? (j - m * K - 1) : (j & 1);
+  return I.slots + (long long)(1 + I.n_ck + w) * I.slot_elems;
+}
+
+template <class T, int N, bool ADJ>
+__global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_constant__ BLaunch<T> L) {
+  __shared__ BSub<T, N> a;
+  __shared__ int sh_seg, sh_lb, sh_inst;
+  if (threadIdx.x == 0) {
+    const BTile tl = L.tiles[blockIdx.x];
+    const BInst<T>& I = L.inst[tl.inst];
+    sh_seg = tl.seg;
+    sh_lb = tl.lb;
+    sh_inst = tl.inst;
+    const int par = L.list;
+    T* own_rd;
+    T* own_wr;
+    T* from_rd;
+    int row;
+    if (!ADJ) {
+      const bool segment = L.mode == BM_RECOMPUTE;
+      const int m = L.j / L.K;
+      T* src = bslot(I, L.j + 1, L.K, segment, m);
+      T* dst = bslot(I, L.j, L.K, segment, m);
+      own_rd = (L.sub == 3) ? dst : src;
+      own_wr = dst;
+      from_rd = (L.sub == 1) ? src : dst;
+      row = I.ns - L.j - 1;
+      a.bc = I.fwd_bc[row];
+      for (int e = 0; e < MAXE; ++e) {
+        a.s[e] = e < I.ne ? I.fwd_s[row * I.ne + e] : T(0);
+        for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.fwd_c[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
+      }
+      a.adjoint_source = 0;
+    } else {
+      own_rd = own_wr = from_rd = I.lam;
+      row = L.j;
+      a.bc = 0.0;
+      for (int e = 0; e < MAXE; ++e) {
+        a.s[e] = e < I.ne ? I.adj_s[row * I.ne + e] : T(0);
+        for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.adj_c[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
+      }
+      a.adjoint_source = 1;
+      for (int r = 0; r < MAXR; ++r) a.sig_src[r] = r < I.nr ? I.adj_src[(long long)row * I.nr + r] : 0.0;
+    }
+    for (int c = 0; c < 8; ++c) {
+      a.g[c] = I.g[c];
+      const bool tgt = class_parity_d(c) == par;
+      a.rd[c] = I.active[c] ? (tgt ? own_rd : from_rd) + I.dev_off[c] : nullptr;
+      a.wr[c] = I.active[c] ? own_wr + I.dev_off[c] : nullptr;
+      a.rho[c] = I.rho[c];
+      for (int k = 0; k < 3; ++k) a.bmat[k][c] = ADJ ? I.bmat_a[k][c] : I.bmat_f[k][c];
+      a.beam[c] = I.beam[c];
+    }
+    for (int k = 0; k < 3; ++k) {
+      a.act[k] = I.act[k];
+      a.inv_h[k] = I.inv_h[k];
+    }
+    a.ne = I.ne;
+    a.nr = I.nr;
+    a.dt = L.sub == 2 ? I.dE : I.dE * T(0.5);
+    a.scale_g = I.scale_g;
+    a.acs = I.acs;
+    a.noa = I.noa;
+    a.ibar = I.ibar;
+    a.wint = I.wint;
+    for (int r = 0; r < MAXR; ++r) a.xel[r] = I.xel[r];
+  }
+  __syncthreads();
+  const Seg& sg = L.inst[sh_inst].seg[L.list][sh_seg];
+  int i = 0, j = 0, k = 0;
+  bool ok;
+  {
+    Seg one = sg;
+    one.block0 = 0;
+    int s0;
+    ok = locate(&one, 1, sh_lb, threadIdx.x, s0, i, j, k);
+  }
+  const bool face = sg.kind == 1;
+  const int cls = sg.cls;
+  double part[MAXR];
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
+  double* pp = (L.partial != nullptr) ? part : nullptr;
+  if (ok) {
+    switch (cls) {
+      case 0: substep_cell<T, N, 0, ADJ, true>(a, i, j, k, face, pp); break;
+      case 1: substep_cell<T, N, 1, ADJ, true>(a, i, j, k, face, pp); break;
+      case 2: substep_cell<T, N, 2, ADJ, true>(a, i, j, k, face, pp); break;
+      case 3: substep_cell<T, N, 3, ADJ, true>(a, i, j, k, face, pp); break;
+      case 4: substep_cell<T, N, 4, ADJ, true>(a, i, j, k, face, pp); break;
+      case 5: substep_cell<T, N, 5, ADJ, true>(a, i, j, k, face, pp); break;
+      case 6: substep_cell<T, N, 6, ADJ, true>(a, i, j, k, face, pp); break;
+      default: substep_cell<T, N, 7, ADJ, true>(a, i, j, k, face, pp); break;
+    }
+  }
+  if (L.partial != nullptr) {
+    __shared__ double red[BLOCK / 32][MAXR];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+      double v = part[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[w][r] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < MAXR) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+      L.partial[(long long)blockIdx.x * MAXR + threadIdx.x] = v;
+    }
+  }
+}
+
+template <class T, int N>
+__global__ void __launch_bounds__(BLOCK) batch_integrate_kernel(const __grid_constant__ BLaunch<T> L) {
+  __shared__ BInt<T, N> a;
+  __shared__ int sh_seg, sh_lb, sh_inst;
+  if (threadIdx.x == 0) {
+    const BTile tl = L.tiles[blockIdx.x];
+    const BInst<T>& I = L.inst[tl.inst];
+    sh_seg = tl.seg;
+    sh_lb = tl.lb;
+    sh_inst = tl.inst;
+    const int it = L.j;   // iteration; it == ns is the final accumulation on the zero state
+    T* u = bslot(I, it, L.K, true, it / L.K);
+    for (int c = 0; c < 8; ++c) {
+      a.g[c] = I.g[c];
+      a.u[c] = I.active[c] ? u + I.dev_off[c] : nullptr;
+      a.lam[c] = I.active[c] ? I.lam + I.dev_off[c] : nullptr;
+      a.rho[c] = I.rho[c];
+      a.rbar[c] = I.rbar[c];
+      for (int k = 0; k < 3; ++k) a.bmat[k][c] = I.bmat_f[k][c];
+      a.beam[c] = I.beam[c];
+    }
+    for (int k = 0; k < 3; ++k) {
+      a.act[k] = I.act[k];
+      a.inv_h[k] = I.inv_h[k];
+    }
+    a.ne = I.ne;
+    a.nr = I.nr;
+    a.bc = I.int_bc[it];
+    a.scale_g = I.scale_g;
+    a.wfac = I.int_wfac[it];
+    for (int e = 0; e < MAXE; ++e) {
+      a.s[e] = e < I.ne ? I.int_s[(long long)it * I.ne + e] : T(0);
+      for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.int_c[((long long)it * I.ne + e) * (N + 1) + l] : T(0);
+    }
+    a.acs = I.acs;
+    a.noa = I.noa;
+    a.ibar = I.ibar;
+    a.acs_bar = I.acs_bar;
+    a.noa_bar = I.noa_bar;
+    for (int r = 0; r < MAXR; ++r) {
+      a.xel[r] = I.xel[r];
+      a.coef[r] = r < I.nr ? I.int_coef[(long long)it * I.nr + r] : 0.0;
+    }
+  }
+  __syncthreads();
+  const Seg& sg = L.inst[sh_inst].seg[2][sh_seg];
+  int i = 0, j = 0, k = 0;
+  Seg one = sg;
+  one.block0 = 0;
+  int s0;
+  if (!locate(&one, 1, sh_lb, threadIdx.x, s0, i, j, k)) return;
+  const bool face = sg.kind == 1;
+  switch (sg.cls) {
+    case 0: integrate_cell<T, N, 0, true>(a, i, j, k, face); break;
+    case 1: integrate_cell<T, N, 1, true>(a, i, j, k, face); break;
+    case 2: integrate_cell<T, N, 2, true>(a, i, j, k, face); break;
+    case 3: integrate_cell<T, N, 3, true>(a, i, j, k, face); break;
+    case 4: integrate_cell<T, N, 4, true>(a, i, j, k, face); break;
+    case 5: integrate_cell<T, N, 5, true>(a, i, j, k, face); break;
+    case 6: integrate_cell<T, N, 6, true>(a, i, j, k, face); break;
+    default: integrate_cell<T, N, 7, true>(a, i, j, k, face); break;
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// batched helpers: one launch over every solve of the group (blockIdx.y = solve)
+// ----------------------------------------------------------------------------------------------
+
+
+template <class T>
+__global__ void batch_load_kernel(const BInst<T>* __restrict__ inst, const BIo* __restrict__ io) {
+  const BInst<T>& I = inst[blockIdx.y];
+  const BIo& o = io[blockIdx.y];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  // densities: caller layout [class][point][e] -> device [e][z][y][x] per active class
+  for (long long q = t0; q < I.n_rho; q += stride) {
+    int c = 0;
+    while (c < 7 && q >= I.off_rho[c + 1]) ++c;
+    if (!I.active[c]) continue;
+    const long long r0 = q - I.off_rho[c];
+    const long long p = r0 / I.ne;
+    const int e = (int)(r0 - p * I.ne);
+    const int nx = I.shape[c][0], ny = I.shape[c][1];
+    const int x = (int)(p % nx);
+    const long long rest = p / nx;
+    const int y = (int)(rest % ny);
+    const int z = (int)(rest / ny);
+    T* dst = const_cast<T*>(I.rho[c]);
+    dst[e * I.g[c].ms + ((long long)z * ny + y) * I.px[c] + x] = T(o.rho[q]);
+  }
+  for (long long q = t0; q < I.n_eee * I.ne; q += stride) I.noa[q] = o.noa[q];
+  for (long long q = t0; q < I.n_eee * I.nr; q += stride) {
+    I.acs[q] = o.acs[q];
+    const long long cell = q / I.nr;
+    const int r = (int)(q - cell * I.nr);
+    I.wint[q] = o.acs[q] * o.noa[cell * I.ne + I.xel[r]];
+  }
+}
+
+template <class T>
+__global__ void batch_zero_kernel(const BInst<T>* __restrict__ inst, int which) {
+  const BInst<T>& I = inst[blockIdx.y];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (which == 0) {
+    for (long long q = t0; q < I.slot_elems; q += stride) I.slots[q] = T(0);
+    for (long long q = t0; q < (long long)(I.ns + 1) * I.nr; q += stride) I.integral[q] = 0.0;
+  } else {
+    for (long long q = t0; q < I.slot_elems; q += stride) I.lam[q] = T(0);
+    for (int c = 0; c < 8; ++c)
+      if (I.active[c])
+        for (long long q = t0; q < I.g[c].ms * I.ne; q += stride) I.rbar[c][q] = 0.0;
+    for (long long q = t0; q < I.n_eee * I.nr; q += stride) I.acs_bar[q] = 0.0;
+    for (long long q = t0; q < I.n_eee * I.ne; q += stride) I.noa_bar[q] = 0.0;
+  }
+}
+
+// integral[i][r] of solve k = sum over its eee tiles of the partials of forward launch t
+template <class T>
+__global__ void batch_reduce_kernel(const BInst<T>* __restrict__ inst, const double* __restrict__ partial,
+                                    int max_ns, int n_tiles0) {
+  const BInst<T>& I = inst[blockIdx.y];
+  const int i = blockIdx.x + 1;  // forward step 1..ns
+  if (i > I.ns) return;
+  const int t = max_ns - I.ns + i;  // launch index (1-based)
+  const int nt = I.nseg[0] > 0 ? (I.seg[0][I.nseg[0] - 1].block0 + I.seg[0][I.nseg[0] - 1].nblocks) : 0;
+  __shared__ double buf[MAXR][128];
+  for (int r = 0; r < MAXR; ++r) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nt; b += blockDim.x)
+      v += partial[((long long)(t - 1) * n_tiles0 + I.tile0[0] + b) * MAXR + r];
+    buf[r][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int r = 0; r < MAXR; ++r) buf[r][threadIdx.x] += buf[r][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < I.nr) I.integral[(long long)i * I.nr + threadIdx.x] = buf[threadIdx.x][0];
+}
+
+template <class T>
+__global__ void batch_final_kernel(const BInst<T>* __restrict__ inst) {
+  const BInst<T>& I = inst[blockIdx.x];
+  const int r = threadIdx.x;
+  if (r >= I.nr) return;
+  double acc = 0.0;
+  for (int i = 0; i <= I.ns; ++i)
+    acc = acc + I.dEd * I.dvol * I.fwd_sigma[(long long)i * I.nr + r] * I.integral[(long long)i * I.nr + r] * I.fwd_weight[i];
+  I.I[r] = acc / I.scale_g;
+}
+
+template <class T>
+__global__ void batch_copy_I_kernel(const BInst<T>* __restrict__ inst, const BIo* __restrict__ io) {
+  const BInst<T>& I = inst[blockIdx.x];
+  if (threadIdx.x < I.nr && io[blockIdx.x].I) io[blockIdx.x].I[threadIdx.x] = I.I[threadIdx.x];
+}
+
+template <class T>
+__global__ void batch_prep_ibar_kernel(const BInst<T>* __restrict__ inst, const BIo* __restrict__ io, int fp32) {
+  const BInst<T>& I = inst[blockIdx.x];
+  if (threadIdx.x != 0) return;
+  const double* in = io[blockIdx.x].ibar;
+  double m = 0.0;
+  for (int r = 0; r < I.nr; ++r) m = fmax(m, fabs(in[r]));
+  double sc = 1.0;
+  const double q = m * I.src_mag;
+  if (fp32 && q > 0.0 && isfinite(q)) sc = ldexp(1.0, -(int)llrint(log2(q)));
+  for (int r = 0; r < I.nr; ++r) I.ibar[r] = in[r] * sc;
+  I.out_mul[0] = 1.0 / (I.scale_g * sc);
+}
+
+template <class T>
+__global__ void batch_store_kernel(const BInst<T>* __restrict__ inst, const BIo* __restrict__ io) {
+  const BInst<T>& I = inst[blockIdx.y];
+  const BIo& o = io[blockIdx.y];
+  const double mul = I.out_mul[0];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (long long q = t0; q < I.n_rho; q += stride) {
+    int c = 0;
+    while (c < 7 && q >= I.off_rho[c + 1]) ++c;
+    double v = 0.0;
+    if (I.active[c]) {
+      const long long r0 = q - I.off_rho[c];
+      const long long p = r0 / I.ne;
+      const int e = (int)(r0 - p * I.ne);
+      const int nx = I.shape[c][0], ny = I.shape[c][1];
+      const int x = (int)(p % nx);
+      const long long rest = p / nx;
+      const int y = (int)(rest % ny);
+      const int z = (int)(rest / ny);
+      v = I.rbar[c][e * I.g[c].ms + ((long long)z * ny + y) * I.px[c] + x] * mul;
+    }
+    o.rho_bar[q] = v;
+  }
+  for (long long q = t0; q < I.n_eee * I.ne; q += stride) o.noa_bar[q] = I.noa_bar[q] * mul;
+  for (long long q = t0; q < I.n_eee * I.nr; q += stride) o.acs_bar[q] = I.acs_bar[q] * mul;
+}
+
+// ----------------------------------------------------------------------------------------------
+// host side: one group of solves with the same order and element type
+// ----------------------------------------------------------------------------------------------
+
+
+template <class T, int N>
+class BatchGroup : public BatchGroupBase {
+ public:
+  std::vector<Layout> Ls;
+  std::vector<int> order;      // position in group -> caller index (sorted by steps, longest first)
+  std::vector<BInst<T>> hinst;
+  BInst<T>* dinst = nullptr;
+  BIo* dio = nullptr;
+  std::vector<BTile> tiles[3];
+  BTile* dtiles[3] = {nullptr, nullptr, nullptr};
+  std::vector<int> tile_end[3];   // cumulative tiles per solve (in group order)
+  double* partial = nullptr;
+  int max_ns = 0, K = 1, n = 0;
+  std::vector<void*> allocs;
+  long long bytes = 0;
+  cudaGraphExec_t gf = nullptr, ga = nullptr;
+  cudaStream_t cap = nullptr;
+  long long nl_f = 0, nl_a = 0, nl = 0;
+
+  ~BatchGroup() override {
+    if (gf) cudaGraphExecDestroy(gf);
+    if (ga) cudaGraphExecDestroy(ga);
+    if (cap) cudaStreamDestroy(cap);
+    for (void* p : allocs) cudaFree(p);
+  }
+  long long device_bytes() const override { return bytes; }
+  long long launches_forward() const override { return nl_f + 2; }
+  long long launches_adjoint() const override { return nl_a + 2; }
+  int stride() const override { return K; }
+
+  template <class U>
+  int alloc(U*& p, long long cnt) {
+    void* q = nullptr;
+    size_t b = (size_t)std::max<long long>(cnt, 1) * sizeof(U);
+    cudaError_t e = cudaMalloc(&q, b);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      err = "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e);
+      return PN_ERR_NO_MEMORY;
+    }
+    allocs.push_back(q);
+    bytes += (long long)b;
+    p = (U*)q;
+    return PN_OK;
+  }
+
+  template <class U>
+  int upload(U*& dst, const std::vector<U>& v) {
+    int rc = alloc(dst, (long long)v.size());
+    if (rc) return rc;
+    if (!v.empty()) PN_CUDA(cudaMemcpy(dst, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice));
+    return PN_OK;
+  }
+
+  int tiles_active(int list, int x) const {
+    // tiles of the solves with n_steps > x (a prefix of the group order)
+    int cnt = 0;
+    for (int q = 0; q < n; ++q)
+      if (hinst[q].ns > x) cnt = tile_end[list][q];
+    return cnt;
+  }
+
+  static int n_ck_for(int ns, int K) { return (ns - 1) / K + 1; }
+  static int n_work_for(int K) { return std::max(2, K - 1); }
+
+  int create(const pn_desc* const* d, const int* idx, int cnt, long long budget, int Kreq) override {
+    n = cnt;
+    members.assign(idx, idx + cnt);
+    order.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return d[idx[a]]->n_steps > d[idx[b]]->n_steps; });
+    std::vector<int> sorted_members(n);
+    for (int q = 0; q < n; ++q) sorted_members[q] = idx[order[q]];
+    members = sorted_members;
+    Ls.resize(n);
+    long long slot_total = 0, fixed = 0;
+    for (int q = 0; q < n; ++q) {
+      const pn_desc* dq = d[members[q]];
+      int rc = Ls[q].init(dq, err);
+      if (rc) return rc;
+      if (Ls[q].ne > MAXE || Ls[q].nr > MAXR || Ls[q].nr < 1) { err = "1..8 x-ray lines and at most 4 elements per solve"; return PN_ERR_UNSUPPORTED; }
+      max_ns = std::max(max_ns, Ls[q].ns);
+      slot_total += Ls[q].slot_elems * (long long)sizeof(T);
+      (void)fixed;
+    }
+    // checkpoint stride: smallest K whose tapes fit the budget
+    auto need = [&](int k) {
+      long long b = 0;
+      for (int q = 0; q < n; ++q)
+        b += (long long)(1 + n_ck_for(Ls[q].ns, k) + n_work_for(k) + 1) * Ls[q].slot_elems * (long long)sizeof(T);
+      return b;
+    };
+    if (Kreq > 0) K = Kreq;
+    else {
+      K = 1;
+      while (K < max_ns && need(K) > budget) ++K;
+      if (need(K) > budget) { err = "the batch does not fit the memory budget"; return PN_ERR_NO_MEMORY; }
+    }
+    if (K > max_ns) K = max_ns;
+    hinst.assign(n, BInst<T>());
+    int rc;
+    for (int q = 0; q < n; ++q) {
+      std::memset(&hinst[q], 0, sizeof(BInst<T>));
+      if ((rc = build_instance(q, d[members[q]]))) return rc;
+    }
+    // tile lists (solve-major, group order)
+    for (int list = 0; list < 3; ++list) {
+      tile_end[list].assign(n, 0);
+      for (int q = 0; q < n; ++q) {
+        hinst[q].tile0[list] = (int)tiles[list].size();
+        for (int sgi = 0; sgi < hinst[q].nseg[list]; ++sgi) {
+          const Seg& sg = hinst[q].seg[list][sgi];
+          for (int lb = 0; lb < sg.nblocks; ++lb) tiles[list].push_back(BTile{q, sgi, lb, 0});
+        }
+        tile_end[list][q] = (int)tiles[list].size();
+      }
+      if ((rc = upload(dtiles[list], tiles[list]))) return rc;
+    }
+    if ((rc = upload(dinst, hinst))) return rc;
+    if ((rc = alloc(dio, n))) return rc;
+    if ((rc = alloc(partial, (long long)max_ns * std::max<size_t>(tiles[0].size(), 1) * MAXR))) return rc;
+    PN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    if ((rc = capture(gf, true))) return rc;
+    if ((rc = capture(ga, false))) return rc;
+    return PN_OK;
+  }
+
+  int build_instance(int q, const pn_desc* d) {
+    const Layout& L = Ls[q];
+    BInst<T>& I = hinst[q];
+    int rc;
+    const int ns = L.ns, ne = L.ne, nr = L.nr, N1 = N + 1;
+    I.ns = ns; I.ne = ne; I.nr = nr; I.N1 = N1;
+    I.slot_elems = L.slot_elems;
+    I.n_ck = n_ck_for(ns, K);
+    const int nslots = 1 + I.n_ck + n_work_for(K);
+    if ((rc = alloc(I.slots, (long long)nslots * L.slot_elems))) return rc;
+    if ((rc = alloc(I.lam, L.slot_elems))) return rc;
+    PN_CUDA(cudaMemset(I.slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems));
+    for (int c = 0; c < 8; ++c) {
+      I.active[c] = L.active[c];
+      I.dev_off[c] = L.dev_off[c];
+      if (L.active[c]) {
+        for (int k = 0; k < 3; ++k) I.g[c].n[k] = L.shape[c][k];
+        I.g[c].px = L.px[c];
+        I.g[c].nm = L.nm[c];
+        I.g[c].ms = L.ms[c];
+      }
+      for (int k = 0; k < 3; ++k) I.shape[c][k] = L.shape[c][k];
+      I.off_rho[c] = L.off_rho[c];
+      I.rho_off[c] = L.rho_off[c];
+      I.px[c] = L.px[c];
+    }
+    I.n_rho = L.n_rho;
+    I.n_eee = L.n_eee_cells;
+    T* rho_d;
+    double* rbar_d;
+    if ((rc = alloc(rho_d, L.rho_elems))) return rc;
+    if ((rc = alloc(rbar_d, L.rho_elems))) return rc;
+    PN_CUDA(cudaMemset(rho_d, 0, sizeof(T) * (size_t)L.rho_elems));
+    for (int c = 0; c < 8; ++c) {
+      I.rho[c] = L.active[c] ? rho_d + L.rho_off[c] : nullptr;
+      I.rbar[c] = L.active[c] ? rbar_d + L.rho_off[c] : nullptr;
+    }
+    for (int k = 0; k < 3; ++k) {
+      I.act[k] = L.act[k];
+      I.inv_h[k] = T(1.0 / d->h[k]);
+    }
+    I.dE = T(d->delta_e);
+    I.dEd = d->delta_e;
+    I.dvol = d->dvol;
+    // tables
+    auto conv = [](const double* p, long long cnt) {
+      std::vector<T> v((size_t)cnt);
+      for (long long q2 = 0; q2 < cnt; ++q2) v[q2] = T(p[q2]);
+      return v;
+    };
+    auto cpd = [](const double* p, long long cnt) { return std::vector<double>(p, p + cnt); };
+    const T* tp;
+    const double* dp;
+    T* tw;
+    double* dw;
+    if ((rc = upload(tw, conv(d->fwd_s, (long long)ns * ne)))) return rc; I.fwd_s = tw;
+    if ((rc = upload(tw, conv(d->fwd_c, (long long)ns * ne * N1)))) return rc; I.fwd_c = tw;
+    if ((rc = upload(dw, cpd(d->fwd_bc, ns)))) return rc; I.fwd_bc = dw;
+    if ((rc = upload(dw, cpd(d->fwd_sigma, (long long)(ns + 1) * nr)))) return rc; I.fwd_sigma = dw;
+    if ((rc = upload(dw, cpd(d->fwd_weight, ns + 1)))) return rc; I.fwd_weight = dw;
+    if ((rc = upload(tw, conv(d->adj_s, (long long)ns * ne)))) return rc; I.adj_s = tw;
+    if ((rc = upload(tw, conv(d->adj_c, (long long)ns * ne * N1)))) return rc; I.adj_c = tw;
+    if ((rc = upload(dw, cpd(d->adj_src_sigma, (long long)ns * nr)))) return rc; I.adj_src = dw;
+    if ((rc = upload(tw, conv(d->adj_int_s, (long long)(ns + 1) * ne)))) return rc; I.int_s = tw;
+    if ((rc = upload(tw, conv(d->adj_int_c, (long long)(ns + 1) * ne * N1)))) return rc; I.int_c = tw;
+    if ((rc = upload(dw, cpd(d->adj_int_bc, ns + 1)))) return rc; I.int_bc = dw;
+    {
+      std::vector<double> coef((size_t)(ns + 1) * nr), wf((size_t)(ns + 1));
+      for (int j = 0; j <= ns; ++j) {
+        wf[j] = d->dvol * d->delta_e * d->adj_weight[j];
+        for (int r = 0; r < nr; ++r) coef[(size_t)j * nr + r] = d->delta_e * d->dvol * d->adj_sigma[(long long)j * nr + r] * d->adj_weight[j];
+      }
+      if ((rc = upload(dw, coef))) return rc; I.int_coef = dw;
+      if ((rc = upload(dw, wf))) return rc; I.int_wfac = dw;
+    }
+    (void)tp;
+    (void)dp;
+    double smax = 0.0;
+    for (long long q2 = 0; q2 < (long long)ns * nr; ++q2) smax = std::max(smax, std::fabs(d->adj_src_sigma[q2]));
+    I.src_mag = smax * 1e23;
+    for (int r = 0; r < nr; ++r) {
+      if (d->xray_element[r] < 0 || d->xray_element[r] >= ne) { err = "xray_element out of range"; return PN_ERR_INVALID; }
+      I.xel[r] = d->xray_element[r];
+    }
+    // coupling: the literal stencil must match the caller's blocks (values as well as sparsity)
+    {
+      const double* pa = d->advection;
+      for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 8; ++c) {
+          const int nrow = L.nm[c], ncol = L.nm[class_switch(c, k)];
+          const int off = Ord<N>::off(c, k);
+          const int endk = (c == 7 && k == 2) ? Ord<N>::n_tab : (k < 2 ? Ord<N>::off(c, k + 1) : Ord<N>::off(c + 1, 0));
+          int cntnz = 0;
+          for (int q2 = 0; q2 < nrow * ncol; ++q2) cntnz += pa[q2] != 0.0;
+          if (cntnz != endk - off) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
+          for (int kk = off; kk < endk; ++kk) {
+            const double v = pa[(long long)Ord<N>::rc[kk][0] * ncol + Ord<N>::rc[kk][1]];
+            if (std::fabs(v - Ord<N>::val[kk]) > 1e-14 * std::fabs(Ord<N>::val[kk])) {
+              err = "the batched path compiles the closed-form coupling blocks; the descriptor's blocks differ";
+              return PN_ERR_INVALID;
+            }
+          }
+          pa += (long long)nrow * ncol;
+        }
+    }
+    double *bf, *ba, *bm;
+    if ((rc = upload(bf, cpd(d->boundary_fwd, L.n_bnd)))) return rc;
+    if ((rc = upload(ba, cpd(d->boundary_adj, L.n_bnd)))) return rc;
+    std::vector<double> beam = cpd(d->beam_face, L.n_beam);
+    // FP32: scale the beam source so the state stays near unity (a power of two: exact)
+    I.scale_g = 1.0;
+    if (sizeof(T) == 4) {
+      double gmax = 0.0, bmax = 0.0;
+      for (double v : beam) gmax = std::max(gmax, std::fabs(v));
+      for (int q2 = 0; q2 < ns; ++q2) bmax = std::max(bmax, std::fabs(d->fwd_bc[q2]));
+      for (int q2 = 0; q2 <= ns; ++q2) bmax = std::max(bmax, std::fabs(d->adj_int_bc[q2]));
+      const double m = gmax * bmax;
+      if (m > 0.0 && std::isfinite(m)) I.scale_g = std::ldexp(1.0, -(int)std::lround(std::log2(m)));
+    }
+    if ((rc = upload(bm, beam.empty() ? std::vector<double>(1, 0.0) : beam))) return rc;
+    {
+      long long o = 0;
+      for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 8; ++c)
+          if (class_bit(c, k)) {
+            I.bmat_f[k][c] = bf + o;
+            I.bmat_a[k][c] = ba + o;
+            o += (long long)L.nm[c] * L.nm[class_switch(c, k)];
+          }
+      for (int c = 4; c < 8; ++c) I.beam[c] = bm + L.beam_off[c];
+    }
+    if ((rc = alloc(I.acs, L.n_eee_cells * nr))) return rc;
+    if ((rc = alloc(I.noa, L.n_eee_cells * ne))) return rc;
+    if ((rc = alloc(I.wint, L.n_eee_cells * nr))) return rc;
+    if ((rc = alloc(I.acs_bar, L.n_eee_cells * nr))) return rc;
+    if ((rc = alloc(I.noa_bar, L.n_eee_cells * ne))) return rc;
+    if ((rc = alloc(I.ibar, nr))) return rc;
+    if ((rc = alloc(I.out_mul, 1))) return rc;
+    if ((rc = alloc(I.I, nr))) return rc;
+    if ((rc = alloc(I.integral, (long long)(ns + 1) * nr))) return rc;
+    // work segments
+    std::vector<int> faces;
+    struct Tmp { int cls; int lo[3], ext[3]; int f0, nf; };
+    std::vector<Tmp> per;
+    for (int c = 0; c < 8; ++c) {
+      if (!L.active[c]) continue;
+      Tmp t{};
+      t.cls = c;
+      int ilo[3], ihi[3];
+      for (int k = 0; k < 3; ++k) {
+        const int nn = L.shape[c][k];
+        if (!L.act[k]) { ilo[k] = 0; ihi[k] = 1; t.lo[k] = 0; t.ext[k] = 1; }
+        else if (class_bit(c, k)) { ilo[k] = 1; ihi[k] = nn - 1; t.lo[k] = 1; t.ext[k] = std::max(0, nn - 2); }
+        else { ilo[k] = 0; ihi[k] = nn; t.lo[k] = 1; t.ext[k] = std::max(0, nn - 2); }
+      }
+      t.f0 = (int)faces.size();
+      for (int kz = ilo[2]; kz < ihi[2]; ++kz)
+        for (int jy = ilo[1]; jy < ihi[1]; ++jy)
+          for (int ix = ilo[0]; ix < ihi[0]; ++ix) {
+            const int cc[3] = {ix, jy, kz};
+            bool f = false;
+            for (int k = 0; k < 3; ++k)
+              if (L.act[k] && !class_bit(c, k) && (cc[k] == 0 || cc[k] == L.shape[c][k] - 1)) f = true;
+            if (f) faces.push_back(pack_cell(ix, jy, kz));
+          }
+      t.nf = (int)faces.size() - t.f0;
+      per.push_back(t);
+    }
+    int* fd;
+    if ((rc = upload(fd, faces.empty() ? std::vector<int>(1, 0) : faces))) return rc;
+    int nblk[3] = {0, 0, 0};
+    for (const Tmp& t : per) {
+      for (int list = 0; list < 3; ++list) {
+        if (list < 2 && class_parity(t.cls) != list) continue;
+        if (t.ext[0] > 0 && t.ext[1] > 0 && t.ext[2] > 0) {
+          Seg& g = I.seg[list][I.nseg[list]++];
+          g.cls = t.cls;
+          g.kind = 0;
+          g.block0 = nblk[list];
+          for (int k = 0; k < 3; ++k) { g.lo[k] = t.lo[k]; g.ext[k] = t.ext[k]; }
+          g.tile_x = (t.ext[1] > 1 || t.ext[2] > 1) ? 32 : BLOCK;
+          g.tiles_x = (t.ext[0] + g.tile_x - 1) / g.tile_x;
+          g.tiles_y = (t.ext[1] + BLOCK / g.tile_x - 1) / (BLOCK / g.tile_x);
+          g.nblocks = g.tiles_x * g.tiles_y * t.ext[2];
+          nblk[list] += g.nblocks;
+        }
+        if (t.nf > 0) {
+          Seg& g = I.seg[list][I.nseg[list]++];
+          g.cls = t.cls;
+          g.kind = 1;
+          g.block0 = nblk[list];
+          g.tile_x = BLOCK;
+          g.tiles_x = g.tiles_y = 1;
+          g.n_face = t.nf;
+          g.faces = fd + t.f0;
+          g.nblocks = (t.nf + BLOCK - 1) / BLOCK;
+          nblk[list] += g.nblocks;
+        }
+      }
+    }
+    if (nblk[0] == 0 || nblk[1] == 0) { err = "grid too small: a parity has no cells"; return PN_ERR_INVALID; }
+    return PN_OK;
+  }
+
+  // --------------------------------------------------------------------------------------------
+  int launch(int list, int mode, int j, int sub, double* part, bool adj, bool integ) {
+    const int x = integ ? j - 1 : j;   // integrate at iteration j includes the solves with ns == j
+    const int nt = tiles_active(integ ? 2 : list, x);
+    if (nt == 0) return PN_OK;
+    BLaunch<T> a;
+    a.inst = dinst;
+    a.tiles = dtiles[integ ? 2 : list];
+    a.list = integ ? 2 : list;
+    a.mode = mode;
+    a.j = j;
+    a.sub = sub;
+    a.K = K;
+    a.partial = part;
+    if (integ)
+      batch_integrate_kernel<T, N><<<nt, BLOCK, 0, cap>>>(a);
+    else if (adj)
+      batch_substep_kernel<T, N, true><<<nt, BLOCK, 0, cap>>>(a);
+    else
+      batch_substep_kernel<T, N, false><<<nt, BLOCK, 0, cap>>>(a);
+    PN_CUDA(cudaGetLastError());
+    ++nl;
+    return PN_OK;
+  }
+
+  int fwd_step(int j, int mode, double* part) {
+    int rc;
+    if ((rc = launch(1, mode, j, 1, nullptr, false, false))) return rc;
+    if ((rc = launch(0, mode, j, 2, part, false, false))) return rc;
+    if ((rc = launch(1, mode, j, 3, nullptr, false, false))) return rc;
+    return PN_OK;
+  }
+
+  int record(bool fwd) {
+    int rc;
+    dim3 gz(64, n);
+    if (fwd) {
+      batch_zero_kernel<T><<<gz, 256, 0, cap>>>(dinst, 0);
+      PN_CUDA(cudaGetLastError());
+      for (int t = 1; t <= max_ns; ++t) {
+        const int j = max_ns - t;
+        double* part = partial + (long long)(t - 1) * tiles[0].size() * MAXR;
+        if ((rc = fwd_step(j, BM_FORWARD, part))) return rc;
+      }
+      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, cap>>>(dinst, partial, max_ns, (int)tiles[0].size());
+      batch_final_kernel<T><<<n, 32, 0, cap>>>(dinst);
+      PN_CUDA(cudaGetLastError());
+      nl += 3;
+    } else {
+      batch_zero_kernel<T><<<gz, 256, 0, cap>>>(dinst, 1);
+      PN_CUDA(cudaGetLastError());
+      nl += 1;
+      for (int m = 0; m * K < max_ns; ++m) {
+        // recompute states (m+1)K-1 .. mK+1 of this segment
+        for (int j = std::min((m + 1) * K, max_ns) - 1; j >= m * K + 1; --j)
+          if ((rc = fwd_step(j, BM_RECOMPUTE, nullptr))) return rc;
+        for (int a = m * K; a < std::min((m + 1) * K, max_ns + 1); ++a) {
+          if ((rc = launch(2, BM_ADJOINT, a, 0, nullptr, false, true))) return rc;
+          for (int sub = 1; sub <= 3; ++sub)
+            if ((rc = launch(sub == 2 ? 0 : 1, BM_ADJOINT, a, sub, nullptr, true, false))) return rc;
+        }
+      }
+      // final accumulation of the longest solves (ns == max_ns) when max_ns is a multiple of K
+      if (max_ns % K == 0)
+        if ((rc = launch(2, BM_ADJOINT, max_ns, 0, nullptr, false, true))) return rc;
+    }
+    return PN_OK;
+  }
+
+  int capture(cudaGraphExec_t& exec, bool fwd) {
+    cudaGraph_t graph = nullptr;
+    nl = 0;
+    PN_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    int rc = record(fwd);
+    cudaError_t e = cudaStreamEndCapture(cap, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    if (e != cudaSuccess) {
+      err = std::string("stream capture: ") + cudaGetErrorString(e);
+      return PN_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      err = std::string("graph instantiate: ") + cudaGetErrorString(e);
+      return PN_ERR_CUDA;
+    }
+    (fwd ? nl_f : nl_a) = nl;
+    return PN_OK;
+  }
+
+  int put_io(const BIo* io_host, cudaStream_t s) {
+    std::vector<BIo> v(n);
+    for (int q = 0; q < n; ++q) v[q] = io_host[members[q]];
+    PN_CUDA(cudaMemcpyAsync(dio, v.data(), sizeof(BIo) * n, cudaMemcpyHostToDevice, s));
+    return PN_OK;
+  }
+
+  int forward(const BIo* io_host, cudaStream_t s) override {
+    int rc;
+    if ((rc = put_io(io_host, s))) return rc;
+    batch_load_kernel<T><<<dim3(256, n), 256, 0, s>>>(dinst, dio);
+    PN_CUDA(cudaGetLastError());
+    PN_CUDA(cudaGraphLaunch(gf, s));
+    batch_copy_I_kernel<T><<<n, 32, 0, s>>>(dinst, dio);
+    PN_CUDA(cudaGetLastError());
+    return PN_OK;
+  }
+
+  int adjoint(const BIo* io_host, cudaStream_t s) override {
+    int rc;
+    if ((rc = put_io(io_host, s))) return rc;
+    batch_prep_ibar_kernel<T><<<n, 32, 0, s>>>(dinst, dio, sizeof(T) == 4 ? 1 : 0);
+    PN_CUDA(cudaGetLastError());
+    PN_CUDA(cudaGraphLaunch(ga, s));
+    batch_store_kernel<T><<<dim3(256, n), 256, 0, s>>>(dinst, dio);
+    PN_CUDA(cudaGetLastError());
+    return PN_OK;
+  }
+};
+
+}  // namespace pn

@@ -1,0 +1,39 @@
+// pn_batch_base.h -- the interface of a group of batched solves (one order, one element type).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pnepma.h"
+
+namespace pn {
+
+// device pointers of one solve's inputs and outputs, in the caller's layouts
+struct BIo {
+  const double* rho;
+  const double* noa;
+  const double* acs;
+  const double* ibar;
+  double* I;
+  double* rho_bar;
+  double* noa_bar;
+  double* acs_bar;
+};
+
+class BatchGroupBase {
+ public:
+  virtual ~BatchGroupBase() {}
+  virtual int create(const pn_desc* const* d, const int* idx, int n, long long budget, int K) = 0;
+  virtual int forward(const BIo* io_host, cudaStream_t s) = 0;
+  virtual int adjoint(const BIo* io_host, cudaStream_t s) = 0;
+  virtual long long device_bytes() const = 0;
+  virtual long long launches_forward() const = 0;
+  virtual long long launches_adjoint() const = 0;
+  virtual int stride() const = 0;
+  std::string err;
+  std::vector<int> members;   // indices into the caller's descriptor array, in group order
+};
+
+}  // namespace pn

@@ -60,6 +60,8 @@ struct Seg {
 
 __host__ __device__ inline int pack_cell(int i, int j, int k) { return i | (j << 11) | (k << 22); }
 
+__host__ __device__ inline int class_parity_d(int c) { return (((c >> 2) & 1) + ((c >> 1) & 1) + (c & 1)) & 1; }
+
 template <class T, int N>
 struct SubArgs {
   Geom g[8];
@@ -238,10 +240,12 @@ __device__ __forceinline__ void ghosts_for_cell(T* const* rd, const Geom* g, con
   }
 }
 
-// acc[m] += sum over active axes of A_d[C] (f_r - f_l) / h_d  (sign flipped for the adjoint)
-template <class T, int N, int C, int D, bool NEG, class Tab>
+// acc[m] += sum over active axes of A_d[C] (f_r - f_l) / h_d  (sign flipped for the adjoint).
+// LIT = false: coefficients from `tab`, already divided by h_d.  LIT = true: the literal closed-form
+// coefficient compiled into the stencil, with the difference multiplied by inv_h.
+template <class T, int N, int C, int D, bool NEG, bool LIT>
 __device__ __forceinline__ void stencil_axis(T* acc, T* const* rd, const Geom* g, int i, int j, int k,
-                                             const Tab& tab) {
+                                             const T* tab, T inv_h) {
   constexpr int F = C ^ (4 >> D);
   constexpr int nf = Ord<N>::n(F);
   if constexpr (nf == 0 || Ord<N>::n(C) == 0) {
@@ -261,20 +265,41 @@ __device__ __forceinline__ void stencil_axis(T* acc, T* const* rd, const Geom* g
     auto diff = [&](int q) -> T {
       const T a = fr[q * ms];
       const T b = fl[q * ms];
-      return NEG ? (b - a) : (a - b);
+      const T d = NEG ? (b - a) : (a - b);
+      if constexpr (LIT) return d * inv_h;
+      else return d;
     };
     constexpr int off = Ord<N>::off(C, D);
-    auto coef = [&](int kk, double) -> T { return tab[off + kk]; };
+    auto coef = [&](int kk, double lit) -> T {
+      if constexpr (LIT) {
+        (void)kk;
+        return T(lit);
+      } else {
+        (void)lit;
+        return tab[off + kk];
+      }
+    };
     Adv<N, C, D>::template apply<T>(acc, diff, coef);
   }
+}
+
+template <bool LIT, class T, class A>
+__device__ __forceinline__ const T* tab_of(const A& a) {
+  if constexpr (LIT) return nullptr;
+  else return a.tab;
+}
+
+template <bool LIT, class T, class A>
+__device__ __forceinline__ T invh_of(const A& a, int d) {
+  if constexpr (LIT) return a.inv_h[d];
+  else return T(1);
 }
 
 // --------------------------------------------------------------------------------------------
 // sub-step kernel
 // --------------------------------------------------------------------------------------------
-template <class T, int N, int C, bool ADJ>
-__device__ __forceinline__ void substep_cell(const SubArgs<T, N>& a, int i, int j, int k, bool face,
-                                             double* part) {
+template <class T, int N, int C, bool ADJ, bool LIT, class A>
+__device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bool face, double* part) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n == 0) {
     return;
@@ -285,9 +310,10 @@ __device__ __forceinline__ void substep_cell(const SubArgs<T, N>& a, int i, int 
     T acc[n];
 #pragma unroll
     for (int m = 0; m < n; ++m) acc[m] = T(0);
-    if (a.act[0]) stencil_axis<T, N, C, 0, ADJ>(acc, rd, a.g, i, j, k, a.tab);
-    if (a.act[1]) stencil_axis<T, N, C, 1, ADJ>(acc, rd, a.g, i, j, k, a.tab);
-    if (a.act[2]) stencil_axis<T, N, C, 2, ADJ>(acc, rd, a.g, i, j, k, a.tab);
+    const T* tab = tab_of<LIT, T>(a);
+    if (a.act[0]) stencil_axis<T, N, C, 0, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 0));
+    if (a.act[1]) stencil_axis<T, N, C, 1, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 1));
+    if (a.act[2]) stencil_axis<T, N, C, 2, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 2));
 
     const Geom& gt = a.g[C];
     const long long p = lin(gt, i, j, k);
@@ -361,14 +387,14 @@ __global__ void __launch_bounds__(BLOCK) substep_kernel(const __grid_constant__ 
   double* pp = (a.partial != nullptr) ? part : nullptr;
   if (ok) {
     switch (cls) {
-      case 0: substep_cell<T, N, 0, ADJ>(a, i, j, k, face, pp); break;
-      case 1: substep_cell<T, N, 1, ADJ>(a, i, j, k, face, pp); break;
-      case 2: substep_cell<T, N, 2, ADJ>(a, i, j, k, face, pp); break;
-      case 3: substep_cell<T, N, 3, ADJ>(a, i, j, k, face, pp); break;
-      case 4: substep_cell<T, N, 4, ADJ>(a, i, j, k, face, pp); break;
-      case 5: substep_cell<T, N, 5, ADJ>(a, i, j, k, face, pp); break;
-      case 6: substep_cell<T, N, 6, ADJ>(a, i, j, k, face, pp); break;
-      default: substep_cell<T, N, 7, ADJ>(a, i, j, k, face, pp); break;
+      case 0: substep_cell<T, N, 0, ADJ, false>(a, i, j, k, face, pp); break;
+      case 1: substep_cell<T, N, 1, ADJ, false>(a, i, j, k, face, pp); break;
+      case 2: substep_cell<T, N, 2, ADJ, false>(a, i, j, k, face, pp); break;
+      case 3: substep_cell<T, N, 3, ADJ, false>(a, i, j, k, face, pp); break;
+      case 4: substep_cell<T, N, 4, ADJ, false>(a, i, j, k, face, pp); break;
+      case 5: substep_cell<T, N, 5, ADJ, false>(a, i, j, k, face, pp); break;
+      case 6: substep_cell<T, N, 6, ADJ, false>(a, i, j, k, face, pp); break;
+      default: substep_cell<T, N, 7, ADJ, false>(a, i, j, k, face, pp); break;
     }
   }
   if (a.partial != nullptr) {
@@ -397,8 +423,8 @@ __global__ void __launch_bounds__(BLOCK) substep_kernel(const __grid_constant__ 
 // --------------------------------------------------------------------------------------------
 // adjoint density kernel
 // --------------------------------------------------------------------------------------------
-template <class T, int N, int C>
-__device__ __forceinline__ void integrate_cell(const IntArgs<T, N>& a, int i, int j, int k, bool face) {
+template <class T, int N, int C, bool LIT, class A>
+__device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, bool face) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n == 0) {
     return;
@@ -407,9 +433,10 @@ __device__ __forceinline__ void integrate_cell(const IntArgs<T, N>& a, int i, in
     T acc[n];
 #pragma unroll
     for (int m = 0; m < n; ++m) acc[m] = T(0);
-    if (a.act[0]) stencil_axis<T, N, C, 0, false>(acc, a.u, a.g, i, j, k, a.tab);
-    if (a.act[1]) stencil_axis<T, N, C, 1, false>(acc, a.u, a.g, i, j, k, a.tab);
-    if (a.act[2]) stencil_axis<T, N, C, 2, false>(acc, a.u, a.g, i, j, k, a.tab);
+    const T* tab = tab_of<LIT, T>(a);
+    if (a.act[0]) stencil_axis<T, N, C, 0, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 0));
+    if (a.act[1]) stencil_axis<T, N, C, 1, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 1));
+    if (a.act[2]) stencil_axis<T, N, C, 2, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 2));
     const Geom& gt = a.g[C];
     const long long p = lin(gt, i, j, k);
     const T* rho = a.rho[C] + p;
@@ -479,14 +506,14 @@ __global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant_
   const int cls = a.seg[s].cls;
   const bool face = a.seg[s].kind == 1;
   switch (cls) {
-    case 0: integrate_cell<T, N, 0>(a, i, j, k, face); break;
-    case 1: integrate_cell<T, N, 1>(a, i, j, k, face); break;
-    case 2: integrate_cell<T, N, 2>(a, i, j, k, face); break;
-    case 3: integrate_cell<T, N, 3>(a, i, j, k, face); break;
-    case 4: integrate_cell<T, N, 4>(a, i, j, k, face); break;
-    case 5: integrate_cell<T, N, 5>(a, i, j, k, face); break;
-    case 6: integrate_cell<T, N, 6>(a, i, j, k, face); break;
-    default: integrate_cell<T, N, 7>(a, i, j, k, face); break;
+    case 0: integrate_cell<T, N, 0, false>(a, i, j, k, face); break;
+    case 1: integrate_cell<T, N, 1, false>(a, i, j, k, face); break;
+    case 2: integrate_cell<T, N, 2, false>(a, i, j, k, face); break;
+    case 3: integrate_cell<T, N, 3, false>(a, i, j, k, face); break;
+    case 4: integrate_cell<T, N, 4, false>(a, i, j, k, face); break;
+    case 5: integrate_cell<T, N, 5, false>(a, i, j, k, face); break;
+    case 6: integrate_cell<T, N, 6, false>(a, i, j, k, face); break;
+    default: integrate_cell<T, N, 7, false>(a, i, j, k, face); break;
   }
 }
 

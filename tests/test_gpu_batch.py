@@ -1,0 +1,97 @@
+"""Batched solves (pn_batch_*) against the CPU oracle: mixed orders, grids and step counts."""
+import numpy as np
+import pytest
+
+from pnepma_gb300 import capi, workloads
+from pnepma_gb300.problem import PN_FP32, PN_FP64
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, float).ravel()
+    b = np.asarray(b, float).ravel()
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def mixed_solves(precision):
+    out = [
+        workloads.small_case(dims=2, N=3, shape=(10, 8), n_steps=9, seed=1, precision=precision),
+        workloads.small_case(dims=2, N=3, shape=(12, 7), n_steps=5, seed=2, precision=precision),
+        workloads.small_case(dims=2, N=5, shape=(9, 9), n_steps=7, seed=3, precision=precision),
+        workloads.small_case(dims=1, N=7, shape=(20,), n_steps=11, seed=4, precision=precision),
+        workloads.small_case(dims=2, N=3, shape=(8, 11), n_steps=9, seed=5, precision=precision,
+                             elements=("Fe", "Cr", "Ni")),
+        workloads.small_case(dims=3, N=3, shape=(6, 5, 5), n_steps=4, seed=6, precision=precision),
+    ]
+    return out
+
+
+def run_batch(torch, solves, K=0):
+    descs, keep = [], []
+    for s in solves:
+        d, k = s.problem.descriptor(s.x_rays)
+        descs.append(d)
+        keep.append(k)
+    b = capi.Batch(descs, keep, checkpoint_stride=K)
+    ins, outs = [], []
+    for s in solves:
+        rho, noa, acs = s.inputs()
+        ins.append([torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (rho, noa, acs)])
+    I = [torch.zeros(len(s.x_rays), dtype=torch.float64, device="cuda") for s in solves]
+    b.forward([x[0].data_ptr() for x in ins], [x[1].data_ptr() for x in ins], [x[2].data_ptr() for x in ins],
+              [t.data_ptr() for t in I])
+    torch.cuda.synchronize()
+    Ih = [t.cpu().numpy() for t in I]
+    ib = [torch.from_numpy(np.linspace(1.0, 2.0, len(x)) / np.abs(x)).cuda() for x in Ih]
+    rb = [torch.zeros(x[0].numel(), dtype=torch.float64, device="cuda") for x in ins]
+    nb = [torch.zeros(x[1].numel(), dtype=torch.float64, device="cuda") for x in ins]
+    ab = [torch.zeros(x[2].numel(), dtype=torch.float64, device="cuda") for x in ins]
+    b.adjoint([t.data_ptr() for t in ib], [t.data_ptr() for t in rb], [t.data_ptr() for t in nb],
+              [t.data_ptr() for t in ab])
+    torch.cuda.synchronize()
+    info = b.info()
+    b.close()
+    return Ih, [t.cpu().numpy() for t in ib], [t.cpu().numpy() for t in rb], [t.cpu().numpy() for t in nb], \
+        [t.cpu().numpy() for t in ab], info
+
+
+def test_batch_fp64_matches_oracle(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    solves = mixed_solves(PN_FP64)
+    I, ib, rb, nb, ab, info = run_batch(torch, solves)
+    assert info.n_solves == len(solves) and info.n_groups == 3
+    for q, s in enumerate(solves):
+        rho, noa, acs = s.inputs()
+        d, k = s.problem.descriptor(s.x_rays)
+        I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[q])
+        assert rel(I[q], I_o) < 1e-10, q
+        assert rel(rb[q], rb_o) < 1e-10, q
+        assert rel(nb[q], nb_o) < 1e-10, q
+        assert rel(ab[q], ab_o) < 1e-10, q
+
+
+def test_batch_checkpoint_stride_does_not_change_results(gpu_lib):
+    torch = pytest.importorskip("torch")
+    solves = mixed_solves(PN_FP64)
+    ref = run_batch(torch, solves, K=1)
+    for K in (2, 3, 5):
+        got = run_batch(torch, solves, K=K)
+        for a, b in zip(got[:5], ref[:5]):
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y), K
+
+
+def test_batch_fp32_against_fp64_oracle(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    solves = mixed_solves(PN_FP32)
+    I, ib, rb, nb, ab, info = run_batch(torch, solves)
+    for q, s in enumerate(solves):
+        rho, noa, acs = s.inputs()
+        s.problem.precision = PN_FP64
+        d, k = s.problem.descriptor(s.x_rays)
+        I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[q])
+        assert rel(I[q], I_o) < 1e-4, q
+        assert rel(rb[q], rb_o) < 1e-3, q
+        assert rel(nb[q], nb_o) < 1e-3, q
+        assert rel(ab[q], ab_o) < 1e-3, q
