@@ -39,7 +39,7 @@ WORKLOAD = "2D 256x128 P11 Fe/Cr/Ni, 20 positions x {10,15,20} keV, forward+adjo
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--positions", type=int, default=20, help="beam positions per energy (20 = full workload)")
@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=3)
     ap.add_argument("--profile", action="store_true",
                     help="run one 10 keV solve (FP64 twice, FP32 once) for a profiler, print nothing else")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
     return ap.parse_args()
 
 
@@ -220,11 +222,6 @@ def run_ours(args):
         s.problem.precision = PN_FP64
         d, k = s.problem.descriptor(s.x_rays)
         handles64.append(capi.Handle(d, k))
-    for s in solves:
-        s.problem.precision = PN_FP32
-        d, k = s.problem.descriptor(s.x_rays)
-        handles32.append(capi.Handle(d, k))
-        s.problem.precision = PN_FP64
     sz = handles64[0].sizes
     outI = torch.zeros((nsol, nr), dtype=torch.float64, device=dev)
     outI32 = torch.zeros((nsol, nr), dtype=torch.float64, device=dev)
@@ -291,45 +288,56 @@ def run_ours(args):
         step_ms = float(t.item())
     value = world * nsol / (step_ms / 1e3)
 
-    # ---------------- FP32 batched: all 60 solves in flight (one stream per handle)
-    streams = [torch.cuda.Stream(device=dev) for _ in range(nsol)]
+    # ---------------- FP32 batched: all 60 solves in one batch (one launch per sub-step)
+    descs32, keep32 = [], []
+    for s in solves:
+        s.problem.precision = PN_FP32
+        d, k = s.problem.descriptor(s.x_rays)
+        descs32.append(d)
+        keep32.append(k)
+        s.problem.precision = PN_FP64
+    batch = capi.Batch(descs32, keep32)
     rb32 = [torch.zeros(sz.n_rho, dtype=torch.float64, device=dev) for _ in range(nsol)]
     nb32 = [torch.zeros(sz.n_noa, dtype=torch.float64, device=dev) for _ in range(nsol)]
     ab32 = [torch.zeros(max(sz.n_acs, 1), dtype=torch.float64, device=dev) for _ in range(nsol)]
+    p_rho = [d_rho.data_ptr()] * nsol
+    p_noa = [d_noa.data_ptr()] * nsol
+    p_acs = [d_acs.data_ptr()] * nsol
+    p_I32 = [outI32[i].data_ptr() for i in range(nsol)]
+    p_ib = [d_ibar[i].data_ptr() for i in range(nsol)]
+    p_rb = [t.data_ptr() for t in rb32]
+    p_nb = [t.data_ptr() for t in nb32]
+    p_ab = [t.data_ptr() for t in ab32]
 
     def batched_step():
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
             start = torch.cuda.Event(enable_timing=True)
+            mid = torch.cuda.Event(enable_timing=True)
+            end = torch.cuda.Event(enable_timing=True)
             start.record(stream)
-        ends = []
-        for i in range(nsol):
-            st = streams[i]
-            st.wait_event(start)
-            h = handles32[i]
-            h.forward_device(d_rho.data_ptr(), d_noa.data_ptr(), d_acs.data_ptr(), outI32[i].data_ptr(), st.cuda_stream)
-            h.adjoint_device(d_ibar[i].data_ptr(), rb32[i].data_ptr(), nb32[i].data_ptr(), ab32[i].data_ptr(),
-                             st.cuda_stream)
-            e = torch.cuda.Event(enable_timing=True)
-            e.record(st)
-            ends.append(e)
-        for e in ends:
-            stream.wait_event(e)
-        end = torch.cuda.Event(enable_timing=True)
-        end.record(stream)
-        return start, ends, end
+            batch.forward(p_rho, p_noa, p_acs, p_I32, sp)
+            mid.record(stream)
+            batch.adjoint(p_ib, p_rb, p_nb, p_ab, sp)
+            end.record(stream)
+        return start, mid, end
 
     for _ in range(args.warmup):
         batched_step()
     torch.cuda.synchronize()
-    b_ms, b_lat = [], []
+    b_ms, b_fwd = [], []
     for _ in range(args.steps):
-        start, ends, end = batched_step()
+        start, mid, end = batched_step()
         torch.cuda.synchronize()
         b_ms.append(start.elapsed_time(end))
-        b_lat += [start.elapsed_time(e) for e in ends]
+        b_fwd.append(start.elapsed_time(mid))
     b_step = float(np.mean(b_ms))
     fp32_value = world * nsol / (b_step / 1e3)
+    bytes32_step, _m = algorithmic_bytes_per_step(solves[0], 4)
+    fwd_bytes32 = bytes32_step * sum(s.problem.N_steps for s in solves)
+    fp32_fwd_gbs = fwd_bytes32 / (float(np.mean(b_fwd)) / 1e3) / 1e9
+    b_lat = b_ms   # every solve of the batch completes with the batch
+    binfo = batch.info()
 
     # accuracy of the FP32 batch against the FP64 plain results (same inputs)
     I64 = outI.cpu().numpy()
@@ -430,8 +438,15 @@ def run_ours(args):
                              "speedup_vs_fp64_plain": fp32_value / value,
                              "latency_ms": {"p50": float(np.percentile(b_lat, 50)),
                                             "p99": float(np.percentile(b_lat, 99))},
+                             "forward_ms": float(np.mean(b_fwd)),
                              "max_rel_err_intensity_vs_fp64": k_err, "max_rel_err_rho_bar_vs_fp64": g_err,
-                             "form": "60 FP32 handles in flight on 60 streams"},
+                             "checkpoint_stride": binfo.checkpoint_stride,
+                             "forward_roofline": {"bound": "hbm", "achieved": fp32_fwd_gbs,
+                                                  "peak": float(json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))).get("hbm_gbs", 6800.0)) if os.path.exists(os.path.join(HERE, "MEASURED_PEAKS.json")) else 6800.0,
+                                                  "unit": "GB/s",
+                                                  "note": "algorithmic bytes of all forward sub-steps of the 60 solves / forward time"},
+                             "kernels_per_step": binfo.forward_kernels + binfo.adjoint_kernels,
+                             "form": "one pn_batch: one launch per sub-step covers all 60 solves"},
             "moment_cell_updates_per_s": world * mcu / (step_ms / 1e3),
             "e2e": {"value": world * nsol / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -447,8 +462,9 @@ def run_ours(args):
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
-    for h in handles64 + handles32:
+    for h in handles64:
         h.close()
+    batch.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -479,10 +495,51 @@ def run_profile(args):
     h32.close()
 
 
+def run_profile_batch(args):
+    """FP32 batch of 16 beam positions at 10 keV (state 160 MB > L2), forward + adjoint twice, tapes
+    within 6 GiB."""
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.problem import PN_FP32
+    torch.cuda.set_device(0)
+    solves = workloads.config2(n_positions=16, energies=(10.0,), precision=PN_FP32)
+    descs, keep = [], []
+    for s in solves:
+        d, k = s.problem.descriptor(s.x_rays)
+        descs.append(d)
+        keep.append(k)
+    b = capi.Batch(descs, keep, memory_budget=6 << 30)
+    rho, noa, acs = solves[0].inputs()
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)
+    n = len(solves)
+    nr = len(solves[0].x_rays)
+    I = torch.zeros((n, nr), dtype=torch.float64, device="cuda")
+    ib = torch.ones((n, nr), dtype=torch.float64, device="cuda")
+    sz = capi.query_sizes(descs[0])
+    rb = [torch.zeros(sz.n_rho, dtype=torch.float64, device="cuda") for _ in range(n)]
+    nb = [torch.zeros(sz.n_noa, dtype=torch.float64, device="cuda") for _ in range(n)]
+    ab = [torch.zeros(sz.n_acs, dtype=torch.float64, device="cuda") for _ in range(n)]
+    for _ in range(2):
+        b.forward([d_rho.data_ptr()] * n, [d_noa.data_ptr()] * n, [d_acs.data_ptr()] * n, [I[i].data_ptr() for i in range(n)])
+        torch.cuda.synchronize()
+        ib.copy_(1.0 / I.abs())
+        b.adjoint([ib[i].data_ptr() for i in range(n)], [t.data_ptr() for t in rb], [t.data_ptr() for t in nb],
+                  [t.data_ptr() for t in ab])
+        torch.cuda.synchronize()
+    info = b.info()
+    print(json.dumps({"profile_batch": len(solves), "steps": solves[0].problem.N_steps,
+                      "stride": info.checkpoint_stride, "bytes": info.device_bytes,
+                      "kernels": info.forward_kernels + info.adjoint_kernels}))
+    b.close()
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
+    elif args.profile_batch:
+        run_profile_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -236,7 +236,7 @@ typedef struct pn_batch_options {
 
 typedef struct pn_batch_info {
   int32_t n_solves;
-  int32_t n_groups;           /* one per distinct order */
+  int32_t n_groups;           /* one per distinct (order, set of active axes) */
   int32_t checkpoint_stride;  /* largest stride in use */
   int32_t reserved;
   int64_t device_bytes;

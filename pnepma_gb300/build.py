@@ -72,12 +72,15 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     objs.append(o)
     if force or _stale(o, deps + [noalloc]):
         jobs.append((noalloc, o, [], extra))
-    order_src = os.path.join(CSRC, "pn_order.cu")
-    for N in codegen.ORDERS:
-        o = os.path.join(OUT, f"pn_order_{N}.o")
-        objs.append(o)
-        if force or _stale(o, deps + [order_src]):
-            jobs.append((order_src, o, [f"-DPN_ORDER={N}"], extra))
+    for unit in ("pn_order", "pn_order_batch"):
+        src = os.path.join(CSRC, unit + ".cu")
+        for N in codegen.ORDERS:
+            o = os.path.join(OUT, f"{unit}_{N}.o")
+            objs.append(o)
+            if force or _stale(o, deps + [src]):
+                jobs.append((src, o, [f"-DPN_ORDER={N}"], extra))
+    # longest units first so the parallel build finishes sooner
+    jobs.sort(key=lambda j: -int(next((d.split("=")[1] for d in j[2] if d.startswith("-DPN_ORDER=")), "0")))
     if jobs:
         workers = max(1, min(len(jobs), os.cpu_count() or 1))
         with ThreadPoolExecutor(workers) as ex:

@@ -14,7 +14,7 @@
 #include "pn_batch_base.h"
 
 namespace pn {
-#define PN_DECL(N) BatchGroupBase* make_batch_group_##N(int precision);
+#define PN_DECL(N) BatchGroupBase* make_batch_group_##N(int precision, int dims);
 PN_FOR_EACH_ORDER(PN_DECL)
 #undef PN_DECL
 void set_last_error(const std::string& msg);
@@ -41,11 +41,11 @@ static int batch_fail(const std::string& m, int code) {
   return code;
 }
 
-static pn::BatchGroupBase* make_group(int N, int precision) {
+static pn::BatchGroupBase* make_group(int N, int precision, int dims) {
   switch (N) {
 #define PN_CASE(K) \
   case K:          \
-    return pn::make_batch_group_##K(precision);
+    return pn::make_batch_group_##K(precision, dims);
     PN_FOR_EACH_ORDER(PN_CASE)
 #undef PN_CASE
     default:
@@ -80,11 +80,14 @@ int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_optio
       return batch_fail("no CUDA device is available", PN_ERR_NO_DEVICE);
     }
     const int precision = descs[0]->precision;
-    std::map<int, std::vector<int>> by_order;
+    // groups: same order and same set of active axes
+    std::map<std::pair<int, int>, std::vector<int>> by_order;
     for (int i = 0; i < n; ++i) {
       if (!descs[i]) return batch_fail("descriptor is NULL", PN_ERR_INVALID);
       if (descs[i]->precision != precision) return batch_fail("all descriptors of a batch share one precision", PN_ERR_INVALID);
-      by_order[descs[i]->order].push_back(i);
+      int dims = 0;
+      for (int k = 0; k < 3; ++k) dims |= (descs[i]->n_points[k] > 1 ? 1 : 0) << k;
+      by_order[{descs[i]->order, dims}].push_back(i);
     }
     long long budget = options ? options->memory_budget : 0;
     const int K = options ? options->checkpoint_stride : 0;
@@ -99,10 +102,11 @@ int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_optio
     b->io.resize(n);
     // share the budget between the groups in proportion to their solve counts
     for (auto& kv : by_order) {
-      pn::BatchGroupBase* g = make_group(kv.first, precision);
+      pn::BatchGroupBase* g = make_group(kv.first.first, precision, kv.first.second);
       if (!g) {
         delete b;
-        return batch_fail("P_N order " + std::to_string(kv.first) + " is not compiled into this build", PN_ERR_UNSUPPORTED);
+        return batch_fail("P_N order " + std::to_string(kv.first.first) + " is not compiled into this build",
+                          PN_ERR_UNSUPPORTED);
       }
       b->groups.push_back(g);
       const long long share = budget * (long long)kv.second.size() / n;

@@ -164,56 +164,52 @@ __device__ __forceinline__ T* bslot(const BInst<T>& I, int j, int K, bool segmen
   return I.slots + (long long)(1 + I.n_ck + w) * I.slot_elems;
 }
 
-template <class T, int N, bool ADJ>
+// Copy solve `q`'s descriptor into shared memory with every thread of the block (coalesced
+// 4-byte words), so the per-block arguments can then be filled in parallel from shared memory.
+template <class T>
+__device__ __forceinline__ const BInst<T>& stage_instance(const BInst<T>* inst, int q, unsigned int* raw) {
+  constexpr int W = (int)(sizeof(BInst<T>) / 4);
+  const unsigned int* src = reinterpret_cast<const unsigned int*>(inst + q);
+  for (int w = threadIdx.x; w < W; w += BLOCK) raw[w] = src[w];
+  __syncthreads();
+  return *reinterpret_cast<const BInst<T>*>(raw);
+}
+
+template <class T, int N, bool ADJ, int DIMS>
 __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_constant__ BLaunch<T> L) {
   __shared__ BSub<T, N> a;
-  __shared__ int sh_seg, sh_lb, sh_inst;
-  if (threadIdx.x == 0) {
-    const BTile tl = L.tiles[blockIdx.x];
-    const BInst<T>& I = L.inst[tl.inst];
-    sh_seg = tl.seg;
-    sh_lb = tl.lb;
-    sh_inst = tl.inst;
-    const int par = L.list;
-    T* own_rd;
-    T* own_wr;
-    T* from_rd;
-    int row;
-    if (!ADJ) {
-      const bool segment = L.mode == BM_RECOMPUTE;
-      const int m = L.j / L.K;
-      T* src = bslot(I, L.j + 1, L.K, segment, m);
-      T* dst = bslot(I, L.j, L.K, segment, m);
-      own_rd = (L.sub == 3) ? dst : src;
-      own_wr = dst;
-      from_rd = (L.sub == 1) ? src : dst;
-      row = I.ns - L.j - 1;
-      a.bc = I.fwd_bc[row];
-      for (int e = 0; e < MAXE; ++e) {
-        a.s[e] = e < I.ne ? I.fwd_s[row * I.ne + e] : T(0);
-        for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.fwd_c[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
-      }
-      a.adjoint_source = 0;
-    } else {
-      own_rd = own_wr = from_rd = I.lam;
-      row = L.j;
-      a.bc = 0.0;
-      for (int e = 0; e < MAXE; ++e) {
-        a.s[e] = e < I.ne ? I.adj_s[row * I.ne + e] : T(0);
-        for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.adj_c[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
-      }
-      a.adjoint_source = 1;
-      for (int r = 0; r < MAXR; ++r) a.sig_src[r] = r < I.nr ? I.adj_src[(long long)row * I.nr + r] : 0.0;
-    }
-    for (int c = 0; c < 8; ++c) {
-      a.g[c] = I.g[c];
-      const bool tgt = class_parity_d(c) == par;
-      a.rd[c] = I.active[c] ? (tgt ? own_rd : from_rd) + I.dev_off[c] : nullptr;
-      a.wr[c] = I.active[c] ? own_wr + I.dev_off[c] : nullptr;
-      a.rho[c] = I.rho[c];
-      for (int k = 0; k < 3; ++k) a.bmat[k][c] = ADJ ? I.bmat_a[k][c] : I.bmat_f[k][c];
-      a.beam[c] = I.beam[c];
-    }
+  __shared__ __align__(16) unsigned int raw[sizeof(BInst<T>) / 4 + 1];
+  const BTile tl = L.tiles[blockIdx.x];
+  const BInst<T>& I = stage_instance(L.inst, tl.inst, raw);
+  const int par = L.list;
+  const int tid = threadIdx.x;
+  int row;
+  T* own_rd;
+  T* own_wr;
+  T* from_rd;
+  if (!ADJ) {
+    const bool segment = L.mode == BM_RECOMPUTE;
+    const int m = L.j / L.K;
+    T* src = bslot(I, L.j + 1, L.K, segment, m);
+    T* dst = bslot(I, L.j, L.K, segment, m);
+    own_rd = (L.sub == 3) ? dst : src;
+    own_wr = dst;
+    from_rd = (L.sub == 1) ? src : dst;
+    row = I.ns - L.j - 1;
+  } else {
+    own_rd = own_wr = from_rd = I.lam;
+    row = L.j;
+  }
+  if (tid < 8) {
+    const int c = tid;
+    a.g[c] = I.g[c];
+    const bool tgt = class_parity_d(c) == par;
+    a.rd[c] = I.active[c] ? (tgt ? own_rd : from_rd) + I.dev_off[c] : nullptr;
+    a.wr[c] = I.active[c] ? own_wr + I.dev_off[c] : nullptr;
+    a.rho[c] = I.rho[c];
+    for (int k = 0; k < 3; ++k) a.bmat[k][c] = ADJ ? I.bmat_a[k][c] : I.bmat_f[k][c];
+    a.beam[c] = I.beam[c];
+  } else if (tid == 8) {
     for (int k = 0; k < 3; ++k) {
       a.act[k] = I.act[k];
       a.inv_h[k] = I.inv_h[k];
@@ -226,34 +222,40 @@ __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_const
     a.noa = I.noa;
     a.ibar = I.ibar;
     a.wint = I.wint;
+    a.adjoint_source = ADJ ? 1 : 0;
+    a.bc = ADJ ? 0.0 : I.fwd_bc[row];
     for (int r = 0; r < MAXR; ++r) a.xel[r] = I.xel[r];
+  } else if (tid >= 16 && tid < 16 + MAXR) {
+    const int r = tid - 16;
+    a.sig_src[r] = (ADJ && r < I.nr) ? I.adj_src[(long long)row * I.nr + r] : 0.0;
+  } else if (tid >= 24 && tid < 24 + MAXE) {
+    const int e = tid - 24;
+    a.s[e] = e < I.ne ? (ADJ ? I.adj_s[row * I.ne + e] : I.fwd_s[row * I.ne + e]) : T(0);
+  } else if (tid >= 32 && tid < 32 + MAXE * (N + 1)) {
+    const int e = (tid - 32) / (N + 1), l = (tid - 32) % (N + 1);
+    const T* cc = ADJ ? I.adj_c : I.fwd_c;
+    a.c[e][l] = e < I.ne ? cc[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
   }
   __syncthreads();
-  const Seg& sg = L.inst[sh_inst].seg[L.list][sh_seg];
-  int i = 0, j = 0, k = 0;
-  bool ok;
-  {
-    Seg one = sg;
-    one.block0 = 0;
-    int s0;
-    ok = locate(&one, 1, sh_lb, threadIdx.x, s0, i, j, k);
-  }
-  const bool face = sg.kind == 1;
-  const int cls = sg.cls;
+  Seg one = I.seg[L.list][tl.seg];
+  one.block0 = 0;
+  int i = 0, j = 0, k = 0, s0;
+  const bool ok = locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k);
+  const bool face = one.kind == 1;
   double part[MAXR];
 #pragma unroll
   for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
   double* pp = (L.partial != nullptr) ? part : nullptr;
   if (ok) {
-    switch (cls) {
-      case 0: substep_cell<T, N, 0, ADJ, true>(a, i, j, k, face, pp); break;
-      case 1: substep_cell<T, N, 1, ADJ, true>(a, i, j, k, face, pp); break;
-      case 2: substep_cell<T, N, 2, ADJ, true>(a, i, j, k, face, pp); break;
-      case 3: substep_cell<T, N, 3, ADJ, true>(a, i, j, k, face, pp); break;
-      case 4: substep_cell<T, N, 4, ADJ, true>(a, i, j, k, face, pp); break;
-      case 5: substep_cell<T, N, 5, ADJ, true>(a, i, j, k, face, pp); break;
-      case 6: substep_cell<T, N, 6, ADJ, true>(a, i, j, k, face, pp); break;
-      default: substep_cell<T, N, 7, ADJ, true>(a, i, j, k, face, pp); break;
+    switch (one.cls) {
+      case 0: substep_cell<T, N, 0, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 1: substep_cell<T, N, 1, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 2: substep_cell<T, N, 2, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 3: substep_cell<T, N, 3, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 4: substep_cell<T, N, 4, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 5: substep_cell<T, N, 5, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      case 6: substep_cell<T, N, 6, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      default: substep_cell<T, N, 7, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
     }
   }
   if (L.partial != nullptr) {
@@ -276,27 +278,25 @@ __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_const
   }
 }
 
-template <class T, int N>
+template <class T, int N, int DIMS>
 __global__ void __launch_bounds__(BLOCK) batch_integrate_kernel(const __grid_constant__ BLaunch<T> L) {
   __shared__ BInt<T, N> a;
-  __shared__ int sh_seg, sh_lb, sh_inst;
-  if (threadIdx.x == 0) {
-    const BTile tl = L.tiles[blockIdx.x];
-    const BInst<T>& I = L.inst[tl.inst];
-    sh_seg = tl.seg;
-    sh_lb = tl.lb;
-    sh_inst = tl.inst;
-    const int it = L.j;   // iteration; it == ns is the final accumulation on the zero state
+  __shared__ __align__(16) unsigned int raw[sizeof(BInst<T>) / 4 + 1];
+  const BTile tl = L.tiles[blockIdx.x];
+  const BInst<T>& I = stage_instance(L.inst, tl.inst, raw);
+  const int it = L.j;   // iteration; it == ns is the final accumulation on the zero state
+  const int tid = threadIdx.x;
+  if (tid < 8) {
+    const int c = tid;
     T* u = bslot(I, it, L.K, true, it / L.K);
-    for (int c = 0; c < 8; ++c) {
-      a.g[c] = I.g[c];
-      a.u[c] = I.active[c] ? u + I.dev_off[c] : nullptr;
-      a.lam[c] = I.active[c] ? I.lam + I.dev_off[c] : nullptr;
-      a.rho[c] = I.rho[c];
-      a.rbar[c] = I.rbar[c];
-      for (int k = 0; k < 3; ++k) a.bmat[k][c] = I.bmat_f[k][c];
-      a.beam[c] = I.beam[c];
-    }
+    a.g[c] = I.g[c];
+    a.u[c] = I.active[c] ? u + I.dev_off[c] : nullptr;
+    a.lam[c] = I.active[c] ? I.lam + I.dev_off[c] : nullptr;
+    a.rho[c] = I.rho[c];
+    a.rbar[c] = I.rbar[c];
+    for (int k = 0; k < 3; ++k) a.bmat[k][c] = I.bmat_f[k][c];
+    a.beam[c] = I.beam[c];
+  } else if (tid == 8) {
     for (int k = 0; k < 3; ++k) {
       a.act[k] = I.act[k];
       a.inv_h[k] = I.inv_h[k];
@@ -306,37 +306,37 @@ __global__ void __launch_bounds__(BLOCK) batch_integrate_kernel(const __grid_con
     a.bc = I.int_bc[it];
     a.scale_g = I.scale_g;
     a.wfac = I.int_wfac[it];
-    for (int e = 0; e < MAXE; ++e) {
-      a.s[e] = e < I.ne ? I.int_s[(long long)it * I.ne + e] : T(0);
-      for (int l = 0; l <= N; ++l) a.c[e][l] = e < I.ne ? I.int_c[((long long)it * I.ne + e) * (N + 1) + l] : T(0);
-    }
     a.acs = I.acs;
     a.noa = I.noa;
     a.ibar = I.ibar;
     a.acs_bar = I.acs_bar;
     a.noa_bar = I.noa_bar;
-    for (int r = 0; r < MAXR; ++r) {
-      a.xel[r] = I.xel[r];
-      a.coef[r] = r < I.nr ? I.int_coef[(long long)it * I.nr + r] : 0.0;
-    }
+    for (int r = 0; r < MAXR; ++r) a.xel[r] = I.xel[r];
+  } else if (tid >= 16 && tid < 16 + MAXR) {
+    const int r = tid - 16;
+    a.coef[r] = r < I.nr ? I.int_coef[(long long)it * I.nr + r] : 0.0;
+  } else if (tid >= 24 && tid < 24 + MAXE) {
+    const int e = tid - 24;
+    a.s[e] = e < I.ne ? I.int_s[(long long)it * I.ne + e] : T(0);
+  } else if (tid >= 32 && tid < 32 + MAXE * (N + 1)) {
+    const int e = (tid - 32) / (N + 1), l = (tid - 32) % (N + 1);
+    a.c[e][l] = e < I.ne ? I.int_c[((long long)it * I.ne + e) * (N + 1) + l] : T(0);
   }
   __syncthreads();
-  const Seg& sg = L.inst[sh_inst].seg[2][sh_seg];
-  int i = 0, j = 0, k = 0;
-  Seg one = sg;
+  Seg one = I.seg[2][tl.seg];
   one.block0 = 0;
-  int s0;
-  if (!locate(&one, 1, sh_lb, threadIdx.x, s0, i, j, k)) return;
-  const bool face = sg.kind == 1;
-  switch (sg.cls) {
-    case 0: integrate_cell<T, N, 0, true>(a, i, j, k, face); break;
-    case 1: integrate_cell<T, N, 1, true>(a, i, j, k, face); break;
-    case 2: integrate_cell<T, N, 2, true>(a, i, j, k, face); break;
-    case 3: integrate_cell<T, N, 3, true>(a, i, j, k, face); break;
-    case 4: integrate_cell<T, N, 4, true>(a, i, j, k, face); break;
-    case 5: integrate_cell<T, N, 5, true>(a, i, j, k, face); break;
-    case 6: integrate_cell<T, N, 6, true>(a, i, j, k, face); break;
-    default: integrate_cell<T, N, 7, true>(a, i, j, k, face); break;
+  int i = 0, j = 0, k = 0, s0;
+  if (!locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k)) return;
+  const bool face = one.kind == 1;
+  switch (one.cls) {
+    case 0: integrate_cell<T, N, 0, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 1: integrate_cell<T, N, 1, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 2: integrate_cell<T, N, 2, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 3: integrate_cell<T, N, 3, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 4: integrate_cell<T, N, 4, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 5: integrate_cell<T, N, 5, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    case 6: integrate_cell<T, N, 6, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    default: integrate_cell<T, N, 7, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
   }
 }
 
@@ -483,7 +483,7 @@ __global__ void batch_store_kernel(const BInst<T>* __restrict__ inst, const BIo*
 // ----------------------------------------------------------------------------------------------
 
 
-template <class T, int N>
+template <class T, int N, int DIMS>
 class BatchGroup : public BatchGroupBase {
  public:
   std::vector<Layout> Ls;
@@ -829,11 +829,11 @@ class BatchGroup : public BatchGroupBase {
     a.K = K;
     a.partial = part;
     if (integ)
-      batch_integrate_kernel<T, N><<<nt, BLOCK, 0, cap>>>(a);
+      batch_integrate_kernel<T, N, DIMS><<<nt, BLOCK, 0, cap>>>(a);
     else if (adj)
-      batch_substep_kernel<T, N, true><<<nt, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, true, DIMS><<<nt, BLOCK, 0, cap>>>(a);
     else
-      batch_substep_kernel<T, N, false><<<nt, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, false, DIMS><<<nt, BLOCK, 0, cap>>>(a);
     PN_CUDA(cudaGetLastError());
     ++nl;
     return PN_OK;

@@ -295,10 +295,86 @@ __device__ __forceinline__ T invh_of(const A& a, int d) {
   else return T(1);
 }
 
+// Neighbour values of one axis, loaded before any arithmetic so that every load of a cell is in
+// flight at once (used when the active axes are known at compile time, DIMS != 0).
+template <class T, int N, int C, int D>
+struct Nbr {
+  static constexpr int F = C ^ (4 >> D);
+  static constexpr int nf = Ord<N>::n(F);
+  T r[nf > 0 ? nf : 1];
+  T l[nf > 0 ? nf : 1];
+};
+
+template <class T, int N, int C, int D>
+__device__ __forceinline__ void load_nbr(Nbr<T, N, C, D>& v, T* const* rd, const Geom* g, int i, int j, int k) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nf > 0 && Ord<N>::n(C) > 0) {
+    const Geom& gf = g[F];
+    int r3[3] = {i, j, k};
+    int l3[3] = {i, j, k};
+    if ((C >> (2 - D)) & 1) l3[D] -= 1;
+    else r3[D] += 1;
+    const T* fr = rd[F] + lin(gf, r3[0], r3[1], r3[2]);
+    const T* fl = rd[F] + lin(gf, l3[0], l3[1], l3[2]);
+    const long long ms = gf.ms;
+#pragma unroll
+    for (int q = 0; q < nf; ++q) {
+      v.r[q] = fr[q * ms];
+      v.l[q] = fl[q * ms];
+    }
+  }
+}
+
+template <class T, int N, int C, int D, bool NEG, bool LIT>
+__device__ __forceinline__ void apply_nbr(T* acc, const Nbr<T, N, C, D>& v, const T* tab, T inv_h) {
+  constexpr int F = C ^ (4 >> D);
+  if constexpr (Ord<N>::n(F) > 0 && Ord<N>::n(C) > 0) {
+    auto diff = [&](int q) -> T {
+      const T d = NEG ? (v.l[q] - v.r[q]) : (v.r[q] - v.l[q]);
+      if constexpr (LIT) return d * inv_h;
+      else return d;
+    };
+    constexpr int off = Ord<N>::off(C, D);
+    auto coef = [&](int kk, double lit) -> T {
+      if constexpr (LIT) {
+        (void)kk;
+        return T(lit);
+      } else {
+        (void)lit;
+        return tab[off + kk];
+      }
+    };
+    Adv<N, C, D>::template apply<T>(acc, diff, coef);
+  }
+}
+
+// advection sum of one cell: DIMS == 0 checks the active axes at run time and loads while it
+// accumulates; DIMS != 0 (bit d = axis d active) loads every neighbour first
+template <class T, int N, int C, bool NEG, bool LIT, int DIMS, class A>
+__device__ __forceinline__ void advection_sum(T* acc, const A& a, T* const* rd, int i, int j, int k) {
+  const T* tab = tab_of<LIT, T>(a);
+  if constexpr (DIMS == 0) {
+    if (a.act[0]) stencil_axis<T, N, C, 0, NEG, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 0));
+    if (a.act[1]) stencil_axis<T, N, C, 1, NEG, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 1));
+    if (a.act[2]) stencil_axis<T, N, C, 2, NEG, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 2));
+  } else {
+    Nbr<T, N, C, 0> vx;
+    Nbr<T, N, C, 1> vy;
+    Nbr<T, N, C, 2> vz;
+    if constexpr ((DIMS & 1) != 0) load_nbr<T, N, C, 0>(vx, rd, a.g, i, j, k);
+    if constexpr ((DIMS & 2) != 0) load_nbr<T, N, C, 1>(vy, rd, a.g, i, j, k);
+    if constexpr ((DIMS & 4) != 0) load_nbr<T, N, C, 2>(vz, rd, a.g, i, j, k);
+    if constexpr ((DIMS & 1) != 0) apply_nbr<T, N, C, 0, NEG, LIT>(acc, vx, tab, invh_of<LIT, T>(a, 0));
+    if constexpr ((DIMS & 2) != 0) apply_nbr<T, N, C, 1, NEG, LIT>(acc, vy, tab, invh_of<LIT, T>(a, 1));
+    if constexpr ((DIMS & 4) != 0) apply_nbr<T, N, C, 2, NEG, LIT>(acc, vz, tab, invh_of<LIT, T>(a, 2));
+  }
+}
+
 // --------------------------------------------------------------------------------------------
 // sub-step kernel
 // --------------------------------------------------------------------------------------------
-template <class T, int N, int C, bool ADJ, bool LIT, class A>
+template <class T, int N, int C, bool ADJ, bool LIT, class A, int DIMS = 0>
 __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bool face, double* part) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n == 0) {
@@ -307,16 +383,19 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
     T* const* rd = a.rd;
     if (face) ghosts_for_cell<T, N, C>(const_cast<T* const*>(rd), a.g, a.act, a.bmat, a.beam,
                                        a.bc * a.scale_g, !ADJ, i, j, k);
+    const Geom& gt = a.g[C];
+    const long long p = lin(gt, i, j, k);
+    T upre[DIMS != 0 ? n : 1];
+    if constexpr (DIMS != 0) {
+      const T* uo0 = a.rd[C] + p;
+#pragma unroll
+      for (int m = 0; m < n; ++m) upre[m] = uo0[m * gt.ms];
+    }
     T acc[n];
 #pragma unroll
     for (int m = 0; m < n; ++m) acc[m] = T(0);
-    const T* tab = tab_of<LIT, T>(a);
-    if (a.act[0]) stencil_axis<T, N, C, 0, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 0));
-    if (a.act[1]) stencil_axis<T, N, C, 1, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 1));
-    if (a.act[2]) stencil_axis<T, N, C, 2, ADJ, LIT>(acc, rd, a.g, i, j, k, tab, invh_of<LIT, T>(a, 2));
+    advection_sum<T, N, C, ADJ, LIT, DIMS>(acc, a, rd, i, j, k);
 
-    const Geom& gt = a.g[C];
-    const long long p = lin(gt, i, j, k);
     const T* rho = a.rho[C] + p;
     T rr[MAXE];
     T S = T(0);
@@ -357,7 +436,9 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
 #pragma unroll
     for (int m = 0; m < n; ++m) {
       const int l = degree_of<N, C>(m);
-      const T u = uo[m * gt.ms];
+      T u;
+      if constexpr (DIMS != 0) u = upre[m];
+      else u = uo[m * gt.ms];
       const T q = (m == 0) ? q0 : T(0);
       const T num = (q - acc[m]) - Cl[l] * u;
       const T du = num * invS * ph[l];
@@ -423,22 +504,30 @@ __global__ void __launch_bounds__(BLOCK) substep_kernel(const __grid_constant__ 
 // --------------------------------------------------------------------------------------------
 // adjoint density kernel
 // --------------------------------------------------------------------------------------------
-template <class T, int N, int C, bool LIT, class A>
+template <class T, int N, int C, bool LIT, class A, int DIMS = 0>
 __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, bool face) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n == 0) {
     return;
   } else {
     if (face) ghosts_for_cell<T, N, C>(a.u, a.g, a.act, a.bmat, a.beam, a.bc * a.scale_g, true, i, j, k);
+    const Geom& gt = a.g[C];
+    const long long p = lin(gt, i, j, k);
+    T upre[DIMS != 0 ? n : 1];
+    T lpre[DIMS != 0 ? n : 1];
+    if constexpr (DIMS != 0) {
+      const T* u0 = a.u[C] + p;
+      const T* l0 = a.lam[C] + p;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        upre[m] = u0[m * gt.ms];
+        lpre[m] = l0[m * gt.ms];
+      }
+    }
     T acc[n];
 #pragma unroll
     for (int m = 0; m < n; ++m) acc[m] = T(0);
-    const T* tab = tab_of<LIT, T>(a);
-    if (a.act[0]) stencil_axis<T, N, C, 0, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 0));
-    if (a.act[1]) stencil_axis<T, N, C, 1, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 1));
-    if (a.act[2]) stencil_axis<T, N, C, 2, false, LIT>(acc, a.u, a.g, i, j, k, tab, invh_of<LIT, T>(a, 2));
-    const Geom& gt = a.g[C];
-    const long long p = lin(gt, i, j, k);
+    advection_sum<T, N, C, false, LIT, DIMS>(acc, a, a.u, i, j, k);
     const T* rho = a.rho[C] + p;
     T rr[MAXE];
     T S = T(0);
@@ -469,8 +558,14 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
 #pragma unroll
     for (int m = 0; m < n; ++m) {
       const int l = degree_of<N, C>(m);
-      const T u = uu[m * gt.ms];
-      const T lm = la[m * gt.ms];
+      T u, lm;
+      if constexpr (DIMS != 0) {
+        u = upre[m];
+        lm = lpre[m];
+      } else {
+        u = uu[m * gt.ms];
+        lm = la[m * gt.ms];
+      }
       const T du = (-acc[m] - Cl[l] * u) * invS;
       P = fma(lm, du, P);
       R[l] = fma(lm, u, R[l]);

@@ -1,6 +1,5 @@
 // pn_order.cu -- instantiates the solver for one P_N order (compiled once per order with
 // -DPN_ORDER=N so the orders build in parallel).
-#include "pn_batch.cuh"
 #include "pn_noalloc.cuh"
 #include "pn_solver.cuh"
 
@@ -15,11 +14,6 @@ namespace pn {
 SolverBase* PN_CAT(make_solver_, PN_ORDER)(int precision) {
   if (precision == PN_FP32) return new Solver<float, PN_ORDER>();
   return new Solver<double, PN_ORDER>();
-}
-
-BatchGroupBase* PN_CAT(make_batch_group_, PN_ORDER)(int precision) {
-  if (precision == PN_FP32) return new BatchGroup<float, PN_ORDER>();
-  return new BatchGroup<double, PN_ORDER>();
 }
 
 int PN_CAT(noalloc_forward_, PN_ORDER)(const pn_desc* d, unsigned char* scratch, size_t cap, const double* rho,

@@ -60,7 +60,7 @@ def test_batch_fp64_matches_oracle(gpu_lib, oracle):
     torch = pytest.importorskip("torch")
     solves = mixed_solves(PN_FP64)
     I, ib, rb, nb, ab, info = run_batch(torch, solves)
-    assert info.n_solves == len(solves) and info.n_groups == 3
+    assert info.n_solves == len(solves) and info.n_groups == 4
     for q, s in enumerate(solves):
         rho, noa, acs = s.inputs()
         d, k = s.problem.descriptor(s.x_rays)
