@@ -252,9 +252,86 @@ int pn_batch_adjoint(pn_batch* b, const double* const* intensities_bar, double* 
 int pn_batch_query(const pn_batch* b, pn_batch_info* info);
 void pn_batch_destroy(pn_batch* b);
 
+/*
+ * Served solves (no counterpart in the reference: its reconstruction loops call calc_intensities
+ * and the pullback one beam position and energy at a time, scripts/reconstructions_1d.jl:56-185,
+ * scripts/2d_full_reconstruction_test.jl:104-234).  A request is a list of solves -- e.g. one
+ * Gauss-Newton iteration's beam positions x energies, forward and adjoint -- submitted from any
+ * thread.  One scheduler thread per server admits waiting requests in arrival order as wave slots
+ * and room in the memory budget free up, merging those waiting into one batched wave
+ * (pn_batch_create's engine; same precision and mode), and runs each wave on its own streams, so
+ * requests admitted while others are on the GPU overlap with them.  Each solve's result does not
+ * depend on which other solves share its wave.  All device memory of a wave (tables, tapes,
+ * checkpoints, inputs, outputs) is carved from one allocation of memory_budget bytes made by
+ * pn_server_create; releasing it never synchronises the device.
+ *
+ * Buffers are the caller's HOST buffers with the layouts of pn_forward / pn_adjoint.  The server
+ * reads the descriptors, their tables and the inputs when it admits the request and writes the
+ * outputs when the request completes: every pointer in the request must stay valid until
+ * pn_poll or pn_wait reports the ticket done.  Inputs passed by the same pointer to several solves
+ * of a wave are uploaded once.
+ */
+typedef struct pn_server pn_server;
+
+typedef struct pn_server_options {
+  int64_t memory_budget;      /* device bytes reserved for the waves; 0 = half of the free memory */
+  int32_t max_waves;          /* waves on the GPU at once; 0 = 4 */
+  int32_t max_wave_solves;    /* solves merged into one wave; 0 = 1024 */
+  int32_t checkpoint_stride;  /* 0 = chosen per wave from its share of the budget */
+  int32_t reserved[3];
+} pn_server_options;
+
+typedef struct pn_request {
+  int32_t n_solves;
+  int32_t adjoint;                        /* 1: forward then adjoint; 0: forward only */
+  const pn_desc* const* descs;            /* [n_solves], one precision */
+  const double* const* rho;               /* [n_solves] x [n_rho] */
+  const double* const* noa;               /* [n_solves] x [n_eee_cells][n_e] */
+  const double* const* acs;               /* [n_solves] x [n_eee_cells][n_r] */
+  const double* const* intensities_bar;   /* [n_solves] x [n_r]; read when adjoint = 1 */
+  double* const* intensities;             /* [n_solves] x [n_r] out */
+  double* const* rho_bar;                 /* outs written when adjoint = 1 */
+  double* const* noa_bar;
+  double* const* acs_bar;
+} pn_request;
+
+typedef struct pn_ticket_info {
+  int32_t done;       /* 1 once the outputs are written */
+  int32_t status;     /* pn_status of the request once done */
+  int32_t wave;       /* wave the request ran in; -1 while waiting */
+  int32_t reserved;
+  double queued_ms;   /* submission to admission (-1 while waiting) */
+  double total_ms;    /* submission to outputs written (-1 until done) */
+} pn_ticket_info;
+
+typedef struct pn_server_info {
+  int64_t memory_budget;
+  int64_t bytes_in_use;
+  int64_t peak_bytes;
+  int64_t requests_submitted;
+  int64_t requests_done;
+  int64_t solves_done;
+  int64_t waves_launched;
+  int32_t waves_in_flight;
+  int32_t max_waves_in_flight;   /* most waves on the GPU at once so far */
+} pn_server_info;
+
+int pn_server_create(const pn_server_options* options, pn_server** out);
+/* Queue a request; *ticket identifies it.  Fails (PN_ERR_INVALID) only for a malformed request;
+   device and budget errors are reported by pn_poll / pn_wait. */
+int pn_submit(pn_server* s, const pn_request* req, uint64_t* ticket);
+/* Non-blocking state of a ticket; a failed request's message goes to pn_last_error(NULL). */
+int pn_poll(pn_server* s, uint64_t ticket, pn_ticket_info* info);
+/* Block until the ticket is done (timeout_ms < 0: no limit) and return its status, or
+   PN_ERR_TIMEOUT.  A failed request's message goes to pn_last_error(NULL). */
+int pn_wait(pn_server* s, uint64_t ticket, int64_t timeout_ms);
+int pn_server_query(pn_server* s, pn_server_info* info);
+/* Requests not yet admitted fail with PN_ERR_STATE; running waves are completed first. */
+void pn_server_destroy(pn_server* s);
+
 /* Human-readable description of the last error on this handle (or, when h is NULL, of the last
    failed call in this thread that has no handle: pn_create, pn_query_sizes, pn_batch_*,
-   pn_forward_noalloc).  Never NULL. */
+   pn_forward_noalloc, pn_server_*, pn_submit, pn_poll, pn_wait).  Never NULL. */
 const char* pn_last_error(const pn_handle* h);
 
 /* ABI version and the compiled P_N orders (bit N set when order N is available). */

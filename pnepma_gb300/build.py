@@ -62,16 +62,12 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     objs.append(o)
     if force or _stale(o, deps + [capi]):
         jobs.append((capi, o, [], extra))
-    batch = os.path.join(CSRC, "pn_batch.cu")
-    o = os.path.join(OUT, "pn_batch.o")
-    objs.append(o)
-    if force or _stale(o, deps + [batch]):
-        jobs.append((batch, o, [], extra))
-    noalloc = os.path.join(CSRC, "pn_noalloc.cu")
-    o = os.path.join(OUT, "pn_noalloc.o")
-    objs.append(o)
-    if force or _stale(o, deps + [noalloc]):
-        jobs.append((noalloc, o, [], extra))
+    for unit in ("pn_batch", "pn_noalloc", "pn_server"):
+        src = os.path.join(CSRC, unit + ".cu")
+        o = os.path.join(OUT, unit + ".o")
+        objs.append(o)
+        if force or _stale(o, deps + [src]):
+            jobs.append((src, o, [], extra))
     for unit in ("pn_order", "pn_order_batch"):
         src = os.path.join(CSRC, unit + ".cu")
         for N in codegen.ORDERS:

@@ -39,7 +39,33 @@ class PnBatchInfo(ctypes.Structure):
                 ("adjoint_kernels", ctypes.c_int64)]
 
 
-EXPORTS = ("pn_batch_create", "pn_batch_forward", "pn_batch_adjoint", "pn_batch_query", "pn_batch_destroy",
+class PnServerOptions(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_int64), ("max_waves", ctypes.c_int32),
+                ("max_wave_solves", ctypes.c_int32), ("checkpoint_stride", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3)]
+
+
+class PnRequest(ctypes.Structure):
+    _fields_ = [("n_solves", ctypes.c_int32), ("adjoint", ctypes.c_int32)] + [
+        (name, ctypes.c_void_p) for name in ("descs", "rho", "noa", "acs", "intensities_bar", "intensities",
+                                             "rho_bar", "noa_bar", "acs_bar")]
+
+
+class PnTicketInfo(ctypes.Structure):
+    _fields_ = [("done", ctypes.c_int32), ("status", ctypes.c_int32), ("wave", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("queued_ms", ctypes.c_double), ("total_ms", ctypes.c_double)]
+
+
+class PnServerInfo(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_int64) for name in ("memory_budget", "bytes_in_use", "peak_bytes",
+                                                     "requests_submitted", "requests_done", "solves_done",
+                                                     "waves_launched")] + [
+        ("waves_in_flight", ctypes.c_int32), ("max_waves_in_flight", ctypes.c_int32)]
+
+
+SERVER_EXPORTS = ("pn_server_create", "pn_submit", "pn_poll", "pn_wait", "pn_server_query", "pn_server_destroy")
+
+EXPORTS = SERVER_EXPORTS + ("pn_batch_create", "pn_batch_forward", "pn_batch_adjoint", "pn_batch_query", "pn_batch_destroy",
            "pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
            "pn_abi_version", "pn_compiled_orders")
@@ -91,6 +117,15 @@ def lib():
         L.pn_destroy.restype = None
         L.pn_last_error.argtypes = [P]
         L.pn_last_error.restype = ctypes.c_char_p
+        L.pn_server_create.argtypes = [ctypes.POINTER(PnServerOptions), ctypes.POINTER(P)]
+        L.pn_submit.argtypes = [P, ctypes.POINTER(PnRequest), ctypes.POINTER(ctypes.c_uint64)]
+        L.pn_poll.argtypes = [P, ctypes.c_uint64, ctypes.POINTER(PnTicketInfo)]
+        L.pn_wait.argtypes = [P, ctypes.c_uint64, ctypes.c_int64]
+        L.pn_server_query.argtypes = [P, ctypes.POINTER(PnServerInfo)]
+        for name in ("pn_server_create", "pn_submit", "pn_poll", "pn_wait", "pn_server_query"):
+            getattr(L, name).restype = ctypes.c_int
+        L.pn_server_destroy.argtypes = [P]
+        L.pn_server_destroy.restype = None
         L.pn_abi_version.restype = ctypes.c_int32
         L.pn_compiled_orders.restype = ctypes.c_int64
         for name in ("pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device",
@@ -206,7 +241,7 @@ class Handle:
 def _ptr_array(ptrs):
     arr = (ctypes.c_void_p * len(ptrs))()
     for i, p in enumerate(ptrs):
-        arr[i] = int(p)
+        arr[i] = p.ctypes.data if isinstance(p, np.ndarray) else int(p)
     return arr
 
 
@@ -250,6 +285,121 @@ class Batch:
         if getattr(self, "_b", None):
             lib().pn_batch_destroy(self._b)
             self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Ticket:
+    """One submitted request: keeps its inputs and descriptors alive and owns its host outputs."""
+
+    def __init__(self, server, tid, solves, adjoint, keep):
+        self.server = server
+        self.id = tid
+        self.adjoint = adjoint
+        self._keep = keep
+        self.intensities = keep["I"]
+        self.rho_bar = keep["rb"] if adjoint else None
+        self.noa_bar = keep["nb"] if adjoint else None
+        self.acs_bar = keep["ab"] if adjoint else None
+
+    def info(self) -> PnTicketInfo:
+        out = PnTicketInfo()
+        rc = lib().pn_poll(self.server._s, self.id, ctypes.byref(out))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        return out
+
+    def done(self) -> bool:
+        return bool(self.info().done)
+
+    def wait(self, timeout_ms: int = -1):
+        """Block until done; raises PnError if the request failed.  Returns (I, rho_bar, noa_bar,
+        acs_bar) lists, one entry per solve (the adjoint lists are None for a forward request)."""
+        rc = lib().pn_wait(self.server._s, self.id, int(timeout_ms))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        return self.intensities, self.rho_bar, self.noa_bar, self.acs_bar
+
+
+class Server:
+    """Owns one ``pn_server``: continuous batching of host-buffer requests on one GPU."""
+
+    def __init__(self, memory_budget: int = 0, max_waves: int = 0, max_wave_solves: int = 0,
+                 checkpoint_stride: int = 0):
+        opt = PnServerOptions(int(memory_budget), int(max_waves), int(max_wave_solves), int(checkpoint_stride))
+        s = ctypes.c_void_p()
+        rc = lib().pn_server_create(ctypes.byref(opt), ctypes.byref(s))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        self._s = s
+
+    def submit(self, solves, adjoint: bool = True) -> Ticket:
+        """solves: list of (desc, rho, noa, acs, ibar) with host numpy inputs (ibar ignored for a
+        forward request).  Arrays passed as the same object are uploaded once per wave."""
+        n = len(solves)
+        descs = (ctypes.c_void_p * n)()
+        keep = {"descs": [], "in": [], "I": [], "rb": [], "nb": [], "ab": []}
+        conv = {}
+
+        def host(a):
+            k = id(a)
+            if k not in conv:
+                conv[k] = _f64(a)
+                keep["in"].append((a, conv[k]))
+            return conv[k]
+
+        arrs = {k: [] for k in ("rho", "noa", "acs", "ibar")}
+        for i, (d, rho, noa, acs, ibar) in enumerate(solves):
+            descs[i] = ctypes.addressof(d)
+            keep["descs"].append(d)
+            z = query_sizes(d)
+            arrs["rho"].append(host(rho))
+            arrs["noa"].append(host(noa))
+            arrs["acs"].append(host(acs))
+            arrs["ibar"].append(host(ibar) if adjoint else None)
+            keep["I"].append(np.zeros(d.n_xrays))
+            if adjoint:
+                keep["rb"].append(np.zeros(z.n_rho))
+                keep["nb"].append(np.zeros(z.n_noa))
+                keep["ab"].append(np.zeros(z.n_acs))
+        req = PnRequest()
+        req.n_solves = n
+        req.adjoint = 1 if adjoint else 0
+        ptrs = {"descs": descs, "rho": _ptr_array(arrs["rho"]), "noa": _ptr_array(arrs["noa"]),
+                "acs": _ptr_array(arrs["acs"]), "intensities": _ptr_array(keep["I"])}
+        if adjoint:
+            ptrs.update(intensities_bar=_ptr_array(arrs["ibar"]), rho_bar=_ptr_array(keep["rb"]),
+                        noa_bar=_ptr_array(keep["nb"]), acs_bar=_ptr_array(keep["ab"]))
+        for k, v in ptrs.items():
+            setattr(req, k, ctypes.cast(v, ctypes.c_void_p))
+        keep["ptrs"] = ptrs
+        tid = ctypes.c_uint64()
+        rc = lib().pn_submit(self._s, ctypes.byref(req), ctypes.byref(tid))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        return Ticket(self, tid.value, solves, adjoint, keep)
+
+    def info(self) -> PnServerInfo:
+        out = PnServerInfo()
+        rc = lib().pn_server_query(self._s, ctypes.byref(out))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        return out
+
+    def close(self):
+        if getattr(self, "_s", None):
+            lib().pn_server_destroy(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:

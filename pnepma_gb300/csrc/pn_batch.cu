@@ -12,6 +12,7 @@
 #include "pn_layout.h"
 
 #include "pn_batch_base.h"
+#include "pn_batch_impl.h"
 
 namespace pn {
 #define PN_DECL(N) BatchGroupBase* make_batch_group_##N(int precision, int dims);
@@ -67,80 +68,120 @@ static int run_groups(pn_batch* b, cudaStream_t s, F fn) {
   return PN_OK;
 }
 
-extern "C" {
+namespace pn {
 
-int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_options* options, pn_batch** out) {
-  if (!out) return batch_fail("out is NULL", PN_ERR_INVALID);
+int batch_create(const pn_desc* const* descs, int n, long long budget, int K, Arena* arena, pn_batch** out,
+                 std::string& err) {
   *out = nullptr;
-  if (!descs || n < 1) return batch_fail("empty batch", PN_ERR_INVALID);
+  if (!descs || n < 1) { err = "empty batch"; return PN_ERR_INVALID; }
+  pn_batch* b = nullptr;
   try {
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
       cudaGetLastError();
-      return batch_fail("no CUDA device is available", PN_ERR_NO_DEVICE);
+      err = "no CUDA device is available";
+      return PN_ERR_NO_DEVICE;
     }
-    const int precision = descs[0]->precision;
+    const int precision = descs[0] ? descs[0]->precision : 0;
     // groups: same order and same set of active axes
     std::map<std::pair<int, int>, std::vector<int>> by_order;
     for (int i = 0; i < n; ++i) {
-      if (!descs[i]) return batch_fail("descriptor is NULL", PN_ERR_INVALID);
-      if (descs[i]->precision != precision) return batch_fail("all descriptors of a batch share one precision", PN_ERR_INVALID);
+      if (!descs[i]) { err = "descriptor is NULL"; return PN_ERR_INVALID; }
+      if (descs[i]->precision != precision) { err = "all descriptors of a batch share one precision"; return PN_ERR_INVALID; }
       int dims = 0;
       for (int k = 0; k < 3; ++k) dims |= (descs[i]->n_points[k] > 1 ? 1 : 0) << k;
       by_order[{descs[i]->order, dims}].push_back(i);
     }
-    long long budget = options ? options->memory_budget : 0;
-    const int K = options ? options->checkpoint_stride : 0;
-    if (budget <= 0) {
-      size_t fr = 0, tot = 0;
-      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return batch_fail("cudaMemGetInfo failed", PN_ERR_CUDA);
-      budget = (long long)(fr / 2);
-    }
-    pn_batch* b = new pn_batch;
+    b = new pn_batch;
     b->n = n;
     b->precision = precision;
     b->io.resize(n);
     // share the budget between the groups in proportion to their solve counts
     for (auto& kv : by_order) {
-      pn::BatchGroupBase* g = make_group(kv.first.first, precision, kv.first.second);
+      BatchGroupBase* g = make_group(kv.first.first, precision, kv.first.second);
       if (!g) {
         delete b;
-        return batch_fail("P_N order " + std::to_string(kv.first.first) + " is not compiled into this build",
-                          PN_ERR_UNSUPPORTED);
+        err = "P_N order " + std::to_string(kv.first.first) + " is not compiled into this build";
+        return PN_ERR_UNSUPPORTED;
       }
+      g->arena = arena;
       b->groups.push_back(g);
       const long long share = budget * (long long)kv.second.size() / n;
       int rc = g->create(descs, kv.second.data(), (int)kv.second.size(), share, K);
       if (rc) {
-        std::string m = g->err;
+        err = g->err;
         delete b;
-        return batch_fail(m, rc);
+        return rc;
       }
       cudaStream_t st;
       cudaEvent_t ev;
       if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
           cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
         delete b;
-        return batch_fail("stream creation failed", PN_ERR_CUDA);
+        err = "stream creation failed";
+        return PN_ERR_CUDA;
       }
       b->streams.push_back(st);
       b->joins.push_back(ev);
     }
     if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
       delete b;
-      return batch_fail("event creation failed", PN_ERR_CUDA);
+      err = "event creation failed";
+      return PN_ERR_CUDA;
     }
-    if (cudaDeviceSynchronize() != cudaSuccess) {
-      delete b;
-      return batch_fail("device error during batch creation", PN_ERR_CUDA);
-    }
+    // the uploads ran on each group's own stream: wait for those, not for the whole device
+    for (auto* g : b->groups)
+      if (int rc = g->wait_created()) {
+        err = "device error during batch creation: " + g->err;
+        delete b;
+        return rc;
+      }
     *out = b;
     return PN_OK;
   } catch (const std::bad_alloc&) {
-    return batch_fail("host allocation failed", PN_ERR_NO_MEMORY);
+    delete b;
+    err = "host allocation failed";
+    return PN_ERR_NO_MEMORY;
+  } catch (...) {
+    delete b;
+    err = "internal error";
+    return PN_ERR_INVALID;
+  }
+}
+
+long long batch_device_bytes(const pn_batch* b) {
+  long long s = 0;
+  for (auto* g : b->groups) s += g->device_bytes();
+  return s;
+}
+
+}  // namespace pn
+
+extern "C" {
+
+int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_options* options, pn_batch** out) {
+  if (!out) return batch_fail("out is NULL", PN_ERR_INVALID);
+  *out = nullptr;
+  std::string err;
+  long long budget = options ? options->memory_budget : 0;
+  const int K = options ? options->checkpoint_stride : 0;
+  try {
+    if (budget <= 0) {
+      int ndev = 0;
+      if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return batch_fail("no CUDA device is available", PN_ERR_NO_DEVICE);
+      }
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return batch_fail("cudaMemGetInfo failed", PN_ERR_CUDA);
+      budget = (long long)(fr / 2);
+    }
   } catch (...) {
     return batch_fail("internal error", PN_ERR_INVALID);
   }
+  int rc = pn::batch_create(descs, n, budget, K, nullptr, out, err);
+  if (rc) return batch_fail(err, rc);
+  return PN_OK;
 }
 
 int pn_batch_forward(pn_batch* b, const double* const* rho, const double* const* noa, const double* const* acs,

@@ -505,23 +505,42 @@ class BatchGroup : public BatchGroupBase {
   ~BatchGroup() override {
     if (gf) cudaGraphExecDestroy(gf);
     if (ga) cudaGraphExecDestroy(ga);
-    if (cap) cudaStreamDestroy(cap);
-    for (void* p : allocs) cudaFree(p);
+    if (cap) {
+      // arena ranges are reused at once: let uploads still in flight land first
+      if (arena) cudaStreamSynchronize(cap);
+      cudaStreamDestroy(cap);
+    }
+    for (void* p : allocs) {
+      if (arena) arena->free(p);
+      else cudaFree(p);
+    }
   }
   long long device_bytes() const override { return bytes; }
   long long launches_forward() const override { return nl_f + 2; }
   long long launches_adjoint() const override { return nl_a + 2; }
   int stride() const override { return K; }
+  int wait_created() override {
+    PN_CUDA(cudaStreamSynchronize(cap));
+    return PN_OK;
+  }
 
   template <class U>
   int alloc(U*& p, long long cnt) {
     void* q = nullptr;
     size_t b = (size_t)std::max<long long>(cnt, 1) * sizeof(U);
-    cudaError_t e = cudaMalloc(&q, b);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      err = "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e);
-      return PN_ERR_NO_MEMORY;
+    if (arena) {
+      q = arena->alloc(b);
+      if (!q) {
+        err = "no free range of " + std::to_string(b) + " bytes in the memory budget";
+        return PN_ERR_NO_MEMORY;
+      }
+    } else {
+      cudaError_t e = cudaMalloc(&q, b);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        err = "device allocation of " + std::to_string(b) + " bytes failed: " + cudaGetErrorString(e);
+        return PN_ERR_NO_MEMORY;
+      }
     }
     allocs.push_back(q);
     bytes += (long long)b;
@@ -533,7 +552,8 @@ class BatchGroup : public BatchGroupBase {
   int upload(U*& dst, const std::vector<U>& v) {
     int rc = alloc(dst, (long long)v.size());
     if (rc) return rc;
-    if (!v.empty()) PN_CUDA(cudaMemcpy(dst, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice));
+    // pageable source: the call returns once the data is staged, so temporaries may be passed
+    if (!v.empty()) PN_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, cap));
     return PN_OK;
   }
 
@@ -584,6 +604,7 @@ class BatchGroup : public BatchGroupBase {
     if (K > max_ns) K = max_ns;
     hinst.assign(n, BInst<T>());
     int rc;
+    PN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     for (int q = 0; q < n; ++q) {
       std::memset(&hinst[q], 0, sizeof(BInst<T>));
       if ((rc = build_instance(q, d[members[q]]))) return rc;
@@ -604,7 +625,7 @@ class BatchGroup : public BatchGroupBase {
     if ((rc = upload(dinst, hinst))) return rc;
     if ((rc = alloc(dio, n))) return rc;
     if ((rc = alloc(partial, (long long)max_ns * std::max<size_t>(tiles[0].size(), 1) * MAXR))) return rc;
-    PN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    PN_CUDA(cudaStreamSynchronize(cap));
     if ((rc = capture(gf, true))) return rc;
     if ((rc = capture(ga, false))) return rc;
     return PN_OK;
@@ -621,7 +642,7 @@ class BatchGroup : public BatchGroupBase {
     const int nslots = 1 + I.n_ck + n_work_for(K);
     if ((rc = alloc(I.slots, (long long)nslots * L.slot_elems))) return rc;
     if ((rc = alloc(I.lam, L.slot_elems))) return rc;
-    PN_CUDA(cudaMemset(I.slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems));
+    PN_CUDA(cudaMemsetAsync(I.slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems, cap));
     for (int c = 0; c < 8; ++c) {
       I.active[c] = L.active[c];
       I.dev_off[c] = L.dev_off[c];
@@ -642,7 +663,7 @@ class BatchGroup : public BatchGroupBase {
     double* rbar_d;
     if ((rc = alloc(rho_d, L.rho_elems))) return rc;
     if ((rc = alloc(rbar_d, L.rho_elems))) return rc;
-    PN_CUDA(cudaMemset(rho_d, 0, sizeof(T) * (size_t)L.rho_elems));
+    PN_CUDA(cudaMemsetAsync(rho_d, 0, sizeof(T) * (size_t)L.rho_elems, cap));
     for (int c = 0; c < 8; ++c) {
       I.rho[c] = L.active[c] ? rho_d + L.rho_off[c] : nullptr;
       I.rbar[c] = L.active[c] ? rbar_d + L.rho_off[c] : nullptr;

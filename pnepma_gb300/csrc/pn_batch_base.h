@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "../../include/pnepma.h"
+#include "pn_arena.h"
 
 namespace pn {
 
@@ -32,6 +33,10 @@ class BatchGroupBase {
   virtual long long launches_forward() const = 0;
   virtual long long launches_adjoint() const = 0;
   virtual int stride() const = 0;
+  // wait for the uploads create() issued on the group's own stream
+  virtual int wait_created() = 0;
+  // device ranges come from this arena when set (returned to it, never cudaFree'd), else cudaMalloc
+  Arena* arena = nullptr;
   std::string err;
   std::vector<int> members;   // indices into the caller's descriptor array, in group order
 };
