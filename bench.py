@@ -49,6 +49,11 @@ def parse():
                     help="run one 10 keV solve (FP64 twice, FP32 once) for a profiler, print nothing else")
     ap.add_argument("--profile-batch", action="store_true",
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
+    ap.add_argument("--serve", action="store_true",
+                    help="served stream: Poisson requests (1D/2D/3D mix) through pn_server; prints its own line")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     return ap.parse_args()
 
 
@@ -534,12 +539,167 @@ def run_profile_batch(args):
     b.close()
 
 
+# ------------------------------------------------------------------------------------------------
+class ServedStream:
+    """The served stream's requests with their descriptors and inputs, prepared before timing."""
+
+    def __init__(self, n_requests, rate, precision):
+        from pnepma_gb300 import workloads
+        self.reqs = workloads.config5(n_requests=n_requests, rate=rate, precision=precision)
+        self.prepared = {}
+        for r in self.reqs:
+            key = id(r.solves)
+            if key in self.prepared:
+                continue
+            items, keep = [], []
+            rho, noa, acs = r.solves[0].inputs()
+            for s in r.solves:
+                d, k = s.problem.descriptor(s.x_rays)
+                keep.append(k)
+                items.append((d, rho, noa, acs, np.ones(len(s.x_rays))))
+            self.prepared[key] = (items, keep)
+
+    def items(self, r):
+        return self.prepared[id(r.solves)][0]
+
+
+def serve_run(stream, budget, rate_scale=1.0, reqs=None):
+    """Submit every request at its arrival time (scaled), wait for all; returns the measurements."""
+    from pnepma_gb300 import capi
+    reqs = stream.reqs if reqs is None else reqs
+    with capi.Server(memory_budget=budget) as srv:
+        tickets = []
+        t0 = time.perf_counter()
+        for r in reqs:
+            due = t0 + r.arrival_s / rate_scale
+            now = time.perf_counter()
+            if due > now:
+                time.sleep(due - now)
+            tickets.append(srv.submit(stream.items(r), adjoint=True))
+        for t in tickets:
+            t.wait()
+        wall = time.perf_counter() - t0
+        infos = [t.info() for t in tickets]
+        sinfo = srv.info()
+    lat = np.array([i.total_ms for i in infos])
+    queued = np.array([i.queued_ms for i in infos])
+    solves = sum(len(r.solves) for r in reqs)
+    out = {"requests": len(reqs), "solves": solves, "wall_s": wall,
+           "solves_per_s": solves / wall, "requests_per_s": len(reqs) / wall,
+           "offered_requests_per_s": len(reqs) / max(reqs[-1].arrival_s / rate_scale, 1e-9),
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(np.mean(lat))},
+           "queued_ms": {"p50": float(np.percentile(queued, 50)), "p99": float(np.percentile(queued, 99))},
+           "waves": int(sinfo.waves_launched), "max_waves_in_flight": int(sinfo.max_waves_in_flight),
+           "wave_build_ms_mean": sinfo.wave_build_us / 1e3 / max(1, sinfo.waves_launched),
+           "peak_device_bytes": int(sinfo.peak_bytes)}
+    by_kind = {}
+    for r, l in zip(reqs, lat):
+        by_kind.setdefault(r.kind, []).append(l)
+    out["latency_ms_by_kind"] = {k: {"n": len(v), "p50": float(np.percentile(v, 50)),
+                                     "p99": float(np.percentile(v, 99))} for k, v in sorted(by_kind.items())}
+    return out
+
+
+def fp64_sequential_seconds(stream):
+    """FP64 plain, one solve at a time (device-pointer ABI, inputs resident): the time of one solve
+    of each (kind, energy), timed with CUDA events, summed over the stream's solves."""
+    import torch
+    from pnepma_gb300 import capi
+    from pnepma_gb300.problem import PN_FP64
+    dev = torch.device("cuda", 0)
+    stream_ = torch.cuda.Stream(device=dev)
+    per = {}
+    samples = {}
+    for r in stream.reqs:
+        for s in r.solves:
+            key = (r.kind, s.problem.N_steps)
+            samples.setdefault(key, s)
+    for key, s in samples.items():
+        prec = s.problem.precision
+        s.problem.precision = PN_FP64
+        d, k = s.problem.descriptor(s.x_rays)
+        s.problem.precision = prec
+        h = capi.Handle(d, k)
+        rho, noa, acs = s.inputs()
+        dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        x, y, z = dv(rho), dv(noa), dv(acs)
+        I = torch.zeros(len(s.x_rays), dtype=torch.float64, device=dev)
+        ib = torch.ones(len(s.x_rays), dtype=torch.float64, device=dev)
+        sz = h.sizes
+        rb = torch.zeros(sz.n_rho, dtype=torch.float64, device=dev)
+        nb = torch.zeros(sz.n_noa, dtype=torch.float64, device=dev)
+        ab = torch.zeros(max(sz.n_acs, 1), dtype=torch.float64, device=dev)
+        sp = stream_.cuda_stream
+        ts = []
+        for it in range(2):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream_):
+                a.record(stream_)
+                h.forward_device(x.data_ptr(), y.data_ptr(), z.data_ptr(), I.data_ptr(), sp)
+                h.adjoint_device(ib.data_ptr(), rb.data_ptr(), nb.data_ptr(), ab.data_ptr(), sp)
+                b.record(stream_)
+            stream_.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        per[key] = ts[-1]
+        h.close()
+    total = 0.0
+    for r in stream.reqs:
+        for s in r.solves:
+            total += per[(r.kind, s.problem.N_steps)]
+    return total, {f"{k[0]} {k[1]} steps": v * 1e3 for k, v in sorted(per.items())}
+
+
+def run_serve(args):
+    import torch
+    from pnepma_gb300.problem import PN_FP32
+    torch.cuda.set_device(0)
+    t_prep = time.perf_counter()
+    stream = ServedStream(args.serve_requests, args.serve_rate, PN_FP32)
+    t_prep = time.perf_counter() - t_prep
+    budget = int(args.serve_budget_gb * 1e9)
+    first = {}
+    for r in stream.reqs:
+        first.setdefault(r.kind, r)
+    serve_run(stream, budget, rate_scale=50.0, reqs=list(first.values()))   # warm-up: one request per kind
+    with Clocks(0) as clk:
+        full = serve_run(stream, budget)
+    seq_s, per_solve_ms = fp64_sequential_seconds(stream)
+    seq = full["solves"] / seq_s
+    # a sustainable load: the same stream at 60 % of the measured request capacity
+    scale = 0.6 * full["requests_per_s"] / args.serve_rate
+    light = serve_run(stream, budget, rate_scale=scale)
+    mix = {}
+    for r in stream.reqs:
+        mix[r.kind] = mix.get(r.kind, 0) + 1
+    line = {
+        "metric": "served forward+adjoint k-ratio solves/s (Poisson 1D/2D/3D request stream)",
+        "value": full["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32 state and stencil, f64 accumulators", "data": "synthetic (seeded)",
+        "config": {"workload": "config5 stream: requests of 16 positions x {10, 15} keV forward+adjoint; "
+                               "1D N=7 200 cells / 2D N=11 128x64 / 3D N=5 64x64x48 at 50/40/10",
+                   "requests": len(stream.reqs), "mix": mix, "rate_requests_per_s": args.serve_rate,
+                   "memory_budget_bytes": budget, "host_prep_s": t_prep},
+        "at_offered_rate": full,
+        "at_60pct_capacity": light,
+        "fp64_plain_sequential": {"solves_per_s": seq, "seconds_for_stream": seq_s,
+                                  "per_solve_ms": per_solve_ms,
+                                  "method": "one FP64 solve per (kind, step count) timed with CUDA events, summed"},
+        "speedup_vs_fp64_plain_sequential": full["solves_per_s"] / seq,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.profile:
         run_profile(args)
     elif args.profile_batch:
         run_profile_batch(args)
+    elif args.serve:
+        run_serve(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -258,9 +258,10 @@ void pn_batch_destroy(pn_batch* b);
  * scripts/2d_full_reconstruction_test.jl:104-234).  A request is a list of solves -- e.g. one
  * Gauss-Newton iteration's beam positions x energies, forward and adjoint -- submitted from any
  * thread.  One scheduler thread per server admits waiting requests in arrival order as wave slots
- * and room in the memory budget free up, merging those waiting into one batched wave
- * (pn_batch_create's engine; same precision and mode), and runs each wave on its own streams, so
- * requests admitted while others are on the GPU overlap with them.  Each solve's result does not
+ * and room in the memory budget free up.  The request at the head of the queue and every later
+ * waiting request of the same kind (precision, mode, and set of (order, active axes) of its
+ * solves) become one batched wave (pn_batch_create's engine), and each wave runs on its own
+ * streams, so requests admitted while others are on the GPU overlap with them.  Each solve's result does not
  * depend on which other solves share its wave.  All device memory of a wave (tables, tapes,
  * checkpoints, inputs, outputs) is carved from one allocation of memory_budget bytes made by
  * pn_server_create; releasing it never synchronises the device.
@@ -275,7 +276,7 @@ typedef struct pn_server pn_server;
 
 typedef struct pn_server_options {
   int64_t memory_budget;      /* device bytes reserved for the waves; 0 = half of the free memory */
-  int32_t max_waves;          /* waves on the GPU at once; 0 = 4 */
+  int32_t max_waves;          /* waves on the GPU at once; 0 = 8 */
   int32_t max_wave_solves;    /* solves merged into one wave; 0 = 1024 */
   int32_t checkpoint_stride;  /* 0 = chosen per wave from its share of the budget */
   int32_t reserved[3];
@@ -314,6 +315,7 @@ typedef struct pn_server_info {
   int64_t waves_launched;
   int32_t waves_in_flight;
   int32_t max_waves_in_flight;   /* most waves on the GPU at once so far */
+  int64_t wave_build_us;         /* host time spent building waves (tables, uploads, graphs), total */
 } pn_server_info;
 
 int pn_server_create(const pn_server_options* options, pn_server** out);

@@ -60,7 +60,8 @@ class PnServerInfo(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int64) for name in ("memory_budget", "bytes_in_use", "peak_bytes",
                                                      "requests_submitted", "requests_done", "solves_done",
                                                      "waves_launched")] + [
-        ("waves_in_flight", ctypes.c_int32), ("max_waves_in_flight", ctypes.c_int32)]
+        ("waves_in_flight", ctypes.c_int32), ("max_waves_in_flight", ctypes.c_int32),
+        ("wave_build_us", ctypes.c_int64)]
 
 
 SERVER_EXPORTS = ("pn_server_create", "pn_submit", "pn_poll", "pn_wait", "pn_server_query", "pn_server_destroy")

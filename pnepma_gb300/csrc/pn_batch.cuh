@@ -82,6 +82,8 @@ struct BInst {
   int px[8];
   // work segments per list (0: parity-0 targets, 1: parity-1 targets, 2: all classes)
   int tile0[3];
+  int ptile0;             // first slot of this solve's eee tiles in the compact partial arrays
+  int n_ptile;            // its eee tiles: the leading tiles of list 0
   int nseg[3];
   Seg seg[3][MAXSEG];
 };
@@ -104,7 +106,8 @@ struct BLaunch {
   int j;        // forward / recompute: state produced; adjoint / integrate: iteration
   int sub;      // 1, 2, 3
   int K;
-  double* partial;   // forward even sub-step: [tile][r] of this launch
+  double* partial;   // forward even sub-step: [eee tile][pr] of this launch
+  int pr;            // line stride of the partials (largest n_r of the group)
 };
 
 // per-block arguments in shared memory, same member names as SubArgs / IntArgs
@@ -258,7 +261,7 @@ __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_const
       default: substep_cell<T, N, 7, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
     }
   }
-  if (L.partial != nullptr) {
+  if (L.partial != nullptr && one.cls == 0) {   // block-uniform: only eee tiles carry intensity
     __shared__ double red[BLOCK / 32][MAXR];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -269,11 +272,11 @@ __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_const
       if (lane == 0) red[w][r] = v;
     }
     __syncthreads();
-    if (threadIdx.x < MAXR) {
+    if (threadIdx.x < L.pr) {
       double v = 0.0;
 #pragma unroll
       for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
-      L.partial[(long long)blockIdx.x * MAXR + threadIdx.x] = v;
+      L.partial[(long long)(I.ptile0 + (int)blockIdx.x - I.tile0[0]) * L.pr + threadIdx.x] = v;
     }
   }
 }
@@ -397,17 +400,17 @@ __global__ void batch_zero_kernel(const BInst<T>* __restrict__ inst, int which) 
 // integral[i][r] of solve k = sum over its eee tiles of the partials of forward launch t
 template <class T>
 __global__ void batch_reduce_kernel(const BInst<T>* __restrict__ inst, const double* __restrict__ partial,
-                                    int max_ns, int n_tiles0) {
+                                    int max_ns, int n_ptiles, int pr) {
   const BInst<T>& I = inst[blockIdx.y];
   const int i = blockIdx.x + 1;  // forward step 1..ns
   if (i > I.ns) return;
   const int t = max_ns - I.ns + i;  // launch index (1-based)
-  const int nt = I.nseg[0] > 0 ? (I.seg[0][I.nseg[0] - 1].block0 + I.seg[0][I.nseg[0] - 1].nblocks) : 0;
   __shared__ double buf[MAXR][128];
   for (int r = 0; r < MAXR; ++r) {
     double v = 0.0;
-    for (int b = threadIdx.x; b < nt; b += blockDim.x)
-      v += partial[((long long)(t - 1) * n_tiles0 + I.tile0[0] + b) * MAXR + r];
+    if (r < pr)
+      for (int b = threadIdx.x; b < I.n_ptile; b += blockDim.x)
+        v += partial[((long long)(t - 1) * n_ptiles + I.ptile0 + b) * pr + r];
     buf[r][threadIdx.x] = v;
   }
   __syncthreads();
@@ -495,6 +498,7 @@ class BatchGroup : public BatchGroupBase {
   BTile* dtiles[3] = {nullptr, nullptr, nullptr};
   std::vector<int> tile_end[3];   // cumulative tiles per solve (in group order)
   double* partial = nullptr;
+  int n_ptiles = 0, pr = 1;   // compact partials: eee tiles of all solves, line stride
   int max_ns = 0, K = 1, n = 0;
   std::vector<void*> allocs;
   long long bytes = 0;
@@ -622,9 +626,29 @@ class BatchGroup : public BatchGroupBase {
       }
       if ((rc = upload(dtiles[list], tiles[list]))) return rc;
     }
+    // compact partials: the eee tiles lead each solve's list-0 tiles (class 0 is built first)
+    n_ptiles = 0;
+    pr = 1;
+    for (int q = 0; q < n; ++q) {
+      int cnt = 0;
+      bool leading = true;
+      for (int sgi = 0; sgi < hinst[q].nseg[0]; ++sgi) {
+        const Seg& sg = hinst[q].seg[0][sgi];
+        if (sg.cls == 0) {
+          if (!leading) { err = "internal: eee segments are not the leading tiles"; return PN_ERR_INVALID; }
+          cnt += sg.nblocks;
+        } else {
+          leading = false;
+        }
+      }
+      hinst[q].ptile0 = n_ptiles;
+      hinst[q].n_ptile = cnt;
+      n_ptiles += cnt;
+      pr = std::max(pr, hinst[q].nr);
+    }
     if ((rc = upload(dinst, hinst))) return rc;
     if ((rc = alloc(dio, n))) return rc;
-    if ((rc = alloc(partial, (long long)max_ns * std::max<size_t>(tiles[0].size(), 1) * MAXR))) return rc;
+    if ((rc = alloc(partial, (long long)max_ns * std::max(n_ptiles, 1) * pr))) return rc;
     PN_CUDA(cudaStreamSynchronize(cap));
     if ((rc = capture(gf, true))) return rc;
     if ((rc = capture(ga, false))) return rc;
@@ -849,6 +873,7 @@ class BatchGroup : public BatchGroupBase {
     a.sub = sub;
     a.K = K;
     a.partial = part;
+    a.pr = pr;
     if (integ)
       batch_integrate_kernel<T, N, DIMS><<<nt, BLOCK, 0, cap>>>(a);
     else if (adj)
@@ -876,10 +901,10 @@ class BatchGroup : public BatchGroupBase {
       PN_CUDA(cudaGetLastError());
       for (int t = 1; t <= max_ns; ++t) {
         const int j = max_ns - t;
-        double* part = partial + (long long)(t - 1) * tiles[0].size() * MAXR;
+        double* part = partial + (long long)(t - 1) * n_ptiles * pr;
         if ((rc = fwd_step(j, BM_FORWARD, part))) return rc;
       }
-      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, cap>>>(dinst, partial, max_ns, (int)tiles[0].size());
+      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, cap>>>(dinst, partial, max_ns, n_ptiles, pr);
       batch_final_kernel<T><<<n, 32, 0, cap>>>(dinst);
       PN_CUDA(cudaGetLastError());
       nl += 3;

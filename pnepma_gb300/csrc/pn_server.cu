@@ -54,6 +54,7 @@ struct Request {
   int n = 0;
   int adjoint = 0;
   int precision = 0;
+  std::vector<std::pair<int, int>> key;   // sorted distinct (order, active axes) of its solves
   std::vector<const pn_desc*> descs;
   std::vector<const double*> rho, noa, acs, ibar;
   std::vector<double*> I, rho_bar, noa_bar, acs_bar;
@@ -84,7 +85,7 @@ struct pn_server {
   int device = 0;
   char* base = nullptr;
   std::unique_ptr<pn::Arena> arena;
-  int max_waves = 4;
+  int max_waves = 8;
   int max_wave_solves = 1024;
   int K = 0;
 
@@ -101,6 +102,7 @@ struct pn_server {
   int in_flight = 0;
   int max_in_flight = 0;
   long long submitted = 0, completed = 0, solves_done = 0, waves = 0;
+  double build_us = 0.0;
   std::thread worker;
 
   void run();
@@ -339,22 +341,30 @@ void pn_server::run() {
     while (!pending.empty() && !mem_blocked && in_flight < max_waves) {
       Wave* w = new Wave;
       w->id = next_wave++;
+      // the head and every later waiting request of the same kind (precision, mode, and set of
+      // (order, active axes)): a wave completes as a whole, so kinds of very different cost are
+      // not mixed, and a kind's later arrivals join the head's wave instead of waiting for a slot
       Request* head = pending.front();
       w->adjoint = head->adjoint;
       int solves = 0;
-      while (!pending.empty()) {
-        Request* r = pending.front();
-        if (r->precision != head->precision || r->adjoint != head->adjoint) break;
+      for (auto it = pending.begin(); it != pending.end();) {
+        Request* r = *it;
+        if (r->precision != head->precision || r->adjoint != head->adjoint || r->key != head->key) {
+          ++it;
+          continue;
+        }
         if (!w->reqs.empty() && solves + r->n > limit) break;
         w->reqs.push_back(r);
         solves += r->n;
-        pending.pop_front();
+        it = pending.erase(it);
       }
       ++in_flight;
       lk.unlock();
       const auto t = Clock::now();
       int rc = launch_wave(w);
+      const auto tb = Clock::now();
       lk.lock();
+      build_us += 1e3 * ms_between(t, tb);
       if (rc == PN_OK) {
         for (Request* r : w->reqs) {
           r->t_admit = t;
@@ -367,8 +377,11 @@ void pn_server::run() {
       }
       --in_flight;
       if (rc == PN_ERR_NO_MEMORY && (w->reqs.size() > 1 || in_flight > 0)) {
-        // back to the head of the queue: fewer requests per wave, or wait for running waves
-        for (auto it = w->reqs.rbegin(); it != w->reqs.rend(); ++it) pending.push_front(*it);
+        // back into the queue in arrival order: fewer requests per wave, or wait for running waves
+        for (Request* r : w->reqs)
+          pending.insert(std::upper_bound(pending.begin(), pending.end(), r,
+                                          [](const Request* a, const Request* b) { return a->id < b->id; }),
+                         r);
         if (w->reqs.size() > 1) limit = std::max(1, solves / 2);
         else mem_blocked = true;
         delete w;
@@ -489,6 +502,9 @@ int pn_submit(pn_server* s, const pn_request* req, uint64_t* ticket) {
         pn::set_last_error("NULL buffer in the request");
         return PN_ERR_INVALID;
       }
+      int dims = 0;
+      for (int k = 0; k < 3; ++k) dims |= (d->n_points[k] > 1 ? 1 : 0) << k;
+      r->key.emplace_back(d->order, dims);
       r->descs.push_back(d);
       r->rho.push_back(req->rho[i]);
       r->noa.push_back(req->noa[i]);
@@ -499,6 +515,8 @@ int pn_submit(pn_server* s, const pn_request* req, uint64_t* ticket) {
       r->noa_bar.push_back(r->adjoint ? req->noa_bar[i] : nullptr);
       r->acs_bar.push_back(r->adjoint ? req->acs_bar[i] : nullptr);
     }
+    std::sort(r->key.begin(), r->key.end());
+    r->key.erase(std::unique(r->key.begin(), r->key.end()), r->key.end());
     r->t_submit = Clock::now();
     {
       std::lock_guard<std::mutex> lk(s->mu);
@@ -581,6 +599,7 @@ int pn_server_query(pn_server* s, pn_server_info* info) {
   info->waves_launched = s->waves;
   info->waves_in_flight = s->in_flight;
   info->max_waves_in_flight = s->max_in_flight;
+  info->wave_build_us = (int64_t)s->build_us;
   return PN_OK;
 }
 

@@ -213,3 +213,68 @@ def small_case(dims: int = 2, N: int = 3, shape=None, n_steps: int = 12, seed: i
                       E_cut=min(physics.ELEMENTS[e].k_edge_ev for e in elements) - 500.0,
                       detector=(50 * NM, 0.1 * UM, 0.0), precision=precision, stabilise=stabilise,
                       checkpoint_stride=checkpoint_stride, label=f"small{dims}d")
+
+
+@dataclass
+class Request:
+    """One served request: a reconstruction iteration's solves (positions x energies) on one material."""
+    kind: str
+    arrival_s: float
+    solves: list
+
+
+def config5_kind(kind: str, seed: int, precision=PN_FP32, positions: int = 16, energies=(10.0, 15.0),
+                 stabilise=True):
+    """The solves of one request of a kind: '1d' N=7 200 cells over 1 um (Cu/Ni); '2d' N=11
+    128 (lateral) x 64 (depth) over 2 x 1 um; '3d' N=5 64 x 64 (lateral) x 48 (depth) over
+    1.5 x 1.5 x 1 um (Fe/Cr/Ni).  Composition: a seeded smooth field; beam positions evenly across
+    the lateral extent (on the axis in 1D)."""
+    rng = _rng(seed)
+    if kind == "1d":
+        gspec = GridSpec.make((200, 1, 1), (-1 * UM, 0.0), 0.0, 0.0)
+        els, N, ys = ["Cu", "Ni"], 7, [0.0] * positions
+    elif kind == "2d":
+        gspec = GridSpec.make((64, 128, 1), (-1 * UM, 0.0), (-1 * UM, 1 * UM), 0.0)
+        els, N = ["Fe", "Cr", "Ni"], 11
+        ys = list(np.linspace(-1 * UM, 1 * UM, positions + 2)[1:-1])
+    elif kind == "3d":
+        gspec = GridSpec.make((48, 64, 64), (-1 * UM, 0.0), (-0.75 * UM, 0.75 * UM), (-0.75 * UM, 0.75 * UM))
+        els, N = ["Fe", "Cr", "Ni"], 5
+        ys = list(np.linspace(-0.75 * UM, 0.75 * UM, positions + 2)[1:-1])
+    else:
+        raise ValueError(kind)
+    frac = smooth_fractions(rng, gspec, len(els))
+    out, mat = [], None
+    for E in energies:
+        for y in ys:
+            s = make_solve(N, gspec, els, frac, E, beam_y=float(y), beam_sigma=50 * NM, n_steps=100,
+                           detector=(100 * NM, 0.0, 0.0), precision=precision, stabilise=stabilise,
+                           label=f"cfg5 {kind} E={E} y={y:.3e}")
+            if mat is None:
+                mat = s.material
+            s.material = mat          # one material per request: the inputs are shared
+            out.append(s)
+    return out
+
+
+def config5(n_requests: int = 64, seed: int = 5, rate: float = 200.0, mix=(0.5, 0.4, 0.1),
+            precision=PN_FP32, materials_per_kind: int = 3, positions: int = 16, energies=(10.0, 15.0)):
+    """Served stream: Poisson arrivals at `rate` requests/s; kinds 1d/2d/3d drawn with `mix`; each
+    request is `positions` x `energies` forward+adjoint solves.  The compositions cycle through a
+    pool of `materials_per_kind` seeded fields per kind (host preparation of a 3D material takes
+    seconds; the device work does not depend on which field a request carries)."""
+    rng = _rng(seed)
+    kinds = rng.choice(["1d", "2d", "3d"], size=n_requests, p=list(mix))
+    t = np.cumsum(rng.exponential(1.0 / rate, size=n_requests))
+    t -= t[0]
+    pool = {}
+    out = []
+    counts = {"1d": 0, "2d": 0, "3d": 0}
+    for i, k in enumerate(kinds):
+        slot = counts[k] % materials_per_kind
+        counts[k] += 1
+        if (k, slot) not in pool:
+            pool[(k, slot)] = config5_kind(k, seed * 1000 + 10 * slot + {"1d": 1, "2d": 2, "3d": 3}[k],
+                                           precision=precision, positions=positions, energies=energies)
+        out.append(Request(str(k), float(t[i]), pool[(k, slot)]))
+    return out
