@@ -231,14 +231,20 @@ typedef struct pn_batch pn_batch;
 typedef struct pn_batch_options {
   int64_t memory_budget;      /* bytes of device memory for the tapes; 0 = half of the free memory */
   int32_t checkpoint_stride;  /* 0 = smallest stride whose tapes fit the budget; K >= 1 forces K */
-  int32_t reserved;
+  int32_t flags;              /* pn_batch_flags */
 } pn_batch_options;
+
+enum pn_batch_flags {
+  /* FP32 2D groups stage their box tiles with TMA unless this is set; the generic kernels give
+     bit-identical results (for comparison and diagnosis) */
+  PN_BATCH_GENERIC_KERNELS = 1
+};
 
 typedef struct pn_batch_info {
   int32_t n_solves;
   int32_t n_groups;           /* one per distinct (order, set of active axes) */
   int32_t checkpoint_stride;  /* largest stride in use */
-  int32_t reserved;
+  int32_t tma_groups;         /* groups whose sub-steps stage their tiles with TMA */
   int64_t device_bytes;
   int64_t forward_kernels;    /* kernel launches of one pn_batch_forward */
   int64_t adjoint_kernels;    /* kernel launches of one pn_batch_adjoint */
@@ -249,6 +255,8 @@ int pn_batch_forward(pn_batch* b, const double* const* rho, const double* const*
                      const double* const* acs, double* const* intensities, void* stream);
 int pn_batch_adjoint(pn_batch* b, const double* const* intensities_bar, double* const* rho_bar,
                      double* const* noa_bar, double* const* acs_bar, void* stream);
+/* Fills *info.  Returns PN_ERR_TIMEOUT when a bounded device-side wait of an earlier launch ran
+   out (call it after that work has completed). */
 int pn_batch_query(const pn_batch* b, pn_batch_info* info);
 void pn_batch_destroy(pn_batch* b);
 
@@ -335,6 +343,10 @@ void pn_server_destroy(pn_server* s);
    failed call in this thread that has no handle: pn_create, pn_query_sizes, pn_batch_*,
    pn_forward_noalloc, pn_server_*, pn_submit, pn_poll, pn_wait).  Never NULL. */
 const char* pn_last_error(const pn_handle* h);
+
+/* Self-test of the FP32 exponential factor phi1(c) = (e^c - 1) / c used by the FP32 kernels
+   (no counterpart in the reference): evaluates it and the expm1f(c) / c form for n arguments. */
+int pn_selftest_phi1(int32_t n, const float* x, float* phi1_fast, float* phi1_ref);
 
 /* ABI version and the compiled P_N orders (bit N set when order N is available). */
 int32_t pn_abi_version(void);

@@ -50,28 +50,33 @@ def _compile(args):
     return r.stderr
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False) -> str:
-    os.makedirs(OUT, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False, out: str | None = None,
+          defines=()) -> str:
+    """Compile every unit for sm_103a and link the library.  `out` and `defines` build a variant
+    (e.g. another occupancy bound) into another directory; the default is the in-tree library."""
+    out_dir = out or OUT
+    lib_path = os.path.join(out_dir, os.path.basename(LIB))
+    os.makedirs(out_dir, exist_ok=True)
     codegen.write_header()
     deps = _sources()
     jobs = []
     objs = []
-    extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    extra = (["-Xptxas", "-v"] if ptxas_verbose else []) + list(defines)
     capi = os.path.join(CSRC, "pn_capi.cu")
-    o = os.path.join(OUT, "pn_capi.o")
+    o = os.path.join(out_dir, "pn_capi.o")
     objs.append(o)
     if force or _stale(o, deps + [capi]):
         jobs.append((capi, o, [], extra))
-    for unit in ("pn_batch", "pn_noalloc", "pn_server"):
+    for unit in ("pn_batch", "pn_noalloc", "pn_server", "pn_selftest"):
         src = os.path.join(CSRC, unit + ".cu")
-        o = os.path.join(OUT, unit + ".o")
+        o = os.path.join(out_dir, unit + ".o")
         objs.append(o)
         if force or _stale(o, deps + [src]):
             jobs.append((src, o, [], extra))
     for unit in ("pn_order", "pn_order_batch"):
         src = os.path.join(CSRC, unit + ".cu")
         for N in codegen.ORDERS:
-            o = os.path.join(OUT, f"{unit}_{N}.o")
+            o = os.path.join(out_dir, f"{unit}_{N}.o")
             objs.append(o)
             if force or _stale(o, deps + [src]):
                 jobs.append((src, o, [f"-DPN_ORDER={N}"], extra))
@@ -83,14 +88,14 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             for log in ex.map(_compile, jobs):
                 if verbose and log:
                     print(log, file=sys.stderr)
-    if force or jobs or _stale(LIB, objs):
-        tmp = LIB + f".tmp{os.getpid()}"
+    if force or jobs or _stale(lib_path, objs):
+        tmp = lib_path + f".tmp{os.getpid()}"
         cmd = [_nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
-    return LIB
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

@@ -27,14 +27,17 @@ class PnHandleInfo(ctypes.Structure):
                 ("adjoint_kernels", ctypes.c_int64)]
 
 
+PN_BATCH_GENERIC_KERNELS = 1
+
+
 class PnBatchOptions(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_int64), ("checkpoint_stride", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("flags", ctypes.c_int32)]
 
 
 class PnBatchInfo(ctypes.Structure):
     _fields_ = [("n_solves", ctypes.c_int32), ("n_groups", ctypes.c_int32),
-                ("checkpoint_stride", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("checkpoint_stride", ctypes.c_int32), ("tma_groups", ctypes.c_int32),
                 ("device_bytes", ctypes.c_int64), ("forward_kernels", ctypes.c_int64),
                 ("adjoint_kernels", ctypes.c_int64)]
 
@@ -127,6 +130,8 @@ def lib():
             getattr(L, name).restype = ctypes.c_int
         L.pn_server_destroy.argtypes = [P]
         L.pn_server_destroy.restype = None
+        L.pn_selftest_phi1.argtypes = [ctypes.c_int32, P, P, P]
+        L.pn_selftest_phi1.restype = ctypes.c_int
         L.pn_abi_version.restype = ctypes.c_int32
         L.pn_compiled_orders.restype = ctypes.c_int64
         for name in ("pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device",
@@ -249,7 +254,7 @@ def _ptr_array(ptrs):
 class Batch:
     """Owns one ``pn_batch``: many solves marched together (device-pointer interface)."""
 
-    def __init__(self, descs, keepalive=None, memory_budget: int = 0, checkpoint_stride: int = 0):
+    def __init__(self, descs, keepalive=None, memory_budget: int = 0, checkpoint_stride: int = 0, flags: int = 0):
         self.descs = list(descs)
         self._keep = keepalive
         self.sizes = [query_sizes(d) for d in self.descs]
@@ -257,7 +262,7 @@ class Batch:
         for i, d in enumerate(self.descs):
             arr[i] = ctypes.addressof(d)
         self._arr = arr
-        opt = PnBatchOptions(int(memory_budget), int(checkpoint_stride), 0)
+        opt = PnBatchOptions(int(memory_budget), int(checkpoint_stride), int(flags))
         b = ctypes.c_void_p()
         rc = lib().pn_batch_create(arr, len(self.descs), ctypes.byref(opt), ctypes.byref(b))
         if rc:

@@ -70,7 +70,7 @@ static int run_groups(pn_batch* b, cudaStream_t s, F fn) {
 
 namespace pn {
 
-int batch_create(const pn_desc* const* descs, int n, long long budget, int K, Arena* arena, pn_batch** out,
+int batch_create(const pn_desc* const* descs, int n, long long budget, int K, int flags, Arena* arena, pn_batch** out,
                  std::string& err) {
   *out = nullptr;
   if (!descs || n < 1) { err = "empty batch"; return PN_ERR_INVALID; }
@@ -107,7 +107,7 @@ int batch_create(const pn_desc* const* descs, int n, long long budget, int K, Ar
       g->arena = arena;
       b->groups.push_back(g);
       const long long share = budget * (long long)kv.second.size() / n;
-      int rc = g->create(descs, kv.second.data(), (int)kv.second.size(), share, K);
+      int rc = g->create(descs, kv.second.data(), (int)kv.second.size(), share, K, flags);
       if (rc) {
         err = g->err;
         delete b;
@@ -149,6 +149,14 @@ int batch_create(const pn_desc* const* descs, int n, long long budget, int K, Ar
   }
 }
 
+int batch_status(pn_batch* b) {
+  for (auto* g : b->groups) {
+    const int s = g->device_status();
+    if (s != PN_OK) return s;
+  }
+  return PN_OK;
+}
+
 long long batch_device_bytes(const pn_batch* b) {
   long long s = 0;
   for (auto* g : b->groups) s += g->device_bytes();
@@ -179,7 +187,7 @@ int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_optio
   } catch (...) {
     return batch_fail("internal error", PN_ERR_INVALID);
   }
-  int rc = pn::batch_create(descs, n, budget, K, nullptr, out, err);
+  int rc = pn::batch_create(descs, n, budget, K, options ? options->flags : 0, nullptr, out, err);
   if (rc) return batch_fail(err, rc);
   return PN_OK;
 }
@@ -225,14 +233,22 @@ int pn_batch_query(const pn_batch* b, pn_batch_info* info) {
   info->n_solves = b->n;
   info->n_groups = (int32_t)b->groups.size();
   info->checkpoint_stride = 0;
+  info->tma_groups = 0;
   info->device_bytes = 0;
   info->forward_kernels = 0;
   info->adjoint_kernels = 0;
   for (auto* g : b->groups) {
     info->checkpoint_stride = std::max(info->checkpoint_stride, g->stride());
+    info->tma_groups += g->tma() ? 1 : 0;
     info->device_bytes += g->device_bytes();
     info->forward_kernels += g->launches_forward();
     info->adjoint_kernels += g->launches_adjoint();
+  }
+  try {
+    const int st = pn::batch_status(const_cast<pn_batch*>(b));
+    if (st != PN_OK) return batch_fail("a bounded device-side wait ran out", st);
+  } catch (...) {
+    return batch_fail("internal error", PN_ERR_INVALID);
   }
   return PN_OK;
 }

@@ -19,13 +19,30 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <string>
 #include <vector>
 
 #include "pn_batch_base.h"
 #include "pn_solver.cuh"
+
+// Occupancy of the batched kernels: PN_BATCH_MIN_BLOCKS > 0 asks the compiler for at least that
+// many resident blocks per SM (fewer registers per thread); PN_BATCH_MAX_TPB caps the tiles one
+// block walks.
+#ifndef PN_BATCH_MIN_BLOCKS
+#define PN_BATCH_MIN_BLOCKS 0
+#endif
+#ifndef PN_BATCH_MAX_TPB
+#define PN_BATCH_MAX_TPB 1
+#endif
+#if PN_BATCH_MIN_BLOCKS > 0
+#define PN_BATCH_BOUNDS __launch_bounds__(BLOCK, PN_BATCH_MIN_BLOCKS)
+#else
+#define PN_BATCH_BOUNDS __launch_bounds__(BLOCK)
+#endif
 
 namespace pn {
 
@@ -92,7 +109,7 @@ struct BTile {
   int inst;
   int seg;
   int lb;   // block index local to the segment
-  int pad;
+  int pad;  // partial slot of an eee tile of list 0, else -1
 };
 
 enum { BM_FORWARD = 0, BM_RECOMPUTE = 1, BM_ADJOINT = 2 };
@@ -108,6 +125,8 @@ struct BLaunch {
   int K;
   double* partial;   // forward even sub-step: [eee tile][pr] of this launch
   int pr;            // line stride of the partials (largest n_r of the group)
+  int n_tiles;       // active tiles of this launch
+  int tpb;           // consecutive tiles per block
 };
 
 // per-block arguments in shared memory, same member names as SubArgs / IntArgs
@@ -167,23 +186,28 @@ __device__ __forceinline__ T* bslot(const BInst<T>& I, int j, int K, bool segmen
   return I.slots + (long long)(1 + I.n_ck + w) * I.slot_elems;
 }
 
-// Copy solve `q`'s descriptor into shared memory with every thread of the block (coalesced
-// 4-byte words), so the per-block arguments can then be filled in parallel from shared memory.
+// Words of a BInst before its segment tables: what a block stages (the segments are read from
+// global memory, one per tile).
+template <class T>
+constexpr int binst_head_words() {
+  return (int)(offsetof(BInst<T>, seg) / 4);
+}
+
+// Copy the head of solve `q`'s descriptor into shared memory with every thread of the block
+// (coalesced 4-byte words), so the per-block arguments can then be filled in parallel from it.
+// Only the fields before `seg` are valid in the returned reference.
 template <class T>
 __device__ __forceinline__ const BInst<T>& stage_instance(const BInst<T>* inst, int q, unsigned int* raw) {
-  constexpr int W = (int)(sizeof(BInst<T>) / 4);
+  constexpr int W = binst_head_words<T>();
   const unsigned int* src = reinterpret_cast<const unsigned int*>(inst + q);
   for (int w = threadIdx.x; w < W; w += BLOCK) raw[w] = src[w];
   __syncthreads();
   return *reinterpret_cast<const BInst<T>*>(raw);
 }
 
-template <class T, int N, bool ADJ, int DIMS>
-__global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_constant__ BLaunch<T> L) {
-  __shared__ BSub<T, N> a;
-  __shared__ __align__(16) unsigned int raw[sizeof(BInst<T>) / 4 + 1];
-  const BTile tl = L.tiles[blockIdx.x];
-  const BInst<T>& I = stage_instance(L.inst, tl.inst, raw);
+// per-block arguments of a sub-step for solve I (threads fill disjoint fields; caller syncs)
+template <class T, int N, bool ADJ>
+__device__ __forceinline__ void fill_sub(BSub<T, N>& a, const BInst<T>& I, const BLaunch<T>& L) {
   const int par = L.list;
   const int tid = threadIdx.x;
   int row;
@@ -239,54 +263,71 @@ __global__ void __launch_bounds__(BLOCK) batch_substep_kernel(const __grid_const
     const T* cc = ADJ ? I.adj_c : I.fwd_c;
     a.c[e][l] = e < I.ne ? cc[((long long)row * I.ne + e) * (N + 1) + l] : T(0);
   }
-  __syncthreads();
-  Seg one = I.seg[L.list][tl.seg];
-  one.block0 = 0;
-  int i = 0, j = 0, k = 0, s0;
-  const bool ok = locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k);
-  const bool face = one.kind == 1;
-  double part[MAXR];
-#pragma unroll
-  for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
-  double* pp = (L.partial != nullptr) ? part : nullptr;
-  if (ok) {
-    switch (one.cls) {
-      case 0: substep_cell<T, N, 0, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 1: substep_cell<T, N, 1, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 2: substep_cell<T, N, 2, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 3: substep_cell<T, N, 3, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 4: substep_cell<T, N, 4, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 5: substep_cell<T, N, 5, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      case 6: substep_cell<T, N, 6, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
-      default: substep_cell<T, N, 7, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+}
+
+// One block walks L.tpb consecutive tiles of the launch's list; the solve's arguments are staged
+// once and again only when the next tile belongs to another solve (tiles are solve-major).
+template <class T, int N, bool ADJ, int DIMS>
+__global__ void PN_BATCH_BOUNDS batch_substep_kernel(const __grid_constant__ BLaunch<T> L) {
+  __shared__ BSub<T, N> a;
+  __shared__ __align__(16) unsigned int raw[binst_head_words<T>() + 1];
+  __shared__ double red[BLOCK / 32][MAXR];
+  const int t_end = min(L.n_tiles, ((int)blockIdx.x + 1) * L.tpb);
+  int cur = -1;
+  for (int t = (int)blockIdx.x * L.tpb; t < t_end; ++t) {
+    const BTile tl = L.tiles[t];
+    if (tl.inst != cur) {
+      if (cur >= 0) __syncthreads();   // every thread is done with the previous solve's arguments
+      const BInst<T>& I0 = stage_instance(L.inst, tl.inst, raw);
+      fill_sub<T, N, ADJ>(a, I0, L);
+      __syncthreads();
+      cur = tl.inst;
     }
-  }
-  if (L.partial != nullptr && one.cls == 0) {   // block-uniform: only eee tiles carry intensity
-    __shared__ double red[BLOCK / 32][MAXR];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const BInst<T>& I = *reinterpret_cast<const BInst<T>*>(raw);
+    Seg one = L.inst[tl.inst].seg[L.list][tl.seg];
+    one.block0 = 0;
+    int i = 0, j = 0, k = 0, s0;
+    const bool ok = locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k);
+    const bool face = one.kind == 1;
+    double part[MAXR];
 #pragma unroll
-    for (int r = 0; r < MAXR; ++r) {
-      double v = part[r];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) red[w][r] = v;
+    for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
+    double* pp = (L.partial != nullptr) ? part : nullptr;
+    if (ok) {
+      switch (one.cls) {
+        case 0: substep_cell<T, N, 0, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 1: substep_cell<T, N, 1, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 2: substep_cell<T, N, 2, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 3: substep_cell<T, N, 3, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 4: substep_cell<T, N, 4, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 5: substep_cell<T, N, 5, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        case 6: substep_cell<T, N, 6, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+        default: substep_cell<T, N, 7, ADJ, true, BSub<T, N>, DIMS>(a, i, j, k, face, pp); break;
+      }
     }
-    __syncthreads();
-    if (threadIdx.x < L.pr) {
-      double v = 0.0;
+    if (L.partial != nullptr && one.cls == 0) {   // block-uniform: only eee tiles carry intensity
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
-      L.partial[(long long)(I.ptile0 + (int)blockIdx.x - I.tile0[0]) * L.pr + threadIdx.x] = v;
+      for (int r = 0; r < MAXR; ++r) {
+        double v = part[r];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][r] = v;
+      }
+      __syncthreads();
+      if (threadIdx.x < L.pr) {
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+        L.partial[(long long)tl.pad * L.pr + threadIdx.x] = v;
+      }
+      __syncthreads();   // red is reused by the next tile
     }
   }
 }
 
-template <class T, int N, int DIMS>
-__global__ void __launch_bounds__(BLOCK) batch_integrate_kernel(const __grid_constant__ BLaunch<T> L) {
-  __shared__ BInt<T, N> a;
-  __shared__ __align__(16) unsigned int raw[sizeof(BInst<T>) / 4 + 1];
-  const BTile tl = L.tiles[blockIdx.x];
-  const BInst<T>& I = stage_instance(L.inst, tl.inst, raw);
+template <class T, int N>
+__device__ __forceinline__ void fill_int(BInt<T, N>& a, const BInst<T>& I, const BLaunch<T>& L) {
   const int it = L.j;   // iteration; it == ns is the final accumulation on the zero state
   const int tid = threadIdx.x;
   if (tid < 8) {
@@ -325,21 +366,38 @@ __global__ void __launch_bounds__(BLOCK) batch_integrate_kernel(const __grid_con
     const int e = (tid - 32) / (N + 1), l = (tid - 32) % (N + 1);
     a.c[e][l] = e < I.ne ? I.int_c[((long long)it * I.ne + e) * (N + 1) + l] : T(0);
   }
-  __syncthreads();
-  Seg one = I.seg[2][tl.seg];
-  one.block0 = 0;
-  int i = 0, j = 0, k = 0, s0;
-  if (!locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k)) return;
-  const bool face = one.kind == 1;
-  switch (one.cls) {
-    case 0: integrate_cell<T, N, 0, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 1: integrate_cell<T, N, 1, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 2: integrate_cell<T, N, 2, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 3: integrate_cell<T, N, 3, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 4: integrate_cell<T, N, 4, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 5: integrate_cell<T, N, 5, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    case 6: integrate_cell<T, N, 6, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
-    default: integrate_cell<T, N, 7, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+}
+
+template <class T, int N, int DIMS>
+__global__ void PN_BATCH_BOUNDS batch_integrate_kernel(const __grid_constant__ BLaunch<T> L) {
+  __shared__ BInt<T, N> a;
+  __shared__ __align__(16) unsigned int raw[binst_head_words<T>() + 1];
+  const int t_end = min(L.n_tiles, ((int)blockIdx.x + 1) * L.tpb);
+  int cur = -1;
+  for (int t = (int)blockIdx.x * L.tpb; t < t_end; ++t) {
+    const BTile tl = L.tiles[t];
+    if (tl.inst != cur) {
+      if (cur >= 0) __syncthreads();
+      const BInst<T>& I0 = stage_instance(L.inst, tl.inst, raw);
+      fill_int<T, N>(a, I0, L);
+      __syncthreads();
+      cur = tl.inst;
+    }
+    Seg one = L.inst[tl.inst].seg[2][tl.seg];
+    one.block0 = 0;
+    int i = 0, j = 0, k = 0, s0;
+    if (!locate(&one, 1, tl.lb, threadIdx.x, s0, i, j, k)) continue;
+    const bool face = one.kind == 1;
+    switch (one.cls) {
+      case 0: integrate_cell<T, N, 0, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 1: integrate_cell<T, N, 1, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 2: integrate_cell<T, N, 2, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 3: integrate_cell<T, N, 3, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 4: integrate_cell<T, N, 4, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 5: integrate_cell<T, N, 5, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      case 6: integrate_cell<T, N, 6, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+      default: integrate_cell<T, N, 7, true, BInt<T, N>, DIMS>(a, i, j, k, face); break;
+    }
   }
 }
 
@@ -481,6 +539,12 @@ __global__ void batch_store_kernel(const BInst<T>* __restrict__ inst, const BIo*
   for (long long q = t0; q < I.n_eee * I.nr; q += stride) o.acs_bar[q] = I.acs_bar[q] * mul;
 }
 
+}  // namespace pn
+
+#include "pn_batch_tma.cuh"
+
+namespace pn {
+
 // ----------------------------------------------------------------------------------------------
 // host side: one group of solves with the same order and element type
 // ----------------------------------------------------------------------------------------------
@@ -505,10 +569,28 @@ class BatchGroup : public BatchGroupBase {
   cudaGraphExec_t gf = nullptr, ga = nullptr;
   cudaStream_t cap = nullptr;
   long long nl_f = 0, nl_a = 0, nl = 0;
+  int sms = 152;
+  // FP32 2D: box tiles through the TMA kernel, face tiles through the generic one
+  bool use_tma = false;
+  std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
+  std::vector<TTile> ttl[2];
+  std::vector<BTile> ftl[2];
+  std::vector<int> tend[2], fend[2];
+  TTile* dttl[2] = {nullptr, nullptr};
+  BTile* dftl[2] = {nullptr, nullptr};
+  CUtensorMap* dmaps = nullptr;
+  void* drows = nullptr;
+  int* dstatus = nullptr;
+  int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
+  cudaStream_t side = nullptr;     // face tiles run on a branch beside the box tiles
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   ~BatchGroup() override {
     if (gf) cudaGraphExecDestroy(gf);
     if (ga) cudaGraphExecDestroy(ga);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     if (cap) {
       // arena ranges are reused at once: let uploads still in flight land first
       if (arena) cudaStreamSynchronize(cap);
@@ -523,6 +605,13 @@ class BatchGroup : public BatchGroupBase {
   long long launches_forward() const override { return nl_f + 2; }
   long long launches_adjoint() const override { return nl_a + 2; }
   int stride() const override { return K; }
+  bool tma() const override { return use_tma; }
+  int device_status() override {
+    if (!dstatus) return PN_OK;
+    int v = 0;
+    PN_CUDA(cudaMemcpy(&v, dstatus, sizeof(int), cudaMemcpyDeviceToHost));
+    return v;
+  }
   int wait_created() override {
     PN_CUDA(cudaStreamSynchronize(cap));
     return PN_OK;
@@ -570,9 +659,16 @@ class BatchGroup : public BatchGroupBase {
   }
 
   static int n_ck_for(int ns, int K) { return (ns - 1) / K + 1; }
+
+  // tiles per block: enough blocks to fill the GPU about twice (SMs x 5 resident blocks), at
+  // most PN_BATCH_MAX_TPB tiles each
+  int tiles_per_block(int nt) const {
+    const int target = 2 * sms * 5;
+    return std::max(1, std::min(PN_BATCH_MAX_TPB, nt / std::max(1, target)));
+  }
   static int n_work_for(int K) { return std::max(2, K - 1); }
 
-  int create(const pn_desc* const* d, const int* idx, int cnt, long long budget, int Kreq) override {
+  int create(const pn_desc* const* d, const int* idx, int cnt, long long budget, int Kreq, int flags) override {
     n = cnt;
     members.assign(idx, idx + cnt);
     order.resize(n);
@@ -607,11 +703,30 @@ class BatchGroup : public BatchGroupBase {
     }
     if (K > max_ns) K = max_ns;
     hinst.assign(n, BInst<T>());
+    cur_descs.assign(n, nullptr);
+    for (int q = 0; q < n; ++q) cur_descs[q] = d[members[q]];
     int rc;
     PN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    {
+      int dev = 0;
+      PN_CUDA(cudaGetDevice(&dev));
+      PN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     for (int q = 0; q < n; ++q) {
       std::memset(&hinst[q], 0, sizeof(BInst<T>));
       if ((rc = build_instance(q, d[members[q]]))) return rc;
+    }
+    // partial slots: the eee tiles of list 0, numbered per solve in tile order
+    n_ptiles = 0;
+    pr = 1;
+    for (int q = 0; q < n; ++q) {
+      int cnt0 = 0;
+      for (int sgi = 0; sgi < hinst[q].nseg[0]; ++sgi)
+        if (hinst[q].seg[0][sgi].cls == 0) cnt0 += hinst[q].seg[0][sgi].nblocks;
+      hinst[q].ptile0 = n_ptiles;
+      hinst[q].n_ptile = cnt0;
+      n_ptiles += cnt0;
+      pr = std::max(pr, hinst[q].nr);
     }
     // tile lists (solve-major, group order)
     for (int list = 0; list < 3; ++list) {
@@ -620,31 +735,17 @@ class BatchGroup : public BatchGroupBase {
         hinst[q].tile0[list] = (int)tiles[list].size();
         for (int sgi = 0; sgi < hinst[q].nseg[list]; ++sgi) {
           const Seg& sg = hinst[q].seg[list][sgi];
-          for (int lb = 0; lb < sg.nblocks; ++lb) tiles[list].push_back(BTile{q, sgi, lb, 0});
+          for (int lb = 0; lb < sg.nblocks; ++lb) tiles[list].push_back(BTile{q, sgi, lb, pslot_of_tile(q, list, sgi, lb)});
         }
         tile_end[list][q] = (int)tiles[list].size();
       }
       if ((rc = upload(dtiles[list], tiles[list]))) return rc;
     }
-    // compact partials: the eee tiles lead each solve's list-0 tiles (class 0 is built first)
-    n_ptiles = 0;
-    pr = 1;
-    for (int q = 0; q < n; ++q) {
-      int cnt = 0;
-      bool leading = true;
-      for (int sgi = 0; sgi < hinst[q].nseg[0]; ++sgi) {
-        const Seg& sg = hinst[q].seg[0][sgi];
-        if (sg.cls == 0) {
-          if (!leading) { err = "internal: eee segments are not the leading tiles"; return PN_ERR_INVALID; }
-          cnt += sg.nblocks;
-        } else {
-          leading = false;
-        }
-      }
-      hinst[q].ptile0 = n_ptiles;
-      hinst[q].n_ptile = cnt;
-      n_ptiles += cnt;
-      pr = std::max(pr, hinst[q].nr);
+    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+      if (!(flags & PN_BATCH_GENERIC_KERNELS))
+        if ((rc = build_tma())) return rc;
+    } else {
+      (void)flags;
     }
     if ((rc = upload(dinst, hinst))) return rc;
     if ((rc = alloc(dio, n))) return rc;
@@ -653,6 +754,158 @@ class BatchGroup : public BatchGroupBase {
     if ((rc = capture(gf, true))) return rc;
     if ((rc = capture(ga, false))) return rc;
     return PN_OK;
+  }
+
+  // TMA path of an FP32 2D group: box/face tile lists, tensor maps, coefficient rows.  Leaves
+  // use_tma false (generic kernels) when a class grid is smaller than a box or the driver lacks
+  // the tensor-map encoder.
+  int build_tma() {
+    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+      using LY = TmaLayout<N>;
+      if (!encode_tiled_fn()) return PN_OK;
+      for (int q = 0; q < n; ++q)
+        for (int c = 0; c < 8; ++c)
+          if (hinst[q].active[c] && (hinst[q].shape[c][0] < BW || hinst[q].shape[c][1] < TY + 1)) return PN_OK;
+      int smem_optin = 0, dev = 0;
+      PN_CUDA(cudaGetDevice(&dev));
+      PN_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+      if (LY::SMEM + 2048 > smem_optin) return PN_OK;
+      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
+      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
+      int occ_f = 0, occ_a = 0;
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma2d_kernel<N, false>, BLOCK, LY::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma2d_kernel<N, true>, BLOCK, LY::SMEM));
+      if (occ_f < 1 || occ_a < 1) return PN_OK;
+      tma_grid[0] = occ_f * sms;
+      tma_grid[1] = occ_a * sms;
+      PN_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+      PN_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+      PN_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+      // coefficient rows: forward then adjoint, per solve
+      std::vector<ArgRow<N>> rows;
+      std::vector<int> arg_fwd(n), arg_adj(n);
+      for (int q = 0; q < n; ++q) {
+        const pn_desc* d = cur_descs[q];
+        const int ns = hinst[q].ns, ne = hinst[q].ne, nr = hinst[q].nr;
+        for (int pass = 0; pass < 2; ++pass) {
+          (pass == 0 ? arg_fwd : arg_adj)[q] = (int)rows.size();
+          const double* S = pass == 0 ? d->fwd_s : d->adj_s;
+          const double* Cc = pass == 0 ? d->fwd_c : d->adj_c;
+          for (int row = 0; row < ns; ++row) {
+            ArgRow<N> a;
+            std::memset(&a, 0, sizeof(a));
+            for (int e = 0; e < ne; ++e) {
+              a.s[e] = float(S[(long long)row * ne + e]);
+              for (int l = 0; l <= N; ++l) a.c[e][l] = float(Cc[((long long)row * ne + e) * (N + 1) + l]);
+            }
+            if (pass == 0) a.bc = d->fwd_bc[row];
+            else
+              for (int r = 0; r < nr; ++r) a.sig[r] = d->adj_src_sigma[(long long)row * nr + r];
+            rows.push_back(a);
+          }
+        }
+      }
+      ArgRow<N>* dr = nullptr;
+      int rc;
+      if ((rc = upload(dr, rows))) return rc;
+      drows = dr;
+      // tensor maps
+      std::vector<CUtensorMap> maps((size_t)n * 8 * TM_KINDS);
+      std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+      for (int q = 0; q < n; ++q) {
+        const BInst<T>& I = hinst[q];
+        const long long nslots = 1 + I.n_ck + n_work_for(K);
+        for (int c = 0; c < 8; ++c) {
+          const int nm = I.g[c].nm;
+          if (!I.active[c] || nm == 0) continue;
+          CUtensorMap* m = &maps[((size_t)q * 8 + c) * TM_KINDS];
+          const long long st_dims[4] = {I.shape[c][0], I.shape[c][1], nm, nslots};
+          const long long st_str[4] = {1, I.px[c], I.g[c].ms, I.slot_elems};
+          const int box4[4] = {BW, TY, nm, 1}, box5[4] = {BW, TY + 1, nm, 1};
+          bool ok = encode_f32(&m[TM_ST4], I.slots + I.dev_off[c], 4, st_dims, st_str, box4) &&
+                    encode_f32(&m[TM_ST5], I.slots + I.dev_off[c], 4, st_dims, st_str, box5) &&
+                    encode_f32(&m[TM_LAM4], I.lam + I.dev_off[c], 3, st_dims, st_str, box4) &&
+                    encode_f32(&m[TM_LAM5], I.lam + I.dev_off[c], 3, st_dims, st_str, box5);
+          const long long rho_dims[3] = {I.shape[c][0], I.shape[c][1], I.ne};
+          const int boxr[3] = {BW, TY, I.ne};
+          ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 3, rho_dims, st_str, boxr);
+          if (!ok) {
+            err = "tensor map encoding failed";
+            return PN_ERR_CUDA;
+          }
+        }
+      }
+      if ((rc = upload(dmaps, maps))) return rc;
+      if ((rc = alloc(dstatus, 1))) return rc;
+      PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), cap));
+      // tile lists: TMA box tiles and the rest (faces) per parity list
+      for (int list = 0; list < 2; ++list) {
+        tend[list].assign(n, 0);
+        fend[list].assign(n, 0);
+        for (int q = 0; q < n; ++q) {
+          for (int sgi = 0; sgi < hinst[q].nseg[list]; ++sgi) {
+            const Seg& sg = hinst[q].seg[list][sgi];
+            const bool box = sg.kind == 0 && sg.tile_x == TX && sg.ext[2] == 1;
+            for (int lb = 0; lb < sg.nblocks; ++lb) {
+              const int ps = pslot_of_tile(q, list, sgi, lb);
+              if (box && class_moments_host(sg.cls) > 0) {
+                TTile tt;
+                const int bx = lb % sg.tiles_x, by = lb / sg.tiles_x;
+                tt.inst = q;
+                tt.cls = sg.cls;
+                tt.x0 = sg.lo[0] + bx * TX;
+                tt.y0 = sg.lo[1] + by * TY;
+                tt.ext_x = std::min(TX, sg.ext[0] - bx * TX);
+                tt.ext_y = std::min(TY, sg.ext[1] - by * TY);
+                tt.pslot = ps;
+                tt.ns = hinst[q].ns;
+                tt.n_ck = hinst[q].n_ck;
+                tt.ne = hinst[q].ne;
+                tt.arg_fwd = arg_fwd[q];
+                tt.arg_adj = arg_adj[q];
+                ttl[list].push_back(tt);
+              } else {
+                ftl[list].push_back(BTile{q, sgi, lb, ps});
+              }
+            }
+          }
+          tend[list][q] = (int)ttl[list].size();
+          fend[list][q] = (int)ftl[list].size();
+        }
+        if ((rc = upload(dttl[list], ttl[list]))) return rc;
+        if ((rc = upload(dftl[list], ftl[list]))) return rc;
+      }
+      use_tma = true;
+    }
+    return PN_OK;
+  }
+
+  static int class_moments_host(int c) {
+    switch (c) {
+      case 0: return Ord<N>::n(0);
+      case 1: return Ord<N>::n(1);
+      case 2: return Ord<N>::n(2);
+      case 3: return Ord<N>::n(3);
+      case 4: return Ord<N>::n(4);
+      case 5: return Ord<N>::n(5);
+      case 6: return Ord<N>::n(6);
+      default: return Ord<N>::n(7);
+    }
+  }
+
+  int pslot_of_tile(int q, int list, int sgi, int lb) const {
+    if (list != 0 || hinst[q].seg[0][sgi].cls != 0) return -1;
+    int s = hinst[q].ptile0;
+    for (int k = 0; k < sgi; ++k)
+      if (hinst[q].seg[0][k].cls == 0) s += hinst[q].seg[0][k].nblocks;
+    return s + lb;
+  }
+
+  static int prefix_active(const std::vector<BInst<T>>& hi, const std::vector<int>& ends, int x) {
+    int cnt = 0;
+    for (size_t q = 0; q < ends.size(); ++q)
+      if (hi[q].ns > x) cnt = ends[q];
+    return cnt;
   }
 
   int build_instance(int q, const pn_desc* d) {
@@ -861,6 +1114,9 @@ class BatchGroup : public BatchGroupBase {
 
   // --------------------------------------------------------------------------------------------
   int launch(int list, int mode, int j, int sub, double* part, bool adj, bool integ) {
+    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+      if (use_tma && !integ) return launch_tma(list, mode, j, sub, part, adj);
+    }
     const int x = integ ? j - 1 : j;   // integrate at iteration j includes the solves with ns == j
     const int nt = tiles_active(integ ? 2 : list, x);
     if (nt == 0) return PN_OK;
@@ -874,14 +1130,75 @@ class BatchGroup : public BatchGroupBase {
     a.K = K;
     a.partial = part;
     a.pr = pr;
+    a.n_tiles = nt;
+    a.tpb = tiles_per_block(nt);
+    const int grid = (nt + a.tpb - 1) / a.tpb;
     if (integ)
-      batch_integrate_kernel<T, N, DIMS><<<nt, BLOCK, 0, cap>>>(a);
+      batch_integrate_kernel<T, N, DIMS><<<grid, BLOCK, 0, cap>>>(a);
     else if (adj)
-      batch_substep_kernel<T, N, true, DIMS><<<nt, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, true, DIMS><<<grid, BLOCK, 0, cap>>>(a);
     else
-      batch_substep_kernel<T, N, false, DIMS><<<nt, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, false, DIMS><<<grid, BLOCK, 0, cap>>>(a);
     PN_CUDA(cudaGetLastError());
     ++nl;
+    return PN_OK;
+  }
+
+  // TMA path of a sub-step: faces (generic kernel) and box tiles (TMA kernel), same stream
+  int launch_tma(int list, int mode, int j, int sub, double* part, bool adj) {
+    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+      const int nf = prefix_active(hinst, fend[list], j);
+      const int nb = prefix_active(hinst, tend[list], j);
+      if (nf > 0) {
+        // faces on a branch beside the box tiles: disjoint cells, partial slots and ghost writes
+        PN_CUDA(cudaEventRecord(ev_fork, cap));
+        PN_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+        BLaunch<T> a;
+        a.inst = dinst;
+        a.tiles = dftl[list];
+        a.list = list;
+        a.mode = mode;
+        a.j = j;
+        a.sub = sub;
+        a.K = K;
+        a.partial = part;
+        a.pr = pr;
+        a.n_tiles = nf;
+        a.tpb = 1;
+        if (adj)
+          batch_substep_kernel<T, N, true, DIMS><<<nf, BLOCK, 0, side>>>(a);
+        else
+          batch_substep_kernel<T, N, false, DIMS><<<nf, BLOCK, 0, side>>>(a);
+        PN_CUDA(cudaGetLastError());
+        PN_CUDA(cudaEventRecord(ev_join, side));
+        ++nl;
+      }
+      if (nb > 0) {
+        TLaunch<N> a;
+        a.inst = dinst;
+        a.tiles = dttl[list];
+        a.maps = dmaps;
+        a.rows = static_cast<const ArgRow<N>*>(drows);
+        a.partial = part;
+        a.status = dstatus;
+        a.pr = pr;
+        a.n_tiles = nb;
+        a.mode = mode;
+        a.j = j;
+        a.sub = sub;
+        a.K = K;
+        const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
+        if (adj)
+          batch_tma2d_kernel<N, true><<<grid, BLOCK, TmaLayout<N>::SMEM, cap>>>(a);
+        else
+          batch_tma2d_kernel<N, false><<<grid, BLOCK, TmaLayout<N>::SMEM, cap>>>(a);
+        PN_CUDA(cudaGetLastError());
+        ++nl;
+      }
+      if (nf > 0) PN_CUDA(cudaStreamWaitEvent(cap, ev_join, 0));
+    } else {
+      (void)list; (void)mode; (void)j; (void)sub; (void)part; (void)adj;
+    }
     return PN_OK;
   }
 

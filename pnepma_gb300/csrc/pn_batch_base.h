@@ -26,7 +26,7 @@ struct BIo {
 class BatchGroupBase {
  public:
   virtual ~BatchGroupBase() {}
-  virtual int create(const pn_desc* const* d, const int* idx, int n, long long budget, int K) = 0;
+  virtual int create(const pn_desc* const* d, const int* idx, int n, long long budget, int K, int flags) = 0;
   virtual int forward(const BIo* io_host, cudaStream_t s) = 0;
   virtual int adjoint(const BIo* io_host, cudaStream_t s) = 0;
   virtual long long device_bytes() const = 0;
@@ -35,6 +35,11 @@ class BatchGroupBase {
   virtual int stride() const = 0;
   // wait for the uploads create() issued on the group's own stream
   virtual int wait_created() = 0;
+  // true when the group's sub-steps run through the TMA tile kernel
+  virtual bool tma() const { return false; }
+  // status word of the group's kernels (PN_OK, or PN_ERR_TIMEOUT after a wait ran out); read it
+  // once the group's work has completed
+  virtual int device_status() { return PN_OK; }
   // device ranges come from this arena when set (returned to it, never cudaFree'd), else cudaMalloc
   Arena* arena = nullptr;
   std::string err;

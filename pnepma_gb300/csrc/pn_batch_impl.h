@@ -12,8 +12,11 @@ namespace pn {
 // Group the solves by (order, active axes), build each group's tables, tiles and graphs.  With
 // an arena every device range is taken from it; without one, from cudaMalloc.  Waits only for
 // the group streams' own uploads.  budget: device bytes the checkpoint tapes may take.
-int batch_create(const pn_desc* const* descs, int n, long long budget, int K, Arena* arena, pn_batch** out,
+int batch_create(const pn_desc* const* descs, int n, long long budget, int K, int flags, Arena* arena, pn_batch** out,
                  std::string& err);
+
+// PN_OK, or the first error status a group's kernels recorded (read after the work completed)
+int batch_status(pn_batch* b);
 
 long long batch_device_bytes(const pn_batch* b);
 

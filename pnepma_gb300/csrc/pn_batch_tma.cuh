@@ -1,0 +1,461 @@
+// pn_batch_tma.cuh -- FP32 2D sub-step of the batched engine with TMA-staged halo tiles.
+//
+// The same arithmetic as batch_substep_kernel (substep_cell with compiled coupling blocks, x then
+// y), so results are bit-identical; only the way operands reach the registers differs:
+//
+//   * persistent CTAs (two per SM) walk the box tiles of a launch in grid-stride order, so the
+//     CTAs resident at any time work on neighbouring tiles;
+//   * for each 32 x 4 tile, one thread issues four cp.async.bulk.tensor loads -- the target
+//     class's moments, the x- and y-neighbour classes with their one-cell halo, the densities --
+//     plus one cp.async.bulk of the step's coefficient row, all completing on one mbarrier;
+//   * a ring of PN_TMA_STAGES stages: with two, the loads of the next tile run while the CTA
+//     computes the current one from shared memory, where every operand sits at a compile-time
+//     offset; with one, more CTAs fit on an SM and overlap one another.
+//
+// Boxes start at x = x0 - 1 = 32 bx (x0 = 1 + 32 bx is the tile's first cell): 4-float aligned,
+// as tiled TMA requires; cells outside the class grid are zero-filled and never used.  Nothing is
+// stored by TMA: results go to global memory from registers, interior cells only.  Face cells
+// (which compute ghost points) stay with batch_substep_kernel.
+//
+// Waits on the mbarrier are bounded (1 s by %globaltimer).  A CTA whose wait runs out records
+// PN_ERR_TIMEOUT in the launch's status word, waits (again bounded) for its copies in flight and
+// returns.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <mutex>
+
+namespace pn {
+
+constexpr int TX = 32;          // tile width (cells)
+constexpr int TY = BLOCK / TX;  // tile height (rows)
+constexpr int BW = TX + 4;      // box width: x0 - 1 .. x0 + 34 (a multiple of 4 floats)
+constexpr int PL4 = BW * TY;    // floats per moment plane of a 4-row box
+constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row box (y halo on the side the stencil reads)
+
+// stages of the tile ring per CTA (1: no prefetch within a CTA, more CTAs per SM)
+#ifndef PN_TMA_STAGES
+#define PN_TMA_STAGES 1
+#endif
+constexpr int TSTAGES = PN_TMA_STAGES;
+
+// Coefficients of one step, copied to shared memory with the tile (16-byte multiple).
+template <int N>
+struct ArgRow {
+  float s[MAXE];
+  float c[MAXE][N + 1];
+  double bc;
+  double sig[MAXR];
+  double pad_;   // the floats fill 16 (N + 2) bytes; bc, sig and this pad 80
+};
+static_assert(MAXE == 4 && MAXR == 8, "ArgRow padding assumes 4 elements and 8 lines");
+
+// One 32 x 4 box tile of a target class (48 bytes).
+struct TTile {
+  int inst;     // solve (group order)
+  int cls;      // target class (z-even in 2D)
+  int x0, y0;   // first cell
+  int ext_x;    // valid cells along x (<= 32)
+  int ext_y;    // valid rows (<= 4)
+  int pslot;    // partial slot of an eee tile, else -1
+  int ns;
+  int n_ck;
+  int ne;
+  int arg_fwd;  // index of the solve's first forward ArgRow
+  int arg_adj;  // ... adjoint ArgRow
+};
+
+// tensor maps per (solve, class)
+enum { TM_ST4 = 0, TM_ST5 = 1, TM_LAM4 = 2, TM_LAM5 = 3, TM_RHO = 4, TM_KINDS = 5 };
+
+template <int N>
+struct TLaunch {
+  const BInst<float>* inst;
+  const TTile* tiles;
+  const CUtensorMap* maps;      // [solve][8][TM_KINDS]
+  const ArgRow<N>* rows;
+  double* partial;
+  int* status;
+  int pr;
+  int n_tiles;
+  int mode, j, sub, K;
+};
+
+template <int N>
+struct TmaLayout {
+  static constexpr int maxn(int a, int b) { return a > b ? a : b; }
+  static constexpr int NO = maxn(maxn(Ord<N>::n(0), Ord<N>::n(2)), maxn(Ord<N>::n(4), Ord<N>::n(6)));
+  static constexpr int NXN = maxn(maxn(Ord<N>::n(4), Ord<N>::n(6)), maxn(Ord<N>::n(0), Ord<N>::n(2)));
+  static constexpr int NYN = NXN;
+  static constexpr int al(int b) { return (b + 127) / 128 * 128; }
+  static constexpr int OWN = 0;
+  static constexpr int XN = OWN + al(NO * PL4 * 4);
+  static constexpr int YN = XN + al(NXN * PL4 * 4);
+  static constexpr int RHO = YN + al(NYN * PL5 * 4);
+  static constexpr int ARG = RHO + al(MAXE * PL4 * 4);
+  static constexpr int STAGE = ARG + al((int)sizeof(ArgRow<N>));
+  static constexpr int SMEM = TSTAGES * STAGE;
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait for phase `parity` of the barrier, at most ~1 s
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(b, parity)) return true;
+    if (global_ns() - t0 > 1000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+// slot of state j (the index form of bslot)
+__device__ __forceinline__ int slot_index(int ns, int n_ck, int j, int K, bool segment, int m) {
+  if (j >= ns) return 0;
+  if (j % K == 0) return 1 + j / K;
+  const int w = segment ? (j - m * K - 1) : (j & 1);
+  return 1 + n_ck + w;
+}
+
+template <int N>
+__device__ __forceinline__ int class_moments(int c) {
+  switch (c) {
+    case 0: return Ord<N>::n(0);
+    case 1: return Ord<N>::n(1);
+    case 2: return Ord<N>::n(2);
+    case 3: return Ord<N>::n(3);
+    case 4: return Ord<N>::n(4);
+    case 5: return Ord<N>::n(5);
+    case 6: return Ord<N>::n(6);
+    default: return Ord<N>::n(7);
+  }
+}
+
+// Issue the loads of tile t into stage `st` (one thread).
+template <int N, bool ADJ>
+__device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
+                                          unsigned long long* bar) {
+  using LY = TmaLayout<N>;
+  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
+  const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
+  int own_slot = 0, from_slot = 0, row;
+  if (!ADJ) {
+    const bool segment = L.mode == BM_RECOMPUTE;
+    const int m = L.j / L.K;
+    const int src = slot_index(tt.ns, tt.n_ck, L.j + 1, L.K, segment, m);
+    const int dst = slot_index(tt.ns, tt.n_ck, L.j, L.K, segment, m);
+    own_slot = (L.sub == 3) ? dst : src;
+    from_slot = (L.sub == 1) ? src : dst;
+    row = tt.arg_fwd + (tt.ns - L.j - 1);
+  } else {
+    row = tt.arg_adj + L.j;
+  }
+  const unsigned bytes = 4u * (unsigned)(PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) + (unsigned)sizeof(ArgRow<N>);
+  // the y box starts one row below the tile for a target odd in y (it reads rows j - 1 and j),
+  // at the tile for one even in y (rows j and j + 1)
+  const int ya = tt.y0 - ((c >> 1) & 1);
+  mbar_expect_tx(bar, bytes);
+  const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
+  const int xa = tt.x0 - 1;
+  if (ADJ) {
+    tma_load_3d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
+    if (n_x > 0) tma_load_3d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
+    if (n_y > 0) tma_load_3d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM5, xa, ya, 0, bar);
+  } else {
+    tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST4, xa, tt.y0, 0, own_slot, bar);
+    if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST4, xa, tt.y0, 0, from_slot, bar);
+    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST5, xa, ya, 0, from_slot, bar);
+  }
+  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
+  bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
+}
+
+// One cell of a staged tile: substep_cell's arithmetic with operands from shared memory.
+template <int N, int C, bool ADJ>
+__device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, const unsigned char* st,
+                                         double (&red)[BLOCK / 32][MAXR]) {
+  using LY = TmaLayout<N>;
+  constexpr int n = Ord<N>::n(C);
+  constexpr bool oddx = (C >> 2) & 1;
+  const float* own = reinterpret_cast<const float*>(st + LY::OWN);
+  const float* xn = reinterpret_cast<const float*>(st + LY::XN);
+  const float* yn = reinterpret_cast<const float*>(st + LY::YN);
+  const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
+  const ArgRow<N>& ar = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
+  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  const bool valid = tx < tt.ext_x && ty < tt.ext_y;
+  const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
+  double part[MAXR];
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
+  if constexpr (n > 0) {
+    if (valid) {
+      const BInst<float>& I = L.inst[tt.inst];
+      const int i = tt.x0 + tx, j = tt.y0 + ty;
+      const int lo = ty * BW + tx + 1;
+      const int xr = ty * BW + tx + (oddx ? 1 : 2), xl = xr - 1;
+      const int yr = (ty + 1) * BW + tx + 1, yl = yr - BW;   // rows j (+1) and j - 1 (j) of the y box
+      const float ihx = I.inv_h[0], ihy = I.inv_h[1];
+      float acc[n];
+#pragma unroll
+      for (int m = 0; m < n; ++m) acc[m] = 0.0f;
+      {
+        constexpr int F = C ^ 4;
+        if constexpr (Ord<N>::n(F) > 0) {
+          auto diff = [&](int q) -> float {
+            const float a = xn[q * PL4 + xr];
+            const float b = xn[q * PL4 + xl];
+            const float d = ADJ ? (b - a) : (a - b);
+            return d * ihx;
+          };
+          auto coef = [&](int kk, double lit) -> float {
+            (void)kk;
+            return float(lit);
+          };
+          Adv<N, C, 0>::template apply<float>(acc, diff, coef);
+        }
+      }
+      {
+        constexpr int F = C ^ 2;
+        if constexpr (Ord<N>::n(F) > 0) {
+          auto diff = [&](int q) -> float {
+            const float a = yn[q * PL5 + yr];
+            const float b = yn[q * PL5 + yl];
+            const float d = ADJ ? (b - a) : (a - b);
+            return d * ihy;
+          };
+          auto coef = [&](int kk, double lit) -> float {
+            (void)kk;
+            return float(lit);
+          };
+          Adv<N, C, 1>::template apply<float>(acc, diff, coef);
+        }
+      }
+      float rr[MAXE];
+      float S = 0.0f;
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        rr[e] = e < tt.ne ? rh[e * PL4 + lo] : 0.0f;
+        S = fmaf(rr[e], ar.s[e], S);
+      }
+      const float invS = recip(S);
+      const float dt = L.sub == 2 ? I.dE : I.dE * 0.5f;
+      constexpr unsigned mask = Ord<N>::deg_mask(C);
+      float Cl[N + 1];
+      float ph[N + 1];
+#pragma unroll
+      for (int l = 0; l <= N; ++l) {
+        if ((mask >> l) & 1u) {
+          float cc = 0.0f;
+#pragma unroll
+          for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
+          Cl[l] = cc;
+          ph[l] = phi1(-cc * invS * dt);
+        } else {
+          Cl[l] = 0.0f;
+          ph[l] = 1.0f;
+        }
+      }
+      float q0 = 0.0f;
+      long long ce = 0;
+      if constexpr (C == 0) ce = eee_cell(I.g[0], i, j, 0);
+      if constexpr (ADJ && C == 0) {
+        double q = 0.0;
+        for (int r = 0; r < I.nr; ++r)
+          q = q - ar.sig[r] * I.acs[ce * I.nr + r] * I.noa[ce * I.ne + I.xel[r]] * I.ibar[r];
+        q0 = float(q);
+      }
+      float* base;
+      if (ADJ) {
+        base = I.lam;
+      } else {
+        const bool segment = L.mode == BM_RECOMPUTE;
+        base = I.slots + (long long)slot_index(tt.ns, tt.n_ck, L.j, L.K, segment, L.j / L.K) * I.slot_elems;
+      }
+      const Geom& gt = I.g[C];
+      float* un = base + I.dev_off[C] + (long long)j * gt.px + i;
+      const long long ms = gt.ms;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const int l = degree_of<N, C>(m);
+        const float u = own[m * PL4 + lo];
+        const float q = (m == 0) ? q0 : 0.0f;
+        const float num = (q - acc[m]) - Cl[l] * u;
+        const float du = num * invS * ph[l];
+        const float unew = u + dt * du;
+        un[m * ms] = unew;
+        if constexpr (C == 0 && !ADJ) {
+          if (m == 0 && want_part) {
+#pragma unroll
+            for (int r = 0; r < MAXR; ++r)
+              if (r < I.nr) part[r] += I.wint[ce * I.nr + r] * double(unew);
+          }
+        }
+      }
+    }
+  }
+  if (want_part && tt.pslot >= 0) {   // block-uniform
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r) {
+      double v = part[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[w][r] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < L.pr) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+      L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+template <int N, bool ADJ>
+__global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_constant__ TLaunch<N> L) {
+  using LY = TmaLayout<N>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long full[TSTAGES];
+  __shared__ double red[BLOCK / 32][MAXR];
+  // tensor copies need 128-byte aligned destinations: refuse (uniformly) rather than fault
+  if ((smem_u32(smem) & 127u) != 0u) {
+    if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TSTAGES; ++s) mbar_init(&full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int G = gridDim.x;
+  const int t0 = blockIdx.x;
+  // tiles t0 + k G, k = 0, 1, ...; tile k lives in stage k % TSTAGES, use (k / TSTAGES) of its barrier
+  if (threadIdx.x == 0)
+    for (int k = 0; k < TSTAGES - 1; ++k) {
+      const int t = t0 + k * G;
+      if (t < L.n_tiles) tma_issue<N, ADJ>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
+    }
+  for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
+    const int t = t0 + k * G;
+    const int s = k % TSTAGES;
+    const int ka = k + TSTAGES - 1;   // tile issued now, into the stage freed by iteration k - 1
+    const int ta = t0 + ka * G;
+    if (ta < L.n_tiles && threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tma_issue<N, ADJ>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
+    }
+    const TTile tt = L.tiles[t];
+    const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(L.status, (int)PN_ERR_TIMEOUT);
+        // let the copies still in flight land before the CTA's shared memory is released
+        for (int kk = k; kk <= ka; ++kk)
+          if (t0 + kk * G < L.n_tiles) mbar_wait_bounded(&full[kk % TSTAGES], (unsigned)((kk / TSTAGES) & 1));
+      }
+      __syncthreads();
+      return;
+    }
+    const unsigned char* st = smem + s * LY::STAGE;
+    switch (tt.cls) {
+      case 0: tma_cell<N, 0, ADJ>(L, tt, st, red); break;
+      case 2: tma_cell<N, 2, ADJ>(L, tt, st, red); break;
+      case 4: tma_cell<N, 4, ADJ>(L, tt, st, red); break;
+      default: tma_cell<N, 6, ADJ>(L, tt, st, red); break;
+    }
+    __syncthreads();   // stage s is free for the loads issued in the next iteration
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host: tensor maps
+// ---------------------------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+inline EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// FP32 tensor of rank 3 (x, y, plane) or 4 (x, y, plane, slot); strides in elements
+inline bool encode_f32(CUtensorMap* out, void* base, int rank, const long long* dims, const long long* strides,
+                       const int* box) {
+  EncodeTiledFn fn = encode_tiled_fn();
+  if (!fn) return false;
+  cuuint64_t gd[4], gs[3];
+  cuuint32_t bd[4], es[4];
+  for (int d = 0; d < rank; ++d) {
+    gd[d] = (cuuint64_t)dims[d];
+    bd[d] = (cuuint32_t)box[d];
+    es[d] = 1;
+    if (d > 0) gs[d - 1] = (cuuint64_t)strides[d] * 4u;
+  }
+  return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, base, gd, gs, bd, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+}  // namespace pn

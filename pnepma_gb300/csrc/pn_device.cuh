@@ -129,8 +129,19 @@ __device__ __forceinline__ double phi1(double c) {
   return (exp(c) - 1.0) / c;
 }
 
+// FP32 phi1(c) = (e^c - 1) / c.  |c| <= 1/4: the Taylor series sum_k c^k / (k+1)! to k = 6
+// (truncation below 2e-9 relative); otherwise the fast exponential and division (ex2.approx-based
+// __expf, __fdividef), whose relative error is ~1e-6 at |c| = 1/4, where e^c - 1 cancels most,
+// and smaller beyond.  pn_selftest_phi1 compares it with expm1f(c) / c on the device.
 __device__ __forceinline__ float phi1(float c) {
-  // FP32: exp(c) - 1 cancels for small |c|; expm1f keeps full relative accuracy
+  const float t = 1.0f + c * (0.5f + c * (1.0f / 6.0f + c * (1.0f / 24.0f + c * (1.0f / 120.0f +
+                  c * (1.0f / 720.0f + c * (1.0f / 5040.0f))))));
+  if (fabsf(c) <= 0.25f) return t;
+  return __fdividef(__expf(c) - 1.0f, c);
+}
+
+// the reference form in FP32, for the self-test
+__device__ __forceinline__ float phi1_ref(float c) {
   if (fabsf(c) <= 1e-3f) return 1.0f + c * (0.5f + c * (1.0f / 6.0f));
   return expm1f(c) / c;
 }

@@ -228,7 +228,7 @@ int pn_server::launch_wave(Wave* w) {
   int rc = PN_ERR_NO_MEMORY;
   for (long long budget : tries) {
     std::string err;
-    rc = pn::batch_create(descs.data(), n, budget, K, arena.get(), &w->b, err);
+    rc = pn::batch_create(descs.data(), n, budget, K, 0, arena.get(), &w->b, err);
     if (rc == PN_OK) break;
     w->err = err;
     if (rc != PN_ERR_NO_MEMORY) break;
@@ -283,6 +283,13 @@ void pn_server::finish_wave(Wave* w) {
   if (e != cudaSuccess && rc == PN_OK) {
     rc = PN_ERR_CUDA;
     err = std::string("wave failed on the device: ") + cudaGetErrorString(e);
+  }
+  if (rc == PN_OK) {
+    const int st = pn::batch_status(w->b);
+    if (st != PN_OK) {
+      rc = st;
+      err = "a bounded device-side wait of the wave ran out";
+    }
   }
   pn_batch_destroy(w->b);
   w->b = nullptr;

@@ -27,13 +27,13 @@ def mixed_solves(precision):
     return out
 
 
-def run_batch(torch, solves, K=0):
+def run_batch(torch, solves, K=0, flags=0):
     descs, keep = [], []
     for s in solves:
         d, k = s.problem.descriptor(s.x_rays)
         descs.append(d)
         keep.append(k)
-    b = capi.Batch(descs, keep, checkpoint_stride=K)
+    b = capi.Batch(descs, keep, checkpoint_stride=K, flags=flags)
     ins, outs = [], []
     for s in solves:
         rho, noa, acs = s.inputs()
@@ -95,3 +95,42 @@ def test_batch_fp32_against_fp64_oracle(gpu_lib, oracle):
         assert rel(rb[q], rb_o) < 1e-3, q
         assert rel(nb[q], nb_o) < 1e-3, q
         assert rel(ab[q], ab_o) < 1e-3, q
+
+
+def tma_solves():
+    """FP32 2D solves on grids wide enough for the TMA box tiles (partial tiles at the edges)."""
+    return [
+        workloads.small_case(dims=2, N=3, shape=(40, 12), n_steps=7, seed=11, precision=PN_FP32),
+        workloads.small_case(dims=2, N=5, shape=(40, 12), n_steps=5, seed=12, precision=PN_FP32),
+        workloads.small_case(dims=2, N=7, shape=(44, 16), n_steps=6, seed=13, precision=PN_FP32,
+                             elements=("Fe", "Cr", "Ni")),
+        workloads.small_case(dims=2, N=11, shape=(40, 12), n_steps=4, seed=14, precision=PN_FP32),
+        workloads.small_case(dims=2, N=3, shape=(70, 9), n_steps=9, seed=15, precision=PN_FP32),
+    ]
+
+
+@pytest.mark.parametrize("K", [1, 3])
+def test_tma_tiles_match_the_generic_kernels_bit_for_bit(gpu_lib, K):
+    torch = pytest.importorskip("torch")
+    solves = tma_solves()
+    got = run_batch(torch, solves, K=K)
+    ref = run_batch(torch, solves, K=K, flags=capi.PN_BATCH_GENERIC_KERNELS)
+    assert got[5].tma_groups == got[5].n_groups == 4
+    assert ref[5].tma_groups == 0
+    for a, b in zip(got[:5], ref[:5]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
+def test_tma_tiles_against_the_oracle(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    solves = tma_solves()[:2]
+    I, ib, rb, nb, ab, info = run_batch(torch, solves)
+    assert info.tma_groups == 2
+    for q, s in enumerate(solves):
+        rho, noa, acs = s.inputs()
+        s.problem.precision = PN_FP64
+        d, k = s.problem.descriptor(s.x_rays)
+        I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[q])
+        assert rel(I[q], I_o) < 1e-4
+        assert rel(rb[q], rb_o) < 1e-3
