@@ -574,23 +574,18 @@ class BatchGroup : public BatchGroupBase {
   bool use_tma = false;
   std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
   std::vector<TTile> ttl[2];
-  std::vector<BTile> ftl[2];
-  std::vector<int> tend[2], fend[2];
+  std::vector<GFace> gfl[2];
+  std::vector<int> tend[2], gend[2], gthr[2];   // per solve: tile / face / ghost-thread prefix ends
   TTile* dttl[2] = {nullptr, nullptr};
-  BTile* dftl[2] = {nullptr, nullptr};
+  GFace* dgfl[2] = {nullptr, nullptr};
   CUtensorMap* dmaps = nullptr;
   void* drows = nullptr;
   int* dstatus = nullptr;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
-  cudaStream_t side = nullptr;     // face tiles run on a branch beside the box tiles
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   ~BatchGroup() override {
     if (gf) cudaGraphExecDestroy(gf);
     if (ga) cudaGraphExecDestroy(ga);
-    if (side) cudaStreamDestroy(side);
-    if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
     if (cap) {
       // arena ranges are reused at once: let uploads still in flight land first
       if (arena) cudaStreamSynchronize(cap);
@@ -765,7 +760,9 @@ class BatchGroup : public BatchGroupBase {
       if (!encode_tiled_fn()) return PN_OK;
       for (int q = 0; q < n; ++q)
         for (int c = 0; c < 8; ++c)
-          if (hinst[q].active[c] && (hinst[q].shape[c][0] < BW || hinst[q].shape[c][1] < TY + 1)) return PN_OK;
+          if (hinst[q].active[c] && (hinst[q].shape[c][0] < BW || hinst[q].shape[c][1] < TY + 1 || hinst[q].shape[c][0] > 2040 ||
+                                     hinst[q].shape[c][1] > 2040))
+            return PN_OK;
       int smem_optin = 0, dev = 0;
       PN_CUDA(cudaGetDevice(&dev));
       PN_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -778,9 +775,6 @@ class BatchGroup : public BatchGroupBase {
       if (occ_f < 1 || occ_a < 1) return PN_OK;
       tma_grid[0] = occ_f * sms;
       tma_grid[1] = occ_a * sms;
-      PN_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
-      PN_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-      PN_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
       // coefficient rows: forward then adjoint, per solve
       std::vector<ArgRow<N>> rows;
       std::vector<int> arg_fwd(n), arg_adj(n);
@@ -838,42 +832,77 @@ class BatchGroup : public BatchGroupBase {
       if ((rc = upload(dmaps, maps))) return rc;
       if ((rc = alloc(dstatus, 1))) return rc;
       PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), cap));
-      // tile lists: TMA box tiles and the rest (faces) per parity list
+      // tiles over every target cell, and the single-axis ghost faces, per parity list; partial
+      // slots are the eee tiles of list 0 in tile order
+      n_ptiles = 0;
+      for (int q = 0; q < n; ++q) {
+        hinst[q].ptile0 = 0;
+        hinst[q].n_ptile = 0;
+      }
       for (int list = 0; list < 2; ++list) {
         tend[list].assign(n, 0);
-        fend[list].assign(n, 0);
+        gend[list].assign(n, 0);
+        gthr[list].assign(n, 0);
+        int threads = 0;
         for (int q = 0; q < n; ++q) {
-          for (int sgi = 0; sgi < hinst[q].nseg[list]; ++sgi) {
-            const Seg& sg = hinst[q].seg[list][sgi];
-            const bool box = sg.kind == 0 && sg.tile_x == TX && sg.ext[2] == 1;
-            for (int lb = 0; lb < sg.nblocks; ++lb) {
-              const int ps = pslot_of_tile(q, list, sgi, lb);
-              if (box && class_moments_host(sg.cls) > 0) {
+          const BInst<T>& I = hinst[q];
+          if (list == 0) hinst[q].ptile0 = n_ptiles;
+          for (int c = 0; c < 8; ++c) {
+            if (!I.active[c] || class_parity(c) != list || class_moments_host(c) == 0) continue;
+            int lo3[2], hi3[2];
+            for (int k = 0; k < 2; ++k) {
+              const int nn = I.shape[c][k];
+              lo3[k] = class_bit(c, k) ? 1 : 0;
+              hi3[k] = class_bit(c, k) ? nn - 1 : nn;
+            }
+            const int xo = class_bit(c, 0) ? 1 : 4;
+            for (int y0 = lo3[1]; y0 < hi3[1]; y0 += TY)
+              for (int x0 = lo3[0]; x0 < hi3[0]; x0 += TX) {
                 TTile tt;
-                const int bx = lb % sg.tiles_x, by = lb / sg.tiles_x;
+                std::memset(&tt, 0, sizeof(tt));
                 tt.inst = q;
-                tt.cls = sg.cls;
-                tt.x0 = sg.lo[0] + bx * TX;
-                tt.y0 = sg.lo[1] + by * TY;
-                tt.ext_x = std::min(TX, sg.ext[0] - bx * TX);
-                tt.ext_y = std::min(TY, sg.ext[1] - by * TY);
-                tt.pslot = ps;
-                tt.ns = hinst[q].ns;
-                tt.n_ck = hinst[q].n_ck;
-                tt.ne = hinst[q].ne;
+                tt.cls = c;
+                tt.x0 = x0;
+                tt.y0 = y0;
+                tt.ext = std::min(TX, hi3[0] - x0) | (std::min(TY, hi3[1] - y0) << 8) | (xo << 16);
+                tt.pslot = (list == 0 && c == 0) ? n_ptiles++ : -1;
+                tt.ns = I.ns;
+                tt.n_ck = I.n_ck;
+                tt.ne = I.ne;
                 tt.arg_fwd = arg_fwd[q];
                 tt.arg_adj = arg_adj[q];
                 ttl[list].push_back(tt);
-              } else {
-                ftl[list].push_back(BTile{q, sgi, lb, ps});
+              }
+            // ghosts read by the class's face cells along each axis where it is even
+            for (int dax = 0; dax < 2; ++dax) {
+              if (class_bit(c, dax)) continue;
+              const int e = 1 - dax;
+              const int nf = class_moments_host(c ^ (4 >> dax));
+              if (nf == 0) continue;
+              for (int side_ = 0; side_ < 2; ++side_) {
+                GFace f;
+                std::memset(&f, 0, sizeof(f));
+                f.inst = q;
+                f.cls = c;
+                f.axis = dax;
+                f.side = side_;
+                f.t_lo = lo3[e];
+                f.t_cnt = hi3[e] - lo3[e];
+                f.thread0 = threads;
+                f.ns = I.ns;
+                f.arg_fwd = arg_fwd[q];
+                threads += f.t_cnt * nf;
+                gfl[list].push_back(f);
               }
             }
           }
+          if (list == 0) hinst[q].n_ptile = n_ptiles - hinst[q].ptile0;
           tend[list][q] = (int)ttl[list].size();
-          fend[list][q] = (int)ftl[list].size();
+          gend[list][q] = (int)gfl[list].size();
+          gthr[list][q] = threads;
         }
         if ((rc = upload(dttl[list], ttl[list]))) return rc;
-        if ((rc = upload(dftl[list], ftl[list]))) return rc;
+        if ((rc = upload(dgfl[list], gfl[list]))) return rc;
       }
       use_tma = true;
     }
@@ -1144,35 +1173,33 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  // TMA path of a sub-step: faces (generic kernel) and box tiles (TMA kernel), same stream
+  // TMA path of a sub-step: the ghost points the face cells read, then every target cell
   int launch_tma(int list, int mode, int j, int sub, double* part, bool adj) {
     if constexpr (std::is_same<T, float>::value && DIMS == 3) {
-      const int nf = prefix_active(hinst, fend[list], j);
-      const int nb = prefix_active(hinst, tend[list], j);
-      if (nf > 0) {
-        // faces on a branch beside the box tiles: disjoint cells, partial slots and ghost writes
-        PN_CUDA(cudaEventRecord(ev_fork, cap));
-        PN_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
-        BLaunch<T> a;
-        a.inst = dinst;
-        a.tiles = dftl[list];
-        a.list = list;
-        a.mode = mode;
-        a.j = j;
-        a.sub = sub;
-        a.K = K;
-        a.partial = part;
-        a.pr = pr;
-        a.n_tiles = nf;
-        a.tpb = 1;
+      int last = -1;
+      for (int q = 0; q < n; ++q)
+        if (hinst[q].ns > j) last = q;
+      if (last < 0) return PN_OK;
+      const int nthr = gthr[list][last];
+      if (nthr > 0) {
+        GLaunch<N> g;
+        g.inst = dinst;
+        g.faces = dgfl[list];
+        g.rows = static_cast<const ArgRow<N>*>(drows);
+        g.n_faces = gend[list][last];
+        g.n_threads = nthr;
+        g.mode = mode;
+        g.j = j;
+        g.sub = sub;
+        g.K = K;
         if (adj)
-          batch_substep_kernel<T, N, true, DIMS><<<nf, BLOCK, 0, side>>>(a);
+          batch_ghost2d_kernel<N, true><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
         else
-          batch_substep_kernel<T, N, false, DIMS><<<nf, BLOCK, 0, side>>>(a);
+          batch_ghost2d_kernel<N, false><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
         PN_CUDA(cudaGetLastError());
-        PN_CUDA(cudaEventRecord(ev_join, side));
         ++nl;
       }
+      const int nb = tend[list][last];
       if (nb > 0) {
         TLaunch<N> a;
         a.inst = dinst;
@@ -1195,7 +1222,6 @@ class BatchGroup : public BatchGroupBase {
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
-      if (nf > 0) PN_CUDA(cudaStreamWaitEvent(cap, ev_join, 0));
     } else {
       (void)list; (void)mode; (void)j; (void)sub; (void)part; (void)adj;
     }

@@ -12,10 +12,11 @@
 //     computes the current one from shared memory, where every operand sits at a compile-time
 //     offset; with one, more CTAs fit on an SM and overlap one another.
 //
-// Boxes start at x = x0 - 1 = 32 bx (x0 = 1 + 32 bx is the tile's first cell): 4-float aligned,
-// as tiled TMA requires; cells outside the class grid are zero-filled and never used.  Nothing is
-// stored by TMA: results go to global memory from registers, interior cells only.  Face cells
-// (which compute ghost points) stay with batch_substep_kernel.
+// Boxes start 4-float aligned, as tiled TMA requires: at x0 - 1 = 32 bx for a class odd in x (first
+// cell x0 = 1 + 32 bx), at x0 - 4 for one even in x (x0 = 32 bx; -4 for the first tile, a negative
+// coordinate that loads zeros).  Cells outside the class grid are zero-filled and never used.
+// Nothing is stored by TMA: results go to global memory from registers, target cells only.  The
+// single-axis ghost points the face cells read are written first by batch_ghost2d_kernel.
 //
 // Waits on the mbarrier are bounded (1 s by %globaltimer).  A CTA whose wait runs out records
 // PN_ERR_TIMEOUT in the launch's status word, waits (again bounded) for its copies in flight and
@@ -31,7 +32,7 @@ namespace pn {
 
 constexpr int TX = 32;          // tile width (cells)
 constexpr int TY = BLOCK / TX;  // tile height (rows)
-constexpr int BW = TX + 4;      // box width: x0 - 1 .. x0 + 34 (a multiple of 4 floats)
+constexpr int BW = TX + 8;      // box width from xa = x0 - xo: covers x0 - 1 .. x0 + 32 (a multiple of 4 floats)
 constexpr int PL4 = BW * TY;    // floats per moment plane of a 4-row box
 constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row box (y halo on the side the stencil reads)
 
@@ -52,19 +53,32 @@ struct ArgRow {
 };
 static_assert(MAXE == 4 && MAXR == 8, "ArgRow padding assumes 4 elements and 8 lines");
 
-// One 32 x 4 box tile of a target class (48 bytes).
+// One 32 x 4 tile of a target class (48 bytes).  Tiles cover every target cell: from x = 0 for a
+// class even in x (its box starts at x0 - 4, an aligned negative coordinate for the first tile,
+// read as zeros), from x = 1 for one odd in x (box at x0 - 1).
 struct TTile {
   int inst;     // solve (group order)
   int cls;      // target class (z-even in 2D)
   int x0, y0;   // first cell
-  int ext_x;    // valid cells along x (<= 32)
-  int ext_y;    // valid rows (<= 4)
+  int ext;      // valid cells along x (<= 32) | valid rows (<= 4) << 8 | xo = x0 - box start << 16
   int pslot;    // partial slot of an eee tile, else -1
   int ns;
   int n_ck;
   int ne;
   int arg_fwd;  // index of the solve's first forward ArgRow
   int arg_adj;  // ... adjoint ArgRow
+  int pad_;
+};
+
+// The single-axis ghosts that a sub-step reads: for target class `cls` (even along `axis`) on
+// side `side`, one thread per (transverse position, component) -- ghost_fill's arithmetic,
+// computed before the cells are updated instead of by the face cells themselves.
+struct GFace {
+  int inst, cls, axis, side;
+  int t_lo, t_cnt;   // transverse positions (the other axis): t_lo .. t_lo + t_cnt - 1
+  int thread0;       // first thread of this face in the launch
+  int ns, arg_fwd;
+  int pad_[3];
 };
 
 // tensor maps per (solve, class)
@@ -204,7 +218,7 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   const int ya = tt.y0 - ((c >> 1) & 1);
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
-  const int xa = tt.x0 - 1;
+  const int xa = tt.x0 - (tt.ext >> 16);
   if (ADJ) {
     tma_load_3d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
     if (n_x > 0) tma_load_3d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
@@ -231,7 +245,8 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, c
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
   const ArgRow<N>& ar = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-  const bool valid = tx < tt.ext_x && ty < tt.ext_y;
+  const int xo = tt.ext >> 16;
+  const bool valid = tx < (tt.ext & 255) && ty < ((tt.ext >> 8) & 255);
   const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
   double part[MAXR];
 #pragma unroll
@@ -240,9 +255,9 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, c
     if (valid) {
       const BInst<float>& I = L.inst[tt.inst];
       const int i = tt.x0 + tx, j = tt.y0 + ty;
-      const int lo = ty * BW + tx + 1;
-      const int xr = ty * BW + tx + (oddx ? 1 : 2), xl = xr - 1;
-      const int yr = (ty + 1) * BW + tx + 1, yl = yr - BW;   // rows j (+1) and j - 1 (j) of the y box
+      const int lo = ty * BW + tx + xo;                       // the cell in the own / density boxes
+      const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;         // x neighbours: i, i - 1 (odd) or i + 1, i
+      const int yr = (ty + 1) * BW + tx + xo, yl = yr - BW;    // rows j, j - 1 (odd) or j + 1, j of the y box
       const float ihx = I.inv_h[0], ihy = I.inv_h[1];
       float acc[n];
 #pragma unroll
@@ -415,6 +430,93 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       default: tma_cell<N, 6, ADJ>(L, tt, st, red); break;
     }
     __syncthreads();   // stage s is free for the loads issued in the next iteration
+  }
+}
+
+template <int N>
+struct GLaunch {
+  const BInst<float>* inst;
+  const GFace* faces;
+  const ArgRow<N>* rows;
+  int n_faces, n_threads;
+  int mode, j, sub, K;
+};
+
+template <int N, int C, int D, bool ADJ>
+__device__ __forceinline__ void ghost_one(const GLaunch<N>& L, const GFace& f, int tpos, int r) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nt = Ord<N>::n(C);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nt == 0 || nf == 0) {
+    return;
+  } else {
+    const BInst<float>& I = L.inst[f.inst];
+    float* own;
+    float* from;
+    double bc = 0.0;
+    if (ADJ) {
+      own = from = I.lam;
+    } else {
+      const bool segment = L.mode == BM_RECOMPUTE;
+      const int m = L.j / L.K;
+      float* src = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j + 1, L.K, segment, m) * I.slot_elems;
+      float* dst = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j, L.K, segment, m) * I.slot_elems;
+      own = (L.sub == 3) ? dst : src;
+      from = (L.sub == 1) ? src : dst;
+      bc = L.rows[f.arg_fwd + (f.ns - L.j - 1)].bc;
+    }
+    const Geom& gt = I.g[C];
+    const Geom& gf = I.g[F];
+    const bool left = f.side == 0;
+    int c3[3] = {0, 0, 0};
+    c3[D] = left ? 0 : gt.n[D] - 1;
+    c3[1 - D] = tpos;
+    int cg[3] = {c3[0], c3[1], 0};
+    int ci[3] = {c3[0], c3[1], 0};
+    if (left) {
+      cg[D] = 0;
+      ci[D] = 1;
+    } else {
+      cg[D] = c3[D] + 1;
+      ci[D] = c3[D];
+    }
+    const float* ut = own + I.dev_off[C] + lin(gt, c3[0], c3[1], 0);
+    const double* B = (ADJ ? I.bmat_a[D][F] : I.bmat_f[D][F]) + (long long)r * nt;
+    float bv = 0.0f;
+#pragma unroll
+    for (int q = 0; q < nt; ++q) bv = fmaf(float(B[q]), ut[q * gt.ms], bv);
+    const bool src = !ADJ && D == 0 && !left;
+    const double bc_scaled = bc * I.scale_g;
+    const float gval = src ? float(I.beam[F][((long long)0 * gf.n[1] + c3[1]) * nf + r] * bc_scaled) : 0.0f;
+    const float interior = from[I.dev_off[F] + lin(gf, ci[0], ci[1], 0) + (long long)r * gf.ms];
+    const float gh = left ? 2.0f * (gval - bv) - interior : 2.0f * (bv + gval) - interior;
+    from[I.dev_off[F] + lin(gf, cg[0], cg[1], 0) + (long long)r * gf.ms] = gh;
+  }
+}
+
+template <int N, bool ADJ>
+__global__ void __launch_bounds__(256) batch_ghost2d_kernel(const __grid_constant__ GLaunch<N> L) {
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= L.n_threads) return;
+  int lo = 0, hi = L.n_faces - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (L.faces[mid].thread0 <= gid) lo = mid;
+    else hi = mid - 1;
+  }
+  const GFace f = L.faces[lo];
+  const int nf = class_moments<N>(f.cls ^ (4 >> f.axis));
+  const int rem = gid - f.thread0;
+  const int tpos = f.t_lo + rem / nf, r = rem % nf;
+  switch (f.cls * 2 + f.axis) {
+    case 0: ghost_one<N, 0, 0, ADJ>(L, f, tpos, r); break;
+    case 1: ghost_one<N, 0, 1, ADJ>(L, f, tpos, r); break;
+    case 4: ghost_one<N, 2, 0, ADJ>(L, f, tpos, r); break;
+    case 5: ghost_one<N, 2, 1, ADJ>(L, f, tpos, r); break;
+    case 8: ghost_one<N, 4, 0, ADJ>(L, f, tpos, r); break;
+    case 9: ghost_one<N, 4, 1, ADJ>(L, f, tpos, r); break;
+    case 12: ghost_one<N, 6, 0, ADJ>(L, f, tpos, r); break;
+    default: ghost_one<N, 6, 1, ADJ>(L, f, tpos, r); break;
   }
 }
 

@@ -27,7 +27,7 @@ def mixed_solves(precision):
     return out
 
 
-def run_batch(torch, solves, K=0, flags=0):
+def run_batch(torch, solves, K=0, flags=0, ibar=None):
     descs, keep = [], []
     for s in solves:
         d, k = s.problem.descriptor(s.x_rays)
@@ -43,7 +43,9 @@ def run_batch(torch, solves, K=0, flags=0):
               [t.data_ptr() for t in I])
     torch.cuda.synchronize()
     Ih = [t.cpu().numpy() for t in I]
-    ib = [torch.from_numpy(np.linspace(1.0, 2.0, len(x)) / np.abs(x)).cuda() for x in Ih]
+    if ibar is None:
+        ibar = [np.linspace(1.0, 2.0, len(x)) / np.abs(x) for x in Ih]
+    ib = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in ibar]
     rb = [torch.zeros(x[0].numel(), dtype=torch.float64, device="cuda") for x in ins]
     nb = [torch.zeros(x[1].numel(), dtype=torch.float64, device="cuda") for x in ins]
     ab = [torch.zeros(x[2].numel(), dtype=torch.float64, device="cuda") for x in ins]
@@ -110,14 +112,19 @@ def tma_solves():
 
 
 @pytest.mark.parametrize("K", [1, 3])
-def test_tma_tiles_match_the_generic_kernels_bit_for_bit(gpu_lib, K):
+def test_tma_tiles_match_the_generic_kernels(gpu_lib, K):
+    """Every cell update and ghost point is the same arithmetic on both paths, so states and
+    gradients agree bit for bit; the intensity partial sums group the cells by the path's own
+    tiles, so intensities agree to rounding."""
     torch = pytest.importorskip("torch")
     solves = tma_solves()
-    got = run_batch(torch, solves, K=K)
     ref = run_batch(torch, solves, K=K, flags=capi.PN_BATCH_GENERIC_KERNELS)
+    got = run_batch(torch, solves, K=K, ibar=ref[1])
     assert got[5].tma_groups == got[5].n_groups == 4
     assert ref[5].tma_groups == 0
-    for a, b in zip(got[:5], ref[:5]):
+    for x, y in zip(got[0], ref[0]):
+        assert rel(x, y) < 1e-13
+    for a, b in zip(got[1:5], ref[1:5]):
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
 
