@@ -573,11 +573,13 @@ class BatchGroup : public BatchGroupBase {
   // FP32 2D: box tiles through the TMA kernel, face tiles through the generic one
   bool use_tma = false;
   std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
-  std::vector<TTile> ttl[2];
-  std::vector<GFace> gfl[2];
-  std::vector<int> tend[2], gend[2], gthr[2];   // per solve: tile / face / ghost-thread prefix ends
-  TTile* dttl[2] = {nullptr, nullptr};
-  GFace* dgfl[2] = {nullptr, nullptr};
+  std::vector<TTile> ttl[3];     // per list: 0 / 1 parity targets, 2 every class (density integral)
+  std::vector<GFace> gfl[3];
+  std::vector<int> tend[3], gend[3], gthr[3];   // per solve: tile / face / ghost-thread prefix ends
+  TTile* dttl[3] = {nullptr, nullptr, nullptr};
+  GFace* dgfl[3] = {nullptr, nullptr, nullptr};
+  void* dirows = nullptr;
+  int tma_int_grid = 0;
   CUtensorMap* dmaps = nullptr;
   void* drows = nullptr;
   int* dstatus = nullptr;
@@ -769,6 +771,12 @@ class BatchGroup : public BatchGroupBase {
       if (LY::SMEM + 2048 > smem_optin) return PN_OK;
       PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
       PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
+      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_int_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   TmaIntLayout<N>::SMEM));
+      int occ_i = 0;
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_i, batch_tma2d_int_kernel<N>, BLOCK, TmaIntLayout<N>::SMEM));
+      if (occ_i < 1) return PN_OK;
+      tma_int_grid = occ_i * sms;
       int occ_f = 0, occ_a = 0;
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma2d_kernel<N, false>, BLOCK, LY::SMEM));
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma2d_kernel<N, true>, BLOCK, LY::SMEM));
@@ -803,6 +811,30 @@ class BatchGroup : public BatchGroupBase {
       int rc;
       if ((rc = upload(dr, rows))) return rc;
       drows = dr;
+      // density-integral rows: iterations 0 .. n_steps per solve
+      std::vector<IntRow<N>> irows;
+      std::vector<int> arg_int(n);
+      for (int q = 0; q < n; ++q) {
+        const pn_desc* d = cur_descs[q];
+        const int ns = hinst[q].ns, ne = hinst[q].ne, nr = hinst[q].nr;
+        arg_int[q] = (int)irows.size();
+        for (int it = 0; it <= ns; ++it) {
+          IntRow<N> a;
+          std::memset(&a, 0, sizeof(a));
+          for (int e = 0; e < ne; ++e) {
+            a.s[e] = float(d->adj_int_s[(long long)it * ne + e]);
+            for (int l = 0; l <= N; ++l) a.c[e][l] = float(d->adj_int_c[((long long)it * ne + e) * (N + 1) + l]);
+          }
+          for (int r = 0; r < nr; ++r)
+            a.coef[r] = d->delta_e * d->dvol * d->adj_sigma[(long long)it * nr + r] * d->adj_weight[it];
+          a.wfac = d->dvol * d->delta_e * d->adj_weight[it];
+          a.bc = d->adj_int_bc[it];
+          irows.push_back(a);
+        }
+      }
+      IntRow<N>* dir = nullptr;
+      if ((rc = upload(dir, irows))) return rc;
+      dirows = dir;
       // tensor maps
       std::vector<CUtensorMap> maps((size_t)n * 8 * TM_KINDS);
       std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
@@ -839,7 +871,7 @@ class BatchGroup : public BatchGroupBase {
         hinst[q].ptile0 = 0;
         hinst[q].n_ptile = 0;
       }
-      for (int list = 0; list < 2; ++list) {
+      for (int list = 0; list < 3; ++list) {
         tend[list].assign(n, 0);
         gend[list].assign(n, 0);
         gthr[list].assign(n, 0);
@@ -848,7 +880,7 @@ class BatchGroup : public BatchGroupBase {
           const BInst<T>& I = hinst[q];
           if (list == 0) hinst[q].ptile0 = n_ptiles;
           for (int c = 0; c < 8; ++c) {
-            if (!I.active[c] || class_parity(c) != list || class_moments_host(c) == 0) continue;
+            if (!I.active[c] || (list < 2 && class_parity(c) != list) || class_moments_host(c) == 0) continue;
             int lo3[2], hi3[2];
             for (int k = 0; k < 2; ++k) {
               const int nn = I.shape[c][k];
@@ -871,6 +903,7 @@ class BatchGroup : public BatchGroupBase {
                 tt.ne = I.ne;
                 tt.arg_fwd = arg_fwd[q];
                 tt.arg_adj = arg_adj[q];
+                tt.arg_int = arg_int[q];
                 ttl[list].push_back(tt);
               }
             // ghosts read by the class's face cells along each axis where it is even
@@ -891,6 +924,7 @@ class BatchGroup : public BatchGroupBase {
                 f.thread0 = threads;
                 f.ns = I.ns;
                 f.arg_fwd = arg_fwd[q];
+                f.arg_int = arg_int[q];
                 threads += f.t_cnt * nf;
                 gfl[list].push_back(f);
               }
@@ -1144,7 +1178,7 @@ class BatchGroup : public BatchGroupBase {
   // --------------------------------------------------------------------------------------------
   int launch(int list, int mode, int j, int sub, double* part, bool adj, bool integ) {
     if constexpr (std::is_same<T, float>::value && DIMS == 3) {
-      if (use_tma && !integ) return launch_tma(list, mode, j, sub, part, adj);
+      if (use_tma) return integ ? launch_tma_int(j) : launch_tma(list, mode, j, sub, part, adj);
     }
     const int x = integ ? j - 1 : j;   // integrate at iteration j includes the solves with ns == j
     const int nt = tiles_active(integ ? 2 : list, x);
@@ -1186,6 +1220,7 @@ class BatchGroup : public BatchGroupBase {
         g.inst = dinst;
         g.faces = dgfl[list];
         g.rows = static_cast<const ArgRow<N>*>(drows);
+        g.irows = static_cast<const IntRow<N>*>(dirows);
         g.n_faces = gend[list][last];
         g.n_threads = nthr;
         g.mode = mode;
@@ -1193,9 +1228,9 @@ class BatchGroup : public BatchGroupBase {
         g.sub = sub;
         g.K = K;
         if (adj)
-          batch_ghost2d_kernel<N, true><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
+          batch_ghost2d_kernel<N, GK_ADJ><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
         else
-          batch_ghost2d_kernel<N, false><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
+          batch_ghost2d_kernel<N, GK_FWD><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
@@ -1224,6 +1259,51 @@ class BatchGroup : public BatchGroupBase {
       }
     } else {
       (void)list; (void)mode; (void)j; (void)sub; (void)part; (void)adj;
+    }
+    return PN_OK;
+  }
+
+  // TMA path of the density integral at iteration j: ghosts of the tape state, then every cell
+  int launch_tma_int(int j) {
+    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+      int last = -1;
+      for (int q = 0; q < n; ++q)
+        if (hinst[q].ns >= j) last = q;   // the integral at iteration j includes solves with ns == j
+      if (last < 0) return PN_OK;
+      const int nthr = gthr[2][last];
+      if (nthr > 0) {
+        GLaunch<N> g;
+        g.inst = dinst;
+        g.faces = dgfl[2];
+        g.rows = static_cast<const ArgRow<N>*>(drows);
+        g.irows = static_cast<const IntRow<N>*>(dirows);
+        g.n_faces = gend[2][last];
+        g.n_threads = nthr;
+        g.mode = BM_ADJOINT;
+        g.j = j;
+        g.sub = 0;
+        g.K = K;
+        batch_ghost2d_kernel<N, GK_INT><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
+        PN_CUDA(cudaGetLastError());
+        ++nl;
+      }
+      const int nb = tend[2][last];
+      if (nb > 0) {
+        TILaunch<N> a;
+        a.inst = dinst;
+        a.tiles = dttl[2];
+        a.maps = dmaps;
+        a.rows = static_cast<const IntRow<N>*>(dirows);
+        a.status = dstatus;
+        a.n_tiles = nb;
+        a.it = j;
+        a.K = K;
+        batch_tma2d_int_kernel<N><<<std::min(nb, tma_int_grid), BLOCK, TmaIntLayout<N>::SMEM, cap>>>(a);
+        PN_CUDA(cudaGetLastError());
+        ++nl;
+      }
+    } else {
+      (void)j;
     }
     return PN_OK;
   }

@@ -53,6 +53,16 @@ struct ArgRow {
 };
 static_assert(MAXE == 4 && MAXR == 8, "ArgRow padding assumes 4 elements and 8 lines");
 
+// Coefficients of one adjoint iteration's density integral (fill_int's fields; 16-byte multiple).
+template <int N>
+struct IntRow {
+  float s[MAXE];
+  float c[MAXE][N + 1];
+  double coef[MAXR];
+  double wfac;
+  double bc;
+};
+
 // One 32 x 4 tile of a target class (48 bytes).  Tiles cover every target cell: from x = 0 for a
 // class even in x (its box starts at x0 - 4, an aligned negative coordinate for the first tile,
 // read as zeros), from x = 1 for one odd in x (box at x0 - 1).
@@ -67,7 +77,7 @@ struct TTile {
   int ne;
   int arg_fwd;  // index of the solve's first forward ArgRow
   int arg_adj;  // ... adjoint ArgRow
-  int pad_;
+  int arg_int;  // ... IntRow (n_steps + 1 rows)
 };
 
 // The single-axis ghosts that a sub-step reads: for target class `cls` (even along `axis`) on
@@ -77,8 +87,8 @@ struct GFace {
   int inst, cls, axis, side;
   int t_lo, t_cnt;   // transverse positions (the other axis): t_lo .. t_lo + t_cnt - 1
   int thread0;       // first thread of this face in the launch
-  int ns, arg_fwd;
-  int pad_[3];
+  int ns, arg_fwd, arg_int;
+  int pad_[2];
 };
 
 // tensor maps per (solve, class)
@@ -433,17 +443,226 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// density integral of the adjoint (integrate_cell's arithmetic), every class of a 2D solve
+// ---------------------------------------------------------------------------------------------
+template <int N>
+struct TILaunch {
+  const BInst<float>* inst;
+  const TTile* tiles;
+  const CUtensorMap* maps;
+  const IntRow<N>* rows;
+  int* status;
+  int n_tiles;
+  int it;   // adjoint iteration (tape state it)
+  int K;
+};
+
+template <int N>
+struct TmaIntLayout {
+  using B = TmaLayout<N>;
+  static constexpr int OWN = 0;
+  static constexpr int LAM = OWN + B::al(B::NO * PL4 * 4);
+  static constexpr int XN = LAM + B::al(B::NO * PL4 * 4);
+  static constexpr int YN = XN + B::al(B::NXN * PL4 * 4);
+  static constexpr int RHO = YN + B::al(B::NYN * PL5 * 4);
+  static constexpr int ARG = RHO + B::al(MAXE * PL4 * 4);
+  static constexpr int STAGE = ARG + B::al((int)sizeof(IntRow<N>));
+  static constexpr int SMEM = TSTAGES * STAGE;
+};
+
+template <int N>
+__device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile& tt, unsigned char* st,
+                                              unsigned long long* bar) {
+  using LY = TmaIntLayout<N>;
+  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
+  const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
+  const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
+  const unsigned bytes =
+      4u * (unsigned)(2 * PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) + (unsigned)sizeof(IntRow<N>);
+  const int ya = tt.y0 - ((c >> 1) & 1);
+  mbar_expect_tx(bar, bytes);
+  const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
+  const int xa = tt.x0 - (tt.ext >> 16);
+  tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST4, xa, tt.y0, 0, slot, bar);
+  tma_load_3d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
+  if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST4, xa, tt.y0, 0, slot, bar);
+  if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST5, xa, ya, 0, slot, bar);
+  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
+  bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
+}
+
+template <int N, int C>
+__device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& tt, const unsigned char* st) {
+  using LY = TmaIntLayout<N>;
+  constexpr int n = Ord<N>::n(C);
+  constexpr bool oddx = (C >> 2) & 1;
+  if constexpr (n > 0) {
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int xo = tt.ext >> 16;
+    if (!(tx < (tt.ext & 255) && ty < ((tt.ext >> 8) & 255))) return;
+    const float* own = reinterpret_cast<const float*>(st + LY::OWN);
+    const float* lam = reinterpret_cast<const float*>(st + LY::LAM);
+    const float* xn = reinterpret_cast<const float*>(st + LY::XN);
+    const float* yn = reinterpret_cast<const float*>(st + LY::YN);
+    const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
+    const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
+    const BInst<float>& I = L.inst[tt.inst];
+    const int i = tt.x0 + tx, j = tt.y0 + ty;
+    const int lo = ty * BW + tx + xo;
+    const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;
+    const int yr = (ty + 1) * BW + tx + xo, yl = yr - BW;
+    const float ihx = I.inv_h[0], ihy = I.inv_h[1];
+    float acc[n];
+#pragma unroll
+    for (int m = 0; m < n; ++m) acc[m] = 0.0f;
+    {
+      constexpr int F = C ^ 4;
+      if constexpr (Ord<N>::n(F) > 0) {
+        auto diff = [&](int q) -> float { return (xn[q * PL4 + xr] - xn[q * PL4 + xl]) * ihx; };
+        auto coef = [&](int kk, double lit) -> float {
+          (void)kk;
+          return float(lit);
+        };
+        Adv<N, C, 0>::template apply<float>(acc, diff, coef);
+      }
+    }
+    {
+      constexpr int F = C ^ 2;
+      if constexpr (Ord<N>::n(F) > 0) {
+        auto diff = [&](int q) -> float { return (yn[q * PL5 + yr] - yn[q * PL5 + yl]) * ihy; };
+        auto coef = [&](int kk, double lit) -> float {
+          (void)kk;
+          return float(lit);
+        };
+        Adv<N, C, 1>::template apply<float>(acc, diff, coef);
+      }
+    }
+    float rr[MAXE];
+    float S = 0.0f;
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+      rr[e] = e < tt.ne ? rh[e * PL4 + lo] : 0.0f;
+      S = fmaf(rr[e], ar.s[e], S);
+    }
+    const float invS = recip(S);
+    constexpr unsigned mask = Ord<N>::deg_mask(C);
+    float Cl[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) {
+      float cc = 0.0f;
+      if ((mask >> l) & 1u) {
+#pragma unroll
+        for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
+      }
+      Cl[l] = cc;
+    }
+    float P = 0.0f;
+    float R[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) R[l] = 0.0f;
+#pragma unroll
+    for (int m = 0; m < n; ++m) {
+      const int l = degree_of<N, C>(m);
+      const float u = own[m * PL4 + lo];
+      const float lm = lam[m * PL4 + lo];
+      const float du = (-acc[m] - Cl[l] * u) * invS;
+      P = fmaf(lm, du, P);
+      R[l] = fmaf(lm, u, R[l]);
+    }
+    const Geom& gt = I.g[C];
+    double* rb = I.rbar[C] + lin(gt, i, j, 0);
+#pragma unroll
+    for (int e = 0; e < MAXE; ++e) {
+      if (e < tt.ne) {
+        double v = double(ar.s[e]) * double(P);
+#pragma unroll
+        for (int l = 0; l <= N; ++l)
+          if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
+        rb[e * gt.ms] += v * ar.wfac;
+      }
+    }
+    if constexpr (C == 0) {
+      const long long ce = eee_cell(gt, i, j, 0);
+      const double u0 = double(own[lo]);
+      for (int r = 0; r < I.nr; ++r) {
+        const double cr = ar.coef[r] * I.ibar[r];
+        const int el = I.xel[r];
+        I.acs_bar[ce * I.nr + r] += I.noa[ce * I.ne + el] * u0 * cr;
+        I.noa_bar[ce * I.ne + el] += I.acs[ce * I.nr + r] * u0 * cr;
+      }
+    }
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_constant__ TILaunch<N> L) {
+  using LY = TmaIntLayout<N>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long full[TSTAGES];
+  if ((smem_u32(smem) & 127u) != 0u) {
+    if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TSTAGES; ++s) mbar_init(&full[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int G = gridDim.x;
+  const int t0 = blockIdx.x;
+  if (threadIdx.x == 0)
+    for (int k = 0; k < TSTAGES - 1; ++k) {
+      const int t = t0 + k * G;
+      if (t < L.n_tiles) tma_issue_int<N>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
+    }
+  for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
+    const int t = t0 + k * G;
+    const int s = k % TSTAGES;
+    const int ka = k + TSTAGES - 1;
+    const int ta = t0 + ka * G;
+    if (ta < L.n_tiles && threadIdx.x == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tma_issue_int<N>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
+    }
+    const TTile tt = L.tiles[t];
+    const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(L.status, (int)PN_ERR_TIMEOUT);
+        for (int kk = k; kk <= ka; ++kk)
+          if (t0 + kk * G < L.n_tiles) mbar_wait_bounded(&full[kk % TSTAGES], (unsigned)((kk / TSTAGES) & 1));
+      }
+      __syncthreads();
+      return;
+    }
+    const unsigned char* st = smem + s * LY::STAGE;
+    switch (tt.cls) {
+      case 0: tma_int_cell<N, 0>(L, tt, st); break;
+      case 2: tma_int_cell<N, 2>(L, tt, st); break;
+      case 4: tma_int_cell<N, 4>(L, tt, st); break;
+      default: tma_int_cell<N, 6>(L, tt, st); break;
+    }
+    __syncthreads();
+  }
+}
+
+// ghost kernel modes: sub-step of the forward (or recompute) march, of the adjoint, density integral
+enum { GK_FWD = 0, GK_ADJ = 1, GK_INT = 2 };
+
 template <int N>
 struct GLaunch {
   const BInst<float>* inst;
   const GFace* faces;
   const ArgRow<N>* rows;
+  const IntRow<N>* irows;
   int n_faces, n_threads;
   int mode, j, sub, K;
 };
 
-template <int N, int C, int D, bool ADJ>
+template <int N, int C, int D, int KIND>
 __device__ __forceinline__ void ghost_one(const GLaunch<N>& L, const GFace& f, int tpos, int r) {
+  constexpr bool ADJ = KIND == GK_ADJ;
   constexpr int F = C ^ (4 >> D);
   constexpr int nt = Ord<N>::n(C);
   constexpr int nf = Ord<N>::n(F);
@@ -454,8 +673,12 @@ __device__ __forceinline__ void ghost_one(const GLaunch<N>& L, const GFace& f, i
     float* own;
     float* from;
     double bc = 0.0;
-    if (ADJ) {
+    if (KIND == GK_ADJ) {
       own = from = I.lam;
+    } else if (KIND == GK_INT) {
+      // the tape state of iteration j, forward boundary blocks, beam source of the iteration
+      own = from = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j, L.K, true, L.j / L.K) * I.slot_elems;
+      bc = L.irows[f.arg_int + L.j].bc;
     } else {
       const bool segment = L.mode == BM_RECOMPUTE;
       const int m = L.j / L.K;
@@ -494,7 +717,7 @@ __device__ __forceinline__ void ghost_one(const GLaunch<N>& L, const GFace& f, i
   }
 }
 
-template <int N, bool ADJ>
+template <int N, int KIND>
 __global__ void __launch_bounds__(256) batch_ghost2d_kernel(const __grid_constant__ GLaunch<N> L) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   if (gid >= L.n_threads) return;
@@ -509,14 +732,14 @@ __global__ void __launch_bounds__(256) batch_ghost2d_kernel(const __grid_constan
   const int rem = gid - f.thread0;
   const int tpos = f.t_lo + rem / nf, r = rem % nf;
   switch (f.cls * 2 + f.axis) {
-    case 0: ghost_one<N, 0, 0, ADJ>(L, f, tpos, r); break;
-    case 1: ghost_one<N, 0, 1, ADJ>(L, f, tpos, r); break;
-    case 4: ghost_one<N, 2, 0, ADJ>(L, f, tpos, r); break;
-    case 5: ghost_one<N, 2, 1, ADJ>(L, f, tpos, r); break;
-    case 8: ghost_one<N, 4, 0, ADJ>(L, f, tpos, r); break;
-    case 9: ghost_one<N, 4, 1, ADJ>(L, f, tpos, r); break;
-    case 12: ghost_one<N, 6, 0, ADJ>(L, f, tpos, r); break;
-    default: ghost_one<N, 6, 1, ADJ>(L, f, tpos, r); break;
+    case 0: ghost_one<N, 0, 0, KIND>(L, f, tpos, r); break;
+    case 1: ghost_one<N, 0, 1, KIND>(L, f, tpos, r); break;
+    case 4: ghost_one<N, 2, 0, KIND>(L, f, tpos, r); break;
+    case 5: ghost_one<N, 2, 1, KIND>(L, f, tpos, r); break;
+    case 8: ghost_one<N, 4, 0, KIND>(L, f, tpos, r); break;
+    case 9: ghost_one<N, 4, 1, KIND>(L, f, tpos, r); break;
+    case 12: ghost_one<N, 6, 0, KIND>(L, f, tpos, r); break;
+    default: ghost_one<N, 6, 1, KIND>(L, f, tpos, r); break;
   }
 }
 
