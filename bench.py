@@ -54,6 +54,15 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--config4", action="store_true",
+                    help="3D 96x96x64 P7 forward+adjoint (FP32 batch, checkpoint stride 16) with a central "
+                         "finite-difference check of the mass-fraction gradient on 32 cells; prints its own line")
+    ap.add_argument("--fd-cells", type=int, default=32)
+    ap.add_argument("--config1", action="store_true",
+                    help="1D slab (config 1): FP64 plain latency, FP32 batch of 256 compositions, gradient vs "
+                         "finite differences of the oracle on all 200 cells; prints its own line")
+    ap.add_argument("--config3", action="store_true",
+                    help="256 mixed 2D instances (config 3) in one FP32 batch, errors against FP64; prints its own line")
     return ap.parse_args()
 
 
@@ -410,6 +419,7 @@ def run_ours(args):
     except Exception:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_source = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
     traffic = None
     try:
         prof = json.load(open(os.path.join(HERE, "profiles", "substep_fp64_traffic.json")))
@@ -446,9 +456,11 @@ def run_ours(args):
                              "forward_ms": float(np.mean(b_fwd)),
                              "max_rel_err_intensity_vs_fp64": k_err, "max_rel_err_rho_bar_vs_fp64": g_err,
                              "checkpoint_stride": binfo.checkpoint_stride,
-                             "forward_roofline": {"bound": "hbm", "achieved": fp32_fwd_gbs,
-                                                  "peak": float(json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))).get("hbm_gbs", 6800.0)) if os.path.exists(os.path.join(HERE, "MEASURED_PEAKS.json")) else 6800.0,
-                                                  "unit": "GB/s",
+                             "tma_groups": binfo.tma_groups,
+                             "forward_roofline": {"bound": "hbm", "achieved": fp32_fwd_gbs, "peak": peak,
+                                                  "unit": "GB/s", "frac": fp32_fwd_gbs / peak,
+                                                  "peak_source": peak_source,
+                                                  "kernel": "batch_tma2d_kernel<11> (with its ghost kernels), forward sweep",
                                                   "note": "algorithmic bytes of all forward sub-steps of the 60 solves / forward time"},
                              "kernels_per_step": binfo.forward_kernels + binfo.adjoint_kernels,
                              "form": "one pn_batch: one launch per sub-step covers all 60 solves"},
@@ -692,6 +704,343 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------------------------------------
+def material_gradient(s, rho_bar, noa_bar, acs_bar, acs):
+    """d J / d(mass fractions) from the solver's adjoint outputs (the material pullbacks of
+    pn_intensities.jl:406-409, on the host)."""
+    m = s.material
+    g = m.grid_pullback(rho_bar)
+    g = g + m.noa_pullback(noa_bar.reshape(m.values.shape[:-1] + (m.n_e,)))
+    g = g + m.absorption_pullback(s.x_rays, s.detector, s.problem.beam_position.mean, acs, acs_bar)[0]
+    return g
+
+
+def run_config4(args):
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.material import BoxPerturbation
+    from pnepma_gb300.problem import PN_FP32, PN_FP64
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    t0 = time.perf_counter()
+    s = workloads.config4(precision=PN_FP32)
+    rho, noa, acs = s.inputs()
+    prep_s = time.perf_counter() - t0
+    nr = len(s.x_rays)
+    m = s.material
+    # FP64 plain: intensities, the cotangent of J = sum_r I_r / I_r(FP64), and the gradient
+    s.problem.precision = PN_FP64
+    d64, k64 = s.problem.descriptor(s.x_rays)
+    h64 = capi.Handle(d64, k64)
+    I64 = h64.forward(rho, noa, acs)
+    ib = 1.0 / np.abs(I64)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    sp = torch.cuda.Stream(device=dev)
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    x_rho, x_noa, x_acs, x_ib = dv(rho), dv(noa), dv(acs), dv(ib)
+    sz = h64.sizes
+    o_I = torch.zeros(nr, dtype=torch.float64, device=dev)
+    o_rb = torch.zeros(sz.n_rho, dtype=torch.float64, device=dev)
+    o_nb = torch.zeros(sz.n_noa, dtype=torch.float64, device=dev)
+    o_ab = torch.zeros(sz.n_acs, dtype=torch.float64, device=dev)
+    with torch.cuda.stream(sp):
+        ev[0].record(sp)
+        h64.forward_device(x_rho.data_ptr(), x_noa.data_ptr(), x_acs.data_ptr(), o_I.data_ptr(), sp.cuda_stream)
+        ev[1].record(sp)
+        h64.adjoint_device(x_ib.data_ptr(), o_rb.data_ptr(), o_nb.data_ptr(), o_ab.data_ptr(), sp.cuda_stream)
+        ev[2].record(sp)
+    sp.synchronize()
+    fp64_fwd_ms, fp64_adj_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    rb64, nb64, ab64 = o_rb.cpu().numpy(), o_nb.cpu().numpy(), o_ab.cpu().numpy()
+    # FP32 batch of the one solve, checkpoint stride 16
+    s.problem.precision = PN_FP32
+    d32, k32 = s.problem.descriptor(s.x_rays)
+    b = capi.Batch([d32], [k32], checkpoint_stride=16)
+    I32 = torch.zeros(nr, dtype=torch.float64, device=dev)
+    rb = torch.zeros(sz.n_rho, dtype=torch.float64, device=dev)
+    nb = torch.zeros(sz.n_noa, dtype=torch.float64, device=dev)
+    ab = torch.zeros(sz.n_acs, dtype=torch.float64, device=dev)
+    fw, ad = [], []
+    for rep in range(1 + max(1, args.steps)):
+        with torch.cuda.stream(sp):
+            ev[0].record(sp)
+            b.forward([x_rho.data_ptr()], [x_noa.data_ptr()], [x_acs.data_ptr()], [I32.data_ptr()], sp.cuda_stream)
+            ev[1].record(sp)
+            b.adjoint([x_ib.data_ptr()], [rb.data_ptr()], [nb.data_ptr()], [ab.data_ptr()], sp.cuda_stream)
+            ev[2].record(sp)
+        sp.synchronize()
+        if rep > 0:
+            fw.append(ev[0].elapsed_time(ev[1]))
+            ad.append(ev[1].elapsed_time(ev[2]))
+    binfo = b.info()
+    rb32, nb32, ab32 = rb.cpu().numpy(), nb.cpu().numpy(), ab.cpu().numpy()
+    I32h = I32.cpu().numpy()
+    # gradients with respect to the per-cell mass fractions
+    g64 = material_gradient(s, rb64, nb64, ab64, acs)
+    g32 = material_gradient(s, rb32, nb32, ab32, acs)
+    # cells: 3/4 drawn from the entries carrying the top tenth of |g|, 1/4 uniformly
+    rng = np.random.default_rng(44)
+    flat = np.abs(g64).ravel()
+    top = np.nonzero(flat >= np.quantile(flat, 0.9))[0]
+    n_top = (3 * args.fd_cells) // 4
+    pick = list(rng.choice(top, n_top, replace=False)) + list(rng.choice(flat.size, args.fd_cells - n_top, replace=False))
+    entries = [np.unravel_index(int(q), g64.shape) for q in pick]
+    boxes = sorted(set(e[:3] for e in entries))
+    t1 = time.perf_counter()
+    bp = BoxPerturbation(m, s.x_rays, s.detector, s.problem.beam_position.mean, boxes, (rho, noa, acs))
+    bp_s = time.perf_counter() - t1
+    hstep = 1e-6
+    fd, t_fd = [], time.perf_counter()
+    for e in entries:
+        delta = np.zeros(m.n_par)
+        delta[e[3]] = hstep
+        Jp = float(ib @ h64.forward(*bp.inputs(e[:3], delta)))
+        Jm = float(ib @ h64.forward(*bp.inputs(e[:3], -delta)))
+        fd.append((Jp - Jm) / (2 * hstep))
+    t_fd = time.perf_counter() - t_fd
+    fd = np.array(fd)
+    a64 = np.array([g64[e] for e in entries])
+    a32 = np.array([g32[e] for e in entries])
+    scale = float(np.max(np.abs(g64)))
+    top_idx = np.arange(n_top)
+    rel64 = np.abs(a64[top_idx] - fd[top_idx]) / np.abs(fd[top_idx])
+    rel32 = np.abs(a32[top_idx] - fd[top_idx]) / np.abs(fd[top_idx])
+    fwd_bytes, m_active = algorithmic_bytes_per_step(s, 4)
+    ns = s.problem.N_steps
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    fwd_ms = float(np.mean(fw))
+    line = {
+        "metric": "3D forward+adjoint solve (config 4) with a finite-difference gradient check",
+        "value": 1e3 / (fwd_ms + float(np.mean(ad))), "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32 state and stencil, f64 accumulators", "data": "synthetic (seeded)",
+        "config": {"workload": "3D 96x96 (lateral) x 64 (depth) over 1.5 x 1.5 x 1 um, P7, Fe/Cr/Ni smooth field "
+                               "with a 0.2 um spherical inclusion, 20 keV", "energy_steps": ns,
+                   "configured_energy_steps": 300, "checkpoint_stride": binfo.checkpoint_stride,
+                   "state_mb_fp32": sz.n_state * 4 / 1e6, "host_prep_s": prep_s},
+        "fp32_batch": {"forward_ms": fwd_ms, "adjoint_ms": float(np.mean(ad)), "device_bytes": binfo.device_bytes,
+                       "forward_roofline": {"bound": "hbm", "achieved": fwd_bytes * ns / (fwd_ms / 1e3) / 1e9,
+                                            "peak": peak, "unit": "GB/s",
+                                            "frac": fwd_bytes * ns / (fwd_ms / 1e3) / 1e9 / peak,
+                                            "kernel": "batch_substep_kernel<float,7,*,7> (generic 3D), forward sweep"},
+                       "moment_cell_updates_per_s": 2 * ns * m_active / ((fwd_ms + float(np.mean(ad))) / 1e3)},
+        "fp64_plain": {"forward_ms": fp64_fwd_ms, "adjoint_ms": fp64_adj_ms},
+        "fp32_vs_fp64": {"max_rel_err_intensity": float(np.max(np.abs(I32h - I64) / np.abs(I64))),
+                         "gradient_rel_err_normwise": float(np.max(np.abs(g32 - g64)) / scale)},
+        "fd_check": {"cells": len(entries), "h": hstep, "functional": "sum_r I_r / I_r(FP64)",
+                     "cells_from_top_decile_of_abs_gradient": n_top,
+                     "fp64_adjoint_vs_fd": {"max_rel_err_top": float(np.max(rel64)),
+                                            "median_rel_err_top": float(np.median(rel64)),
+                                            "max_abs_err_over_max_abs_gradient": float(np.max(np.abs(a64 - fd)) / scale)},
+                     "fp32_adjoint_vs_fd": {"max_rel_err_top": float(np.max(rel32)),
+                                            "median_rel_err_top": float(np.median(rel32)),
+                                            "max_abs_err_over_max_abs_gradient": float(np.max(np.abs(a32 - fd)) / scale)},
+                     "forward_solves": 2 * len(entries), "seconds": t_fd, "perturbation_setup_s": bp_s,
+                     "note": "the reference's adjoint is continuous-style, so agreement is at discretisation level"},
+    }
+    print(json.dumps(line), flush=True)
+    h64.close()
+    b.close()
+
+
+# ------------------------------------------------------------------------------------------------
+def _batch_run(torch, descs, keep, inputs, ibars, K=0, reps=2):
+    """Forward + adjoint of one pn_batch over device copies of the inputs; returns timings and outputs."""
+    from pnepma_gb300 import capi
+    dev = torch.device("cuda", 0)
+    b = capi.Batch(descs, keep, checkpoint_stride=K)
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    cache = {}
+
+    def dcopy(a):
+        if id(a) not in cache:
+            cache[id(a)] = dv(a)
+        return cache[id(a)]
+
+    x = [[dcopy(a) for a in inp] for inp in inputs]
+    ib = [dv(v) for v in ibars]
+    I = [torch.zeros(d.n_xrays, dtype=torch.float64, device=dev) for d in descs]
+    sizes = [capi.query_sizes(d) for d in descs]
+    rb = [torch.zeros(z.n_rho, dtype=torch.float64, device=dev) for z in sizes]
+    nb = [torch.zeros(z.n_noa, dtype=torch.float64, device=dev) for z in sizes]
+    ab = [torch.zeros(max(z.n_acs, 1), dtype=torch.float64, device=dev) for z in sizes]
+    sp = torch.cuda.Stream(device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fw, ad = [], []
+    for rep in range(reps + 1):
+        with torch.cuda.stream(sp):
+            ev[0].record(sp)
+            b.forward([q[0].data_ptr() for q in x], [q[1].data_ptr() for q in x], [q[2].data_ptr() for q in x],
+                      [t.data_ptr() for t in I], sp.cuda_stream)
+            ev[1].record(sp)
+            b.adjoint([t.data_ptr() for t in ib], [t.data_ptr() for t in rb], [t.data_ptr() for t in nb],
+                      [t.data_ptr() for t in ab], sp.cuda_stream)
+            ev[2].record(sp)
+        sp.synchronize()
+        if rep > 0:
+            fw.append(ev[0].elapsed_time(ev[1]))
+            ad.append(ev[1].elapsed_time(ev[2]))
+    info = b.info()
+    out = ([t.cpu().numpy() for t in I], [t.cpu().numpy() for t in rb], [t.cpu().numpy() for t in nb],
+           [t.cpu().numpy() for t in ab])
+    b.close()
+    return float(np.mean(fw)), float(np.mean(ad)), info, out
+
+
+def _rel(a, b):
+    a = np.asarray(a, float).ravel()
+    b = np.asarray(b, float).ravel()
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def run_config1(args):
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.problem import PN_FP32, PN_FP64
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    torch.cuda.set_device(0)
+    s = workloads.config1(precision=PN_FP64)
+    rho, noa, acs = s.inputs()
+    d64, k64 = s.problem.descriptor(s.x_rays)
+    h = capi.Handle(d64, k64)
+    I64 = h.forward(rho, noa, acs)
+    ib = 1.0 / np.abs(I64)
+    rb64, nb64, ab64 = h.adjoint(ib)
+    lat = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        h.forward(rho, noa, acs)
+        h.adjoint(ib)
+        lat.append((time.perf_counter() - t0) * 1e3)
+    # parity with the oracle and the gradient against its finite differences (all 200 cells)
+    I_o, rb_o, nb_o, ab_o = oracle.adjoint(d64, rho, noa, acs, ib)
+    g64 = material_gradient(s, rb64, nb64, ab64, acs)
+    m = s.material
+    hstep = 1e-6
+    vals = m.values.reshape(-1)
+    fd = np.zeros_like(vals)
+    from pnepma_gb300.material import BoxedMassFraction
+    for q in range(vals.size):
+        out = []
+        for sgn in (1.0, -1.0):
+            v = vals.copy()
+            v[q] += sgn * hstep
+            m2 = BoxedMassFraction(m.elements, m.gspec, v.reshape(m.values.shape), sc=m.sc)
+            r2 = m2.rho_flat()
+            n2 = m2.number_of_atoms().reshape(-1, m.n_e)
+            a2 = m2.absorption(s.x_rays, s.detector, s.problem.beam_position.mean).reshape(acs.shape)
+            out.append(float(ib @ oracle.forward(d64, r2, n2, a2)))
+        fd[q] = (out[0] - out[1]) / (2 * hstep)
+    g = g64.reshape(-1)
+    big = np.abs(fd) >= 1e-3 * np.max(np.abs(fd))
+    # FP32 batch of 256 compositions (the layer fractions redrawn per instance)
+    solves = [workloads.config1(seed=100 + i, precision=PN_FP32) for i in range(256)]
+    descs, keep, inputs, ibars = [], [], [], []
+    for q in solves:
+        dq, kq = q.problem.descriptor(q.x_rays)
+        descs.append(dq)
+        keep.append(kq)
+        inputs.append(q.inputs())
+        ibars.append(ib)
+    fw, ad, info, out = _batch_run(torch, descs, keep, inputs, ibars)
+    # FP32 errors against FP64 on the first 8 instances
+    e_I, e_g = 0.0, 0.0
+    for i in range(8):
+        q = solves[i]
+        q.problem.precision = PN_FP64
+        dq, kq = q.problem.descriptor(q.x_rays)
+        hq = capi.Handle(dq, kq)
+        Iq = hq.forward(*inputs[i])
+        rq, _, _ = hq.adjoint(ib)
+        e_I = max(e_I, _rel(out[0][i], Iq))
+        e_g = max(e_g, _rel(out[1][i], rq))
+        hq.close()
+    line = {
+        "metric": "1D slab forward+adjoint (config 1)", "value": 1e3 / float(np.median(lat)), "unit": "solves/s",
+        "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "1D 200 cells over 1 um, P7, Cu/Ni in 4 layers (SC mass fractions), 15 keV",
+                   "energy_steps": s.problem.N_steps, "configured_energy_steps": 100},
+        "fp64_plain_latency_ms": {"p50": float(np.median(lat)), "p99": float(np.percentile(lat, 99)),
+                                  "note": "host API (pn_forward + pn_adjoint) with copies"},
+        "parity_vs_oracle": {"intensity": _rel(I64, I_o), "rho_bar": _rel(rb64, rb_o), "noa_bar": _rel(nb64, nb_o),
+                             "acs_bar": _rel(ab64, ab_o)},
+        "gradient_vs_oracle_fd": {"cells": int(vals.size), "h": hstep,
+                                  "max_rel_err_where_fd_above_1e-3_of_max": float(np.max(np.abs(g[big] - fd[big]) / np.abs(fd[big]))),
+                                  "normwise": float(np.max(np.abs(g - fd)) / np.max(np.abs(fd))),
+                                  "directional_rel_err": float(abs(g @ np.ones_like(g) - fd @ np.ones_like(fd)) / abs(fd @ np.ones_like(fd)))},
+        "fp32_batch_256": {"solves_per_s": 256 / ((fw + ad) / 1e3), "forward_ms": fw, "adjoint_ms": ad,
+                           "max_rel_err_intensity_vs_fp64": e_I, "max_rel_err_rho_bar_vs_fp64": e_g,
+                           "kernels": info.forward_kernels + info.adjoint_kernels},
+    }
+    print(json.dumps(line), flush=True)
+    h.close()
+
+
+def run_config3(args):
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.problem import PN_FP64
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    solves = workloads.config3()
+    descs, keep, inputs, ibars = [], [], [], []
+    for q in solves:
+        dq, kq = q.problem.descriptor(q.x_rays)
+        descs.append(dq)
+        keep.append(kq)
+        inputs.append(q.inputs())
+        ibars.append(np.ones(len(q.x_rays)))
+    prep = time.perf_counter() - t0
+    fw, ad, info, out = _batch_run(torch, descs, keep, inputs, ibars)
+    # every instance against FP64 plain (pinned to the oracle by the parity tests)
+    e_I, e_g, per = 0.0, 0.0, []
+    for i, q in enumerate(solves):
+        q.problem.precision = PN_FP64
+        dq, kq = q.problem.descriptor(q.x_rays)
+        hq = capi.Handle(dq, kq)
+        Iq = hq.forward(*inputs[i])
+        rq, _, _ = hq.adjoint(ibars[i])
+        per.append((_rel(out[0][i], Iq), _rel(out[1][i], rq)))
+        hq.close()
+    per = np.array(per)
+    # and the smallest instances against the CPU oracle directly
+    small = sorted(range(len(solves)), key=lambda i: descs[i].n_points[0] * descs[i].n_points[1] * descs[i].n_steps)[:4]
+    ora = []
+    for i in small:
+        q = solves[i]
+        dq, kq = q.problem.descriptor(q.x_rays)
+        I_o, rb_o, _, _ = oracle.adjoint(dq, *inputs[i], ibars[i])
+        ora.append((_rel(out[0][i], I_o), _rel(out[1][i], rb_o)))
+    mcu = 0
+    for q in solves:
+        _b, ma = algorithmic_bytes_per_step(q, 4)
+        mcu += 2 * q.problem.N_steps * ma
+    line = {
+        "metric": "batched FP32 forward+adjoint solves/s (config 3: 256 mixed 2D instances in one batch)",
+        "value": len(solves) / ((fw + ad) / 1e3), "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f32 state and stencil, f64 accumulators", "data": "synthetic (seeded)",
+        "config": {"workload": "256 instances: grids {64x32, 128x64, 256x128}, N in {5, 7, 11}, 2-4 of Fe/Cr/Ni/Cu, "
+                               "E ~ U(8, 25) keV, 10 steps per keV (stabilised)", "host_prep_s": prep,
+                   "groups": info.n_groups, "tma_groups": info.tma_groups, "checkpoint_stride": info.checkpoint_stride},
+        "forward_ms": fw, "adjoint_ms": ad, "moment_cell_updates_per_s": mcu / ((fw + ad) / 1e3),
+        "errors_vs_fp64_plain": {"max_rel_err_intensity": float(per[:, 0].max()),
+                                 "median_rel_err_intensity": float(np.median(per[:, 0])),
+                                 "max_rel_err_rho_bar": float(per[:, 1].max()),
+                                 "median_rel_err_rho_bar": float(np.median(per[:, 1]))},
+        "errors_vs_cpu_oracle_smallest4": {"max_rel_err_intensity": float(max(a for a, _ in ora)),
+                                           "max_rel_err_rho_bar": float(max(b for _, b in ora))},
+        "kernels": info.forward_kernels + info.adjoint_kernels,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.profile:
@@ -700,6 +1049,12 @@ def main():
         run_profile_batch(args)
     elif args.serve:
         run_serve(args)
+    elif args.config4:
+        run_config4(args)
+    elif args.config1:
+        run_config1(args)
+    elif args.config3:
+        run_config3(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -574,10 +574,8 @@ class BatchGroup : public BatchGroupBase {
   bool use_tma = false;
   std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
   std::vector<TTile> ttl[3];     // per list: 0 / 1 parity targets, 2 every class (density integral)
-  std::vector<GFace> gfl[3];
-  std::vector<int> tend[3], gend[3], gthr[3];   // per solve: tile / face / ghost-thread prefix ends
+  std::vector<int> tend[3];   // per solve: end of its tiles (solve-major lists)
   TTile* dttl[3] = {nullptr, nullptr, nullptr};
-  GFace* dgfl[3] = {nullptr, nullptr, nullptr};
   void* dirows = nullptr;
   int tma_int_grid = 0;
   CUtensorMap* dmaps = nullptr;
@@ -762,7 +760,9 @@ class BatchGroup : public BatchGroupBase {
       if (!encode_tiled_fn()) return PN_OK;
       for (int q = 0; q < n; ++q)
         for (int c = 0; c < 8; ++c)
-          if (hinst[q].active[c] && (hinst[q].shape[c][0] < BW || hinst[q].shape[c][1] < TY + 1 || hinst[q].shape[c][0] > 2040 ||
+          // boxes may overhang a narrow grid (the overhang reads zeros); the encoder rejects what
+          // the tensor unit cannot address, and the group then keeps the generic kernels
+          if (hinst[q].active[c] && (hinst[q].shape[c][0] < 8 || hinst[q].shape[c][1] < 4 || hinst[q].shape[c][0] > 2040 ||
                                      hinst[q].shape[c][1] > 2040))
             return PN_OK;
       int smem_optin = 0, dev = 0;
@@ -855,17 +855,14 @@ class BatchGroup : public BatchGroupBase {
           const long long rho_dims[3] = {I.shape[c][0], I.shape[c][1], I.ne};
           const int boxr[3] = {BW, TY, I.ne};
           ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 3, rho_dims, st_str, boxr);
-          if (!ok) {
-            err = "tensor map encoding failed";
-            return PN_ERR_CUDA;
-          }
+          ok = ok && encode_tensor(&m[TM_RBAR], I.rbar[c], 3, rho_dims, st_str, boxr, 8);
+          if (!ok) return PN_OK;   // generic kernels for this group
         }
       }
       if ((rc = upload(dmaps, maps))) return rc;
       if ((rc = alloc(dstatus, 1))) return rc;
       PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), cap));
-      // tiles over every target cell, and the single-axis ghost faces, per parity list; partial
-      // slots are the eee tiles of list 0 in tile order
+      // tiles over every target cell per list; partial slots are the eee tiles of list 0 in tile order
       n_ptiles = 0;
       for (int q = 0; q < n; ++q) {
         hinst[q].ptile0 = 0;
@@ -873,9 +870,6 @@ class BatchGroup : public BatchGroupBase {
       }
       for (int list = 0; list < 3; ++list) {
         tend[list].assign(n, 0);
-        gend[list].assign(n, 0);
-        gthr[list].assign(n, 0);
-        int threads = 0;
         for (int q = 0; q < n; ++q) {
           const BInst<T>& I = hinst[q];
           if (list == 0) hinst[q].ptile0 = n_ptiles;
@@ -906,37 +900,11 @@ class BatchGroup : public BatchGroupBase {
                 tt.arg_int = arg_int[q];
                 ttl[list].push_back(tt);
               }
-            // ghosts read by the class's face cells along each axis where it is even
-            for (int dax = 0; dax < 2; ++dax) {
-              if (class_bit(c, dax)) continue;
-              const int e = 1 - dax;
-              const int nf = class_moments_host(c ^ (4 >> dax));
-              if (nf == 0) continue;
-              for (int side_ = 0; side_ < 2; ++side_) {
-                GFace f;
-                std::memset(&f, 0, sizeof(f));
-                f.inst = q;
-                f.cls = c;
-                f.axis = dax;
-                f.side = side_;
-                f.t_lo = lo3[e];
-                f.t_cnt = hi3[e] - lo3[e];
-                f.thread0 = threads;
-                f.ns = I.ns;
-                f.arg_fwd = arg_fwd[q];
-                f.arg_int = arg_int[q];
-                threads += f.t_cnt * nf;
-                gfl[list].push_back(f);
-              }
-            }
           }
           if (list == 0) hinst[q].n_ptile = n_ptiles - hinst[q].ptile0;
           tend[list][q] = (int)ttl[list].size();
-          gend[list][q] = (int)gfl[list].size();
-          gthr[list][q] = threads;
         }
         if ((rc = upload(dttl[list], ttl[list]))) return rc;
-        if ((rc = upload(dgfl[list], gfl[list]))) return rc;
       }
       use_tma = true;
     }
@@ -1207,33 +1175,13 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  // TMA path of a sub-step: the ghost points the face cells read, then every target cell
+  // TMA path of a sub-step: every target cell (face tiles compute their ghosts in place)
   int launch_tma(int list, int mode, int j, int sub, double* part, bool adj) {
     if constexpr (std::is_same<T, float>::value && DIMS == 3) {
       int last = -1;
       for (int q = 0; q < n; ++q)
         if (hinst[q].ns > j) last = q;
       if (last < 0) return PN_OK;
-      const int nthr = gthr[list][last];
-      if (nthr > 0) {
-        GLaunch<N> g;
-        g.inst = dinst;
-        g.faces = dgfl[list];
-        g.rows = static_cast<const ArgRow<N>*>(drows);
-        g.irows = static_cast<const IntRow<N>*>(dirows);
-        g.n_faces = gend[list][last];
-        g.n_threads = nthr;
-        g.mode = mode;
-        g.j = j;
-        g.sub = sub;
-        g.K = K;
-        if (adj)
-          batch_ghost2d_kernel<N, GK_ADJ><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
-        else
-          batch_ghost2d_kernel<N, GK_FWD><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
-        PN_CUDA(cudaGetLastError());
-        ++nl;
-      }
       const int nb = tend[list][last];
       if (nb > 0) {
         TLaunch<N> a;
@@ -1263,30 +1211,13 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  // TMA path of the density integral at iteration j: ghosts of the tape state, then every cell
+  // TMA path of the density integral at iteration j: every cell of every class
   int launch_tma_int(int j) {
     if constexpr (std::is_same<T, float>::value && DIMS == 3) {
       int last = -1;
       for (int q = 0; q < n; ++q)
         if (hinst[q].ns >= j) last = q;   // the integral at iteration j includes solves with ns == j
       if (last < 0) return PN_OK;
-      const int nthr = gthr[2][last];
-      if (nthr > 0) {
-        GLaunch<N> g;
-        g.inst = dinst;
-        g.faces = dgfl[2];
-        g.rows = static_cast<const ArgRow<N>*>(drows);
-        g.irows = static_cast<const IntRow<N>*>(dirows);
-        g.n_faces = gend[2][last];
-        g.n_threads = nthr;
-        g.mode = BM_ADJOINT;
-        g.j = j;
-        g.sub = 0;
-        g.K = K;
-        batch_ghost2d_kernel<N, GK_INT><<<(nthr + 255) / 256, 256, 0, cap>>>(g);
-        PN_CUDA(cudaGetLastError());
-        ++nl;
-      }
       const int nb = tend[2][last];
       if (nb > 0) {
         TILaunch<N> a;

@@ -15,8 +15,8 @@
 // Boxes start 4-float aligned, as tiled TMA requires: at x0 - 1 = 32 bx for a class odd in x (first
 // cell x0 = 1 + 32 bx), at x0 - 4 for one even in x (x0 = 32 bx; -4 for the first tile, a negative
 // coordinate that loads zeros).  Cells outside the class grid are zero-filled and never used.
-// Nothing is stored by TMA: results go to global memory from registers, target cells only.  The
-// single-axis ghost points the face cells read are written first by batch_ghost2d_kernel.
+// Nothing is stored by TMA: results go to global memory from registers, target cells only.  A
+// face tile computes the single-axis ghost points its cells read into its staged halo boxes.
 //
 // Waits on the mbarrier are bounded (1 s by %globaltimer).  A CTA whose wait runs out records
 // PN_ERR_TIMEOUT in the launch's status word, waits (again bounded) for its copies in flight and
@@ -80,19 +80,8 @@ struct TTile {
   int arg_int;  // ... IntRow (n_steps + 1 rows)
 };
 
-// The single-axis ghosts that a sub-step reads: for target class `cls` (even along `axis`) on
-// side `side`, one thread per (transverse position, component) -- ghost_fill's arithmetic,
-// computed before the cells are updated instead of by the face cells themselves.
-struct GFace {
-  int inst, cls, axis, side;
-  int t_lo, t_cnt;   // transverse positions (the other axis): t_lo .. t_lo + t_cnt - 1
-  int thread0;       // first thread of this face in the launch
-  int ns, arg_fwd, arg_int;
-  int pad_[2];
-};
-
 // tensor maps per (solve, class)
-enum { TM_ST4 = 0, TM_ST5 = 1, TM_LAM4 = 2, TM_LAM5 = 3, TM_RHO = 4, TM_KINDS = 5 };
+enum { TM_ST4 = 0, TM_ST5 = 1, TM_LAM4 = 2, TM_LAM5 = 3, TM_RHO = 4, TM_RBAR = 5, TM_KINDS = 6 };
 
 template <int N>
 struct TLaunch {
@@ -242,13 +231,88 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
 }
 
+// Ghost points of a face tile, computed into its staged halo boxes (ghost_fill's arithmetic).  A
+// class even along an axis reads, at the faces of that axis, a ghost point of the switched class;
+// its value depends on the target's values at the face cell (own box) and on the switched class's
+// first interior point (halo box), both staged.  No other tile reads these ghosts, so they are
+// never written to global memory.  All threads call this; the caller syncs before reading.
+//   own: [n(C)][TY][BW], xb: [n(C^4)][TY][BW] (x halo), yb: [n(C^2)][TY+1][BW] (y halo)
+template <int N, int C, int KIND>
+__device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TTile& tt, const float* own, float* xb,
+                                            float* yb, double bc) {
+  constexpr bool ADJ = KIND == 1;
+  constexpr int nt = Ord<N>::n(C);
+  const int xo = tt.ext >> 16;
+  const int ex = tt.ext & 255, ey = (tt.ext >> 8) & 255;
+  const double bc_scaled = bc * I.scale_g;
+  if constexpr (!((C >> 2) & 1)) {   // even in x: ghosts of C ^ 4 at x = 0 and x = n_C
+    constexpr int F = C ^ 4;
+    constexpr int nf = Ord<N>::n(F);
+    if constexpr (nt > 0 && nf > 0) {
+      const int ncx = I.g[C].n[0];
+      const double* B = ADJ ? I.bmat_a[0][F] : I.bmat_f[0][F];
+      for (int side = 0; side < 2; ++side) {
+        const bool left = side == 0;
+        if (left ? tt.x0 != 0 : tt.x0 + ex != ncx) continue;
+        // columns (the own and halo boxes start at the same xa = x0 - xo): the face cell, F's
+        // ghost (index 0 on the left, n_C on the right), F's first interior point (1, n_C - 1)
+        const int cc = left ? xo : ex - 1 + xo;
+        const int gcol = left ? xo : ex + xo;
+        const int icol = left ? xo + 1 : ex + xo - 1;
+        const bool src = !ADJ && !left;
+        for (int w = threadIdx.x; w < ey * nf; w += BLOCK) {
+          const int ty = w / nf, r = w % nf;
+          float bv = 0.0f;
+#pragma unroll
+          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PL4 + ty * BW + cc], bv);
+          const int j = tt.y0 + ty;
+          const float gval = src ? float(I.beam[F][(long long)j * nf + r] * bc_scaled) : 0.0f;
+          const float interior = xb[r * PL4 + ty * BW + icol];
+          xb[r * PL4 + ty * BW + gcol] = left ? 2.0f * (gval - bv) - interior : 2.0f * (bv + gval) - interior;
+        }
+      }
+    }
+  }
+  if constexpr (!((C >> 1) & 1)) {   // even in y: ghosts of C ^ 2 at y = 0 and y = n_C (the y box starts at y0)
+    constexpr int F = C ^ 2;
+    constexpr int nf = Ord<N>::n(F);
+    if constexpr (nt > 0 && nf > 0) {
+      const int ncy = I.g[C].n[1];
+      const double* B = ADJ ? I.bmat_a[1][F] : I.bmat_f[1][F];
+      for (int side = 0; side < 2; ++side) {
+        const bool left = side == 0;
+        if (left ? tt.y0 != 0 : tt.y0 + ey != ncy) continue;
+        const int crow = left ? 0 : ey - 1;   // the face cells' row in the own box
+        const int grow = left ? 0 : ey;       // the ghost row in the y box
+        const int irow = left ? 1 : ey - 1;   // the first interior row of F
+        for (int w = threadIdx.x; w < ex * nf; w += BLOCK) {
+          const int tx = w % ex, r = w / ex;
+          float bv = 0.0f;
+#pragma unroll
+          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PL4 + crow * BW + tx + xo], bv);
+          const float interior = yb[r * PL5 + irow * BW + tx + xo];
+          yb[r * PL5 + grow * BW + tx + xo] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
+        }
+      }
+    }
+  }
+}
+
 // One cell of a staged tile: substep_cell's arithmetic with operands from shared memory.
 template <int N, int C, bool ADJ>
-__device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, const unsigned char* st,
+__device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                          double (&red)[BLOCK / 32][MAXR]) {
   using LY = TmaLayout<N>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
+  {
+    const BInst<float>& I = L.inst[tt.inst];
+    const ArgRow<N>& ar0 = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
+    tile_ghosts<N, C, ADJ ? 1 : 0>(I, tt, reinterpret_cast<const float*>(st + LY::OWN),
+                                   reinterpret_cast<float*>(st + LY::XN), reinterpret_cast<float*>(st + LY::YN),
+                                   ADJ ? 0.0 : ar0.bc);
+    __syncthreads();
+  }
   const float* own = reinterpret_cast<const float*>(st + LY::OWN);
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
@@ -432,7 +496,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       __syncthreads();
       return;
     }
-    const unsigned char* st = smem + s * LY::STAGE;
+    unsigned char* st = smem + s * LY::STAGE;
     switch (tt.cls) {
       case 0: tma_cell<N, 0, ADJ>(L, tt, st, red); break;
       case 2: tma_cell<N, 2, ADJ>(L, tt, st, red); break;
@@ -466,7 +530,8 @@ struct TmaIntLayout {
   static constexpr int XN = LAM + B::al(B::NO * PL4 * 4);
   static constexpr int YN = XN + B::al(B::NXN * PL4 * 4);
   static constexpr int RHO = YN + B::al(B::NYN * PL5 * 4);
-  static constexpr int ARG = RHO + B::al(MAXE * PL4 * 4);
+  static constexpr int RBAR = RHO + B::al(MAXE * PL4 * 4);   // FP64
+  static constexpr int ARG = RBAR + B::al(MAXE * PL4 * 8);
   static constexpr int STAGE = ARG + B::al((int)sizeof(IntRow<N>));
   static constexpr int SMEM = TSTAGES * STAGE;
 };
@@ -478,8 +543,8 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
-  const unsigned bytes =
-      4u * (unsigned)(2 * PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) + (unsigned)sizeof(IntRow<N>);
+  const unsigned bytes = 4u * (unsigned)(2 * PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) +
+                         8u * (unsigned)(PL4 * tt.ne) + (unsigned)sizeof(IntRow<N>);
   const int ya = tt.y0 - ((c >> 1) & 1);
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
@@ -489,14 +554,22 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST4, xa, tt.y0, 0, slot, bar);
   if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST5, xa, ya, 0, slot, bar);
   tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
+  tma_load_3d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, xa, tt.y0, 0, bar);
   bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
 }
 
 template <int N, int C>
-__device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& tt, const unsigned char* st) {
+__device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& tt, unsigned char* st) {
   using LY = TmaIntLayout<N>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
+  {
+    const BInst<float>& I = L.inst[tt.inst];
+    const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
+    tile_ghosts<N, C, 2>(I, tt, reinterpret_cast<const float*>(st + LY::OWN), reinterpret_cast<float*>(st + LY::XN),
+                         reinterpret_cast<float*>(st + LY::YN), ar0.bc);
+    __syncthreads();
+  }
   if constexpr (n > 0) {
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int xo = tt.ext >> 16;
@@ -506,6 +579,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
     const float* xn = reinterpret_cast<const float*>(st + LY::XN);
     const float* yn = reinterpret_cast<const float*>(st + LY::YN);
     const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
+    const double* rbs = reinterpret_cast<const double*>(st + LY::RBAR);
     const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
     const BInst<float>& I = L.inst[tt.inst];
     const int i = tt.x0 + tx, j = tt.y0 + ty;
@@ -579,7 +653,8 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
 #pragma unroll
         for (int l = 0; l <= N; ++l)
           if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
-        rb[e * gt.ms] += v * ar.wfac;
+        const double old = rbs[e * PL4 + lo];   // this cell's rho_bar, staged with the tile
+        rb[e * gt.ms] = old + v * ar.wfac;
       }
     }
     if constexpr (C == 0) {
@@ -636,7 +711,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       __syncthreads();
       return;
     }
-    const unsigned char* st = smem + s * LY::STAGE;
+    unsigned char* st = smem + s * LY::STAGE;
     switch (tt.cls) {
       case 0: tma_int_cell<N, 0>(L, tt, st); break;
       case 2: tma_int_cell<N, 2>(L, tt, st); break;
@@ -644,102 +719,6 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       default: tma_int_cell<N, 6>(L, tt, st); break;
     }
     __syncthreads();
-  }
-}
-
-// ghost kernel modes: sub-step of the forward (or recompute) march, of the adjoint, density integral
-enum { GK_FWD = 0, GK_ADJ = 1, GK_INT = 2 };
-
-template <int N>
-struct GLaunch {
-  const BInst<float>* inst;
-  const GFace* faces;
-  const ArgRow<N>* rows;
-  const IntRow<N>* irows;
-  int n_faces, n_threads;
-  int mode, j, sub, K;
-};
-
-template <int N, int C, int D, int KIND>
-__device__ __forceinline__ void ghost_one(const GLaunch<N>& L, const GFace& f, int tpos, int r) {
-  constexpr bool ADJ = KIND == GK_ADJ;
-  constexpr int F = C ^ (4 >> D);
-  constexpr int nt = Ord<N>::n(C);
-  constexpr int nf = Ord<N>::n(F);
-  if constexpr (nt == 0 || nf == 0) {
-    return;
-  } else {
-    const BInst<float>& I = L.inst[f.inst];
-    float* own;
-    float* from;
-    double bc = 0.0;
-    if (KIND == GK_ADJ) {
-      own = from = I.lam;
-    } else if (KIND == GK_INT) {
-      // the tape state of iteration j, forward boundary blocks, beam source of the iteration
-      own = from = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j, L.K, true, L.j / L.K) * I.slot_elems;
-      bc = L.irows[f.arg_int + L.j].bc;
-    } else {
-      const bool segment = L.mode == BM_RECOMPUTE;
-      const int m = L.j / L.K;
-      float* src = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j + 1, L.K, segment, m) * I.slot_elems;
-      float* dst = I.slots + (long long)slot_index(I.ns, I.n_ck, L.j, L.K, segment, m) * I.slot_elems;
-      own = (L.sub == 3) ? dst : src;
-      from = (L.sub == 1) ? src : dst;
-      bc = L.rows[f.arg_fwd + (f.ns - L.j - 1)].bc;
-    }
-    const Geom& gt = I.g[C];
-    const Geom& gf = I.g[F];
-    const bool left = f.side == 0;
-    int c3[3] = {0, 0, 0};
-    c3[D] = left ? 0 : gt.n[D] - 1;
-    c3[1 - D] = tpos;
-    int cg[3] = {c3[0], c3[1], 0};
-    int ci[3] = {c3[0], c3[1], 0};
-    if (left) {
-      cg[D] = 0;
-      ci[D] = 1;
-    } else {
-      cg[D] = c3[D] + 1;
-      ci[D] = c3[D];
-    }
-    const float* ut = own + I.dev_off[C] + lin(gt, c3[0], c3[1], 0);
-    const double* B = (ADJ ? I.bmat_a[D][F] : I.bmat_f[D][F]) + (long long)r * nt;
-    float bv = 0.0f;
-#pragma unroll
-    for (int q = 0; q < nt; ++q) bv = fmaf(float(B[q]), ut[q * gt.ms], bv);
-    const bool src = !ADJ && D == 0 && !left;
-    const double bc_scaled = bc * I.scale_g;
-    const float gval = src ? float(I.beam[F][((long long)0 * gf.n[1] + c3[1]) * nf + r] * bc_scaled) : 0.0f;
-    const float interior = from[I.dev_off[F] + lin(gf, ci[0], ci[1], 0) + (long long)r * gf.ms];
-    const float gh = left ? 2.0f * (gval - bv) - interior : 2.0f * (bv + gval) - interior;
-    from[I.dev_off[F] + lin(gf, cg[0], cg[1], 0) + (long long)r * gf.ms] = gh;
-  }
-}
-
-template <int N, int KIND>
-__global__ void __launch_bounds__(256) batch_ghost2d_kernel(const __grid_constant__ GLaunch<N> L) {
-  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (gid >= L.n_threads) return;
-  int lo = 0, hi = L.n_faces - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (L.faces[mid].thread0 <= gid) lo = mid;
-    else hi = mid - 1;
-  }
-  const GFace f = L.faces[lo];
-  const int nf = class_moments<N>(f.cls ^ (4 >> f.axis));
-  const int rem = gid - f.thread0;
-  const int tpos = f.t_lo + rem / nf, r = rem % nf;
-  switch (f.cls * 2 + f.axis) {
-    case 0: ghost_one<N, 0, 0, KIND>(L, f, tpos, r); break;
-    case 1: ghost_one<N, 0, 1, KIND>(L, f, tpos, r); break;
-    case 4: ghost_one<N, 2, 0, KIND>(L, f, tpos, r); break;
-    case 5: ghost_one<N, 2, 1, KIND>(L, f, tpos, r); break;
-    case 8: ghost_one<N, 4, 0, KIND>(L, f, tpos, r); break;
-    case 9: ghost_one<N, 4, 1, KIND>(L, f, tpos, r); break;
-    case 12: ghost_one<N, 6, 0, KIND>(L, f, tpos, r); break;
-    default: ghost_one<N, 6, 1, KIND>(L, f, tpos, r); break;
   }
 }
 
@@ -765,9 +744,9 @@ inline EncodeTiledFn encode_tiled_fn() {
   return fn;
 }
 
-// FP32 tensor of rank 3 (x, y, plane) or 4 (x, y, plane, slot); strides in elements
-inline bool encode_f32(CUtensorMap* out, void* base, int rank, const long long* dims, const long long* strides,
-                       const int* box) {
+// tensor of rank 3 (x, y, plane) or 4 (x, y, plane, slot) of 4- or 8-byte floats; strides in elements
+inline bool encode_tensor(CUtensorMap* out, void* base, int rank, const long long* dims, const long long* strides,
+                          const int* box, int elem_bytes) {
   EncodeTiledFn fn = encode_tiled_fn();
   if (!fn) return false;
   cuuint64_t gd[4], gs[3];
@@ -776,11 +755,17 @@ inline bool encode_f32(CUtensorMap* out, void* base, int rank, const long long* 
     gd[d] = (cuuint64_t)dims[d];
     bd[d] = (cuuint32_t)box[d];
     es[d] = 1;
-    if (d > 0) gs[d - 1] = (cuuint64_t)strides[d] * 4u;
+    if (d > 0) gs[d - 1] = (cuuint64_t)strides[d] * (cuuint64_t)elem_bytes;
   }
-  return fn(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, base, gd, gs, bd, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  const CUtensorMapDataType dt = elem_bytes == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  return fn(out, dt, (cuuint32_t)rank, base, gd, gs, bd, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
          CUDA_SUCCESS;
+}
+
+inline bool encode_f32(CUtensorMap* out, void* base, int rank, const long long* dims, const long long* strides,
+                       const int* box) {
+  return encode_tensor(out, base, rank, dims, strides, box, 4);
 }
 
 }  // namespace pn

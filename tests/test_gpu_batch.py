@@ -108,6 +108,8 @@ def tma_solves():
                              elements=("Fe", "Cr", "Ni")),
         workloads.small_case(dims=2, N=11, shape=(40, 12), n_steps=4, seed=14, precision=PN_FP32),
         workloads.small_case(dims=2, N=3, shape=(70, 9), n_steps=9, seed=15, precision=PN_FP32),
+        workloads.small_case(dims=2, N=5, shape=(32, 20), n_steps=6, seed=16, precision=PN_FP32),
+        workloads.small_case(dims=2, N=11, shape=(20, 8), n_steps=3, seed=17, precision=PN_FP32),
     ]
 
 
