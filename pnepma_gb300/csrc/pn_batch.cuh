@@ -577,6 +577,7 @@ class BatchGroup : public BatchGroupBase {
   std::vector<int> tend[3];   // per solve: end of its tiles (solve-major lists)
   TTile* dttl[3] = {nullptr, nullptr, nullptr};
   void* dirows = nullptr;
+  TSolve* dsolves = nullptr;
   int tma_int_grid = 0;
   CUtensorMap* dmaps = nullptr;
   void* drows = nullptr;
@@ -860,6 +861,38 @@ class BatchGroup : public BatchGroupBase {
         }
       }
       if ((rc = upload(dmaps, maps))) return rc;
+      // per-solve arguments staged with every tile
+      std::vector<TSolve> hs(n);
+      for (int q = 0; q < n; ++q) {
+        const BInst<T>& I = hinst[q];
+        TSolve& S = hs[q];
+        std::memset(&S, 0, sizeof(S));
+        S.slots = I.slots;
+        S.lam = I.lam;
+        S.slot_elems = I.slot_elems;
+        S.wint = I.wint;
+        S.acs = I.acs;
+        S.noa = I.noa;
+        S.ibar = I.ibar;
+        S.acs_bar = I.acs_bar;
+        S.noa_bar = I.noa_bar;
+        for (int c = 0; c < 8; ++c) {
+          S.rbar[c] = I.rbar[c];
+          S.dev_off[c] = I.dev_off[c];
+          S.ms[c] = I.g[c].ms;
+          S.px[c] = I.g[c].px;
+          S.n0[c] = I.g[c].n[0];
+          S.n1[c] = I.g[c].n[1];
+        }
+        for (int r = 0; r < MAXR; ++r) S.xel[r] = I.xel[r];
+        S.inv_h[0] = I.inv_h[0];
+        S.inv_h[1] = I.inv_h[1];
+        S.dE = I.dE;
+        S.nr = I.nr;
+        S.ne = I.ne;
+        S.scale_g = I.scale_g;
+      }
+      if ((rc = upload(dsolves, hs))) return rc;
       if ((rc = alloc(dstatus, 1))) return rc;
       PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), cap));
       // tiles over every target cell per list; partial slots are the eee tiles of list 0 in tile order
@@ -1186,6 +1219,7 @@ class BatchGroup : public BatchGroupBase {
       if (nb > 0) {
         TLaunch<N> a;
         a.inst = dinst;
+        a.solves = dsolves;
         a.tiles = dttl[list];
         a.maps = dmaps;
         a.rows = static_cast<const ArgRow<N>*>(drows);
@@ -1222,6 +1256,7 @@ class BatchGroup : public BatchGroupBase {
       if (nb > 0) {
         TILaunch<N> a;
         a.inst = dinst;
+        a.solves = dsolves;
         a.tiles = dttl[2];
         a.maps = dmaps;
         a.rows = static_cast<const IntRow<N>*>(dirows);

@@ -80,12 +80,42 @@ struct TTile {
   int arg_int;  // ... IntRow (n_steps + 1 rows)
 };
 
+// The fields of a solve the cell code reads, copied to shared memory with every tile so that no
+// per-tile argument costs a dependent global load (16-byte multiple).
+struct TSolve {
+  float* slots;
+  float* lam;
+  long long slot_elems;
+  double* wint;
+  const double* acs;
+  const double* noa;
+  const double* ibar;
+  double* acs_bar;
+  double* noa_bar;
+  double* rbar[8];
+  long long dev_off[8];
+  long long ms[8];
+  int px[8];
+  int n0[8];
+  int n1[8];
+  int xel[MAXR];
+  float inv_h[2];
+  float dE;
+  int nr;
+  int ne;
+  int pad_[3];
+  double scale_g;
+};
+static_assert(sizeof(TSolve) % 16 == 0, "TSolve must be a 16-byte multiple");
+static_assert(sizeof(TTile) % 16 == 0, "TTile must be a 16-byte multiple");
+
 // tensor maps per (solve, class)
 enum { TM_ST4 = 0, TM_ST5 = 1, TM_LAM4 = 2, TM_LAM5 = 3, TM_RHO = 4, TM_RBAR = 5, TM_KINDS = 6 };
 
 template <int N>
 struct TLaunch {
   const BInst<float>* inst;
+  const TSolve* solves;
   const TTile* tiles;
   const CUtensorMap* maps;      // [solve][8][TM_KINDS]
   const ArgRow<N>* rows;
@@ -108,7 +138,9 @@ struct TmaLayout {
   static constexpr int YN = XN + al(NXN * PL4 * 4);
   static constexpr int RHO = YN + al(NYN * PL5 * 4);
   static constexpr int ARG = RHO + al(MAXE * PL4 * 4);
-  static constexpr int STAGE = ARG + al((int)sizeof(ArgRow<N>));
+  static constexpr int TIL = ARG + (int)sizeof(ArgRow<N>);
+  static constexpr int SOL = TIL + (int)sizeof(TTile);
+  static constexpr int STAGE = al(SOL + (int)sizeof(TSolve));
   static constexpr int SMEM = TSTAGES * STAGE;
 };
 
@@ -193,6 +225,7 @@ __device__ __forceinline__ int class_moments(int c) {
 }
 
 // Issue the loads of tile t into stage `st` (one thread).
+// `tt` must be the tile record in global memory (it is also bulk-copied into the stage)
 template <int N, bool ADJ>
 __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                           unsigned long long* bar) {
@@ -211,7 +244,8 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   } else {
     row = tt.arg_adj + L.j;
   }
-  const unsigned bytes = 4u * (unsigned)(PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) + (unsigned)sizeof(ArgRow<N>);
+  const unsigned bytes = 4u * (unsigned)(PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) +
+                         (unsigned)(sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
   // the y box starts one row below the tile for a target odd in y (it reads rows j - 1 and j),
   // at the tile for one even in y (rows j and j + 1)
   const int ya = tt.y0 - ((c >> 1) & 1);
@@ -229,6 +263,8 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   }
   tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
   bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
+  bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
+  bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
 }
 
 // Ghost points of a face tile, computed into its staged halo boxes (ghost_fill's arithmetic).  A
@@ -238,22 +274,23 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
 // never written to global memory.  All threads call this; the caller syncs before reading.
 //   own: [n(C)][TY][BW], xb: [n(C^4)][TY][BW] (x halo), yb: [n(C^2)][TY+1][BW] (y halo)
 template <int N, int C, int KIND>
-__device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TTile& tt, const float* own, float* xb,
-                                            float* yb, double bc) {
+__device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, const float* own,
+                                            float* xb, float* yb, double bc) {
   constexpr bool ADJ = KIND == 1;
   constexpr int nt = Ord<N>::n(C);
   const int xo = tt.ext >> 16;
   const int ex = tt.ext & 255, ey = (tt.ext >> 8) & 255;
-  const double bc_scaled = bc * I.scale_g;
+  const double bc_scaled = bc * S.scale_g;
   if constexpr (!((C >> 2) & 1)) {   // even in x: ghosts of C ^ 4 at x = 0 and x = n_C
     constexpr int F = C ^ 4;
     constexpr int nf = Ord<N>::n(F);
     if constexpr (nt > 0 && nf > 0) {
-      const int ncx = I.g[C].n[0];
+      const int ncx = S.n0[C];
       const double* B = ADJ ? I.bmat_a[0][F] : I.bmat_f[0][F];
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
         if (left ? tt.x0 != 0 : tt.x0 + ex != ncx) continue;
+        // a face tile: the boundary blocks and the beam face come from the full descriptor
         // columns (the own and halo boxes start at the same xa = x0 - xo): the face cell, F's
         // ghost (index 0 on the left, n_C on the right), F's first interior point (1, n_C - 1)
         const int cc = left ? xo : ex - 1 + xo;
@@ -277,7 +314,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TTile& 
     constexpr int F = C ^ 2;
     constexpr int nf = Ord<N>::n(F);
     if constexpr (nt > 0 && nf > 0) {
-      const int ncy = I.g[C].n[1];
+      const int ncy = S.n1[C];
       const double* B = ADJ ? I.bmat_a[1][F] : I.bmat_f[1][F];
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
@@ -305,10 +342,10 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   using LY = TmaLayout<N>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
+  const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   {
-    const BInst<float>& I = L.inst[tt.inst];
     const ArgRow<N>& ar0 = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, ADJ ? 1 : 0>(I, tt, reinterpret_cast<const float*>(st + LY::OWN),
+    tile_ghosts<N, C, ADJ ? 1 : 0>(L.inst[tt.inst], I, tt, reinterpret_cast<const float*>(st + LY::OWN),
                                    reinterpret_cast<float*>(st + LY::XN), reinterpret_cast<float*>(st + LY::YN),
                                    ADJ ? 0.0 : ar0.bc);
     __syncthreads();
@@ -327,7 +364,6 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
   if constexpr (n > 0) {
     if (valid) {
-      const BInst<float>& I = L.inst[tt.inst];
       const int i = tt.x0 + tx, j = tt.y0 + ty;
       const int lo = ty * BW + tx + xo;                       // the cell in the own / density boxes
       const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;         // x neighbours: i, i - 1 (odd) or i + 1, i
@@ -395,7 +431,7 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
       }
       float q0 = 0.0f;
       long long ce = 0;
-      if constexpr (C == 0) ce = eee_cell(I.g[0], i, j, 0);
+      if constexpr (C == 0) ce = (long long)j * I.n0[0] + i;
       if constexpr (ADJ && C == 0) {
         double q = 0.0;
         for (int r = 0; r < I.nr; ++r)
@@ -409,9 +445,8 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
         const bool segment = L.mode == BM_RECOMPUTE;
         base = I.slots + (long long)slot_index(tt.ns, tt.n_ck, L.j, L.K, segment, L.j / L.K) * I.slot_elems;
       }
-      const Geom& gt = I.g[C];
-      float* un = base + I.dev_off[C] + (long long)j * gt.px + i;
-      const long long ms = gt.ms;
+      float* un = base + I.dev_off[C] + (long long)j * I.px[C] + i;
+      const long long ms = I.ms[C];
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
@@ -484,7 +519,6 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_issue<N, ADJ>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
-    const TTile tt = L.tiles[t];
     const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
@@ -497,6 +531,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       return;
     }
     unsigned char* st = smem + s * LY::STAGE;
+    const TTile& tt = *reinterpret_cast<const TTile*>(st + LY::TIL);
     switch (tt.cls) {
       case 0: tma_cell<N, 0, ADJ>(L, tt, st, red); break;
       case 2: tma_cell<N, 2, ADJ>(L, tt, st, red); break;
@@ -513,6 +548,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
 template <int N>
 struct TILaunch {
   const BInst<float>* inst;
+  const TSolve* solves;
   const TTile* tiles;
   const CUtensorMap* maps;
   const IntRow<N>* rows;
@@ -532,7 +568,9 @@ struct TmaIntLayout {
   static constexpr int RHO = YN + B::al(B::NYN * PL5 * 4);
   static constexpr int RBAR = RHO + B::al(MAXE * PL4 * 4);   // FP64
   static constexpr int ARG = RBAR + B::al(MAXE * PL4 * 8);
-  static constexpr int STAGE = ARG + B::al((int)sizeof(IntRow<N>));
+  static constexpr int TIL = ARG + (int)sizeof(IntRow<N>);
+  static constexpr int SOL = TIL + (int)sizeof(TTile);
+  static constexpr int STAGE = B::al(SOL + (int)sizeof(TSolve));
   static constexpr int SMEM = TSTAGES * STAGE;
 };
 
@@ -544,7 +582,7 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
   const unsigned bytes = 4u * (unsigned)(2 * PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) +
-                         8u * (unsigned)(PL4 * tt.ne) + (unsigned)sizeof(IntRow<N>);
+                         8u * (unsigned)(PL4 * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
   const int ya = tt.y0 - ((c >> 1) & 1);
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
@@ -556,6 +594,8 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
   tma_load_3d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, xa, tt.y0, 0, bar);
   bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
+  bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
+  bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
 }
 
 template <int N, int C>
@@ -563,11 +603,11 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   using LY = TmaIntLayout<N>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
+  const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   {
-    const BInst<float>& I = L.inst[tt.inst];
     const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, 2>(I, tt, reinterpret_cast<const float*>(st + LY::OWN), reinterpret_cast<float*>(st + LY::XN),
-                         reinterpret_cast<float*>(st + LY::YN), ar0.bc);
+    tile_ghosts<N, C, 2>(L.inst[tt.inst], I, tt, reinterpret_cast<const float*>(st + LY::OWN),
+                         reinterpret_cast<float*>(st + LY::XN), reinterpret_cast<float*>(st + LY::YN), ar0.bc);
     __syncthreads();
   }
   if constexpr (n > 0) {
@@ -581,7 +621,6 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
     const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
     const double* rbs = reinterpret_cast<const double*>(st + LY::RBAR);
     const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    const BInst<float>& I = L.inst[tt.inst];
     const int i = tt.x0 + tx, j = tt.y0 + ty;
     const int lo = ty * BW + tx + xo;
     const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;
@@ -644,8 +683,8 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       P = fmaf(lm, du, P);
       R[l] = fmaf(lm, u, R[l]);
     }
-    const Geom& gt = I.g[C];
-    double* rb = I.rbar[C] + lin(gt, i, j, 0);
+    double* rb = I.rbar[C] + (long long)j * I.px[C] + i;
+    const long long ms = I.ms[C];
 #pragma unroll
     for (int e = 0; e < MAXE; ++e) {
       if (e < tt.ne) {
@@ -654,11 +693,11 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
         for (int l = 0; l <= N; ++l)
           if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
         const double old = rbs[e * PL4 + lo];   // this cell's rho_bar, staged with the tile
-        rb[e * gt.ms] = old + v * ar.wfac;
+        rb[e * ms] = old + v * ar.wfac;
       }
     }
     if constexpr (C == 0) {
-      const long long ce = eee_cell(gt, i, j, 0);
+      const long long ce = (long long)j * I.n0[0] + i;
       const double u0 = double(own[lo]);
       for (int r = 0; r < I.nr; ++r) {
         const double cr = ar.coef[r] * I.ibar[r];
@@ -700,7 +739,6 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_issue_int<N>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
-    const TTile tt = L.tiles[t];
     const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
@@ -712,6 +750,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       return;
     }
     unsigned char* st = smem + s * LY::STAGE;
+    const TTile& tt = *reinterpret_cast<const TTile*>(st + LY::TIL);
     switch (tt.cls) {
       case 0: tma_int_cell<N, 0>(L, tt, st); break;
       case 2: tma_int_cell<N, 2>(L, tt, st); break;
