@@ -848,13 +848,15 @@ class BatchGroup : public BatchGroupBase {
           CUtensorMap* m = &maps[((size_t)q * 8 + c) * TM_KINDS];
           const long long st_dims[4] = {I.shape[c][0], I.shape[c][1], nm, nslots};
           const long long st_str[4] = {1, I.px[c], I.g[c].ms, I.slot_elems};
-          const int box4[4] = {BW, TY, nm, 1}, box5[4] = {BW, TY + 1, nm, 1};
-          bool ok = encode_f32(&m[TM_ST4], I.slots + I.dev_off[c], 4, st_dims, st_str, box4) &&
-                    encode_f32(&m[TM_ST5], I.slots + I.dev_off[c], 4, st_dims, st_str, box5) &&
-                    encode_f32(&m[TM_LAM4], I.lam + I.dev_off[c], 3, st_dims, st_str, box4) &&
-                    encode_f32(&m[TM_LAM5], I.lam + I.dev_off[c], 3, st_dims, st_str, box5);
+          const int boxt[4] = {TX, TY, nm, 1}, boxx[4] = {BW, TY, nm, 1}, boxy[4] = {BW, TY + 1, nm, 1};
+          bool ok = encode_f32(&m[TM_ST_T], I.slots + I.dev_off[c], 4, st_dims, st_str, boxt) &&
+                    encode_f32(&m[TM_ST_X], I.slots + I.dev_off[c], 4, st_dims, st_str, boxx) &&
+                    encode_f32(&m[TM_ST_Y], I.slots + I.dev_off[c], 4, st_dims, st_str, boxy) &&
+                    encode_f32(&m[TM_LAM_T], I.lam + I.dev_off[c], 3, st_dims, st_str, boxt) &&
+                    encode_f32(&m[TM_LAM_X], I.lam + I.dev_off[c], 3, st_dims, st_str, boxx) &&
+                    encode_f32(&m[TM_LAM_Y], I.lam + I.dev_off[c], 3, st_dims, st_str, boxy);
           const long long rho_dims[3] = {I.shape[c][0], I.shape[c][1], I.ne};
-          const int boxr[3] = {BW, TY, I.ne};
+          const int boxr[3] = {TX, TY, I.ne};
           ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 3, rho_dims, st_str, boxr);
           ok = ok && encode_tensor(&m[TM_RBAR], I.rbar[c], 3, rho_dims, st_str, boxr, 8);
           if (!ok) return PN_OK;   // generic kernels for this group
@@ -914,16 +916,18 @@ class BatchGroup : public BatchGroupBase {
               lo3[k] = class_bit(c, k) ? 1 : 0;
               hi3[k] = class_bit(c, k) ? nn - 1 : nn;
             }
-            const int xo = class_bit(c, 0) ? 1 : 4;
+            // x0 = 32 bx over the class's points; target lanes [lo - x0, hi - x0) within the tile
             for (int y0 = lo3[1]; y0 < hi3[1]; y0 += TY)
-              for (int x0 = lo3[0]; x0 < hi3[0]; x0 += TX) {
+              for (int x0 = 0; x0 < hi3[0]; x0 += TX) {
+                const int xv0 = std::max(lo3[0] - x0, 0), xv1 = std::min(hi3[0] - x0, TX);
+                if (xv1 <= xv0) continue;
                 TTile tt;
                 std::memset(&tt, 0, sizeof(tt));
                 tt.inst = q;
                 tt.cls = c;
                 tt.x0 = x0;
                 tt.y0 = y0;
-                tt.ext = std::min(TX, hi3[0] - x0) | (std::min(TY, hi3[1] - y0) << 8) | (xo << 16);
+                tt.ext = xv0 | (xv1 << 8) | (std::min(TY, hi3[1] - y0) << 16);
                 tt.pslot = (list == 0 && c == 0) ? n_ptiles++ : -1;
                 tt.ns = I.ns;
                 tt.n_ck = I.n_ck;

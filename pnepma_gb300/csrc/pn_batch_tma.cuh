@@ -1,22 +1,24 @@
-// pn_batch_tma.cuh -- FP32 2D sub-step of the batched engine with TMA-staged halo tiles.
+// pn_batch_tma.cuh -- FP32 2D sub-steps and density integral of the batched engine with TMA tiles.
 //
-// The same arithmetic as batch_substep_kernel (substep_cell with compiled coupling blocks, x then
-// y), so results are bit-identical; only the way operands reach the registers differs:
+// The same arithmetic as batch_substep_kernel / batch_integrate_kernel (compiled coupling blocks,
+// x then y), so states and gradients are bit-identical; only the way operands move differs:
 //
-//   * persistent CTAs (two per SM) walk the box tiles of a launch in grid-stride order, so the
-//     CTAs resident at any time work on neighbouring tiles;
-//   * for each 32 x 4 tile, one thread issues four cp.async.bulk.tensor loads -- the target
-//     class's moments, the x- and y-neighbour classes with their one-cell halo, the densities --
-//     plus one cp.async.bulk of the step's coefficient row, all completing on one mbarrier;
-//   * a ring of PN_TMA_STAGES stages: with two, the loads of the next tile run while the CTA
-//     computes the current one from shared memory, where every operand sits at a compile-time
-//     offset; with one, more CTAs fit on an SM and overlap one another.
-//
-// Boxes start 4-float aligned, as tiled TMA requires: at x0 - 1 = 32 bx for a class odd in x (first
-// cell x0 = 1 + 32 bx), at x0 - 4 for one even in x (x0 = 32 bx; -4 for the first tile, a negative
-// coordinate that loads zeros).  Cells outside the class grid are zero-filled and never used.
-// Nothing is stored by TMA: results go to global memory from registers, target cells only.  A
-// face tile computes the single-axis ghost points its cells read into its staged halo boxes.
+//   * persistent CTAs walk the tiles of a launch in grid-stride order, so the CTAs resident at
+//     any time work on neighbouring tiles;
+//   * a tile is 32 x 4 points of one target class starting at x0 = 32 bx: lanes outside the
+//     class's target cells (its ghost points, or points past the grid) keep the values they
+//     were loaded with;
+//   * one thread issues, on one mbarrier, cp.async.bulk.tensor loads of the target class's
+//     moments (32 x 4 box), the x- and y-neighbour classes with their one-cell halo (40 x 4 and
+//     40 x 5 boxes from x0 - 4, the first tile's negative start reading zeros) and the densities,
+//     plus cp.async.bulk copies of the step's coefficient row, the tile record and the solve's
+//     arguments; every operand then sits at a compile-time shared-memory offset;
+//   * results overwrite the target box in shared memory and go back with one cp.async.bulk.tensor
+//     store (bounded by the tensor, aligned at x0).  Stored non-target lanes are ghost points of
+//     the target class, which no kernel of a batched solve reads from memory (a face tile computes
+//     the ghosts its cells read, below), and no other tile owns them;
+//   * a face tile computes the single-axis ghost points its cells read into its staged halo boxes
+//     (ghost_fill's arithmetic).
 //
 // Waits on the mbarrier are bounded (1 s by %globaltimer).  A CTA whose wait runs out records
 // PN_ERR_TIMEOUT in the launch's status word, waits (again bounded) for its copies in flight and
@@ -30,11 +32,13 @@
 
 namespace pn {
 
-constexpr int TX = 32;          // tile width (cells)
-constexpr int TY = BLOCK / TX;  // tile height (rows)
-constexpr int BW = TX + 8;      // box width from xa = x0 - xo: covers x0 - 1 .. x0 + 32 (a multiple of 4 floats)
-constexpr int PL4 = BW * TY;    // floats per moment plane of a 4-row box
-constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row box (y halo on the side the stencil reads)
+constexpr int TX = 32;              // tile width (points)
+constexpr int TY = BLOCK / TX;      // tile height (rows)
+constexpr int BW = TX + 8;          // neighbour box width: x0 - 4 .. x0 + 35 (a multiple of 4 floats)
+constexpr int XO = 4;               // the tile's first point in a neighbour box
+constexpr int PLO = TX * TY;        // floats per moment plane of a target / density box
+constexpr int PL4 = BW * TY;        // ... of a 4-row neighbour box
+constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row neighbour box (y halo on the side the stencil reads)
 
 // stages of the tile ring per CTA (1: no prefetch within a CTA, more CTAs per SM)
 #ifndef PN_TMA_STAGES
@@ -63,14 +67,13 @@ struct IntRow {
   double bc;
 };
 
-// One 32 x 4 tile of a target class (48 bytes).  Tiles cover every target cell: from x = 0 for a
-// class even in x (its box starts at x0 - 4, an aligned negative coordinate for the first tile,
-// read as zeros), from x = 1 for one odd in x (box at x0 - 1).
+// One 32 x 4 tile of a target class (48 bytes): points x0 .. x0 + 31 (x0 = 32 bx), rows
+// y0 .. y0 + 3; target lanes xv0 <= tx < xv1, rows ty < ey.
 struct TTile {
   int inst;     // solve (group order)
   int cls;      // target class (z-even in 2D)
-  int x0, y0;   // first cell
-  int ext;      // valid cells along x (<= 32) | valid rows (<= 4) << 8 | xo = x0 - box start << 16
+  int x0, y0;
+  int ext;      // xv0 | xv1 << 8 | ey << 16
   int pslot;    // partial slot of an eee tile, else -1
   int ns;
   int n_ck;
@@ -109,8 +112,13 @@ struct TSolve {
 static_assert(sizeof(TSolve) % 16 == 0, "TSolve must be a 16-byte multiple");
 static_assert(sizeof(TTile) % 16 == 0, "TTile must be a 16-byte multiple");
 
-// tensor maps per (solve, class)
-enum { TM_ST4 = 0, TM_ST5 = 1, TM_LAM4 = 2, TM_LAM5 = 3, TM_RHO = 4, TM_RBAR = 5, TM_KINDS = 6 };
+// tensor maps per (solve, class): state (x, y, moment, slot) and adjoint state (x, y, moment) as
+// target boxes and as x / y neighbour boxes; densities; rho_bar (FP64)
+enum {
+  TM_ST_T = 0, TM_ST_X = 1, TM_ST_Y = 2,
+  TM_LAM_T = 3, TM_LAM_X = 4, TM_LAM_Y = 5,
+  TM_RHO = 6, TM_RBAR = 7, TM_KINDS = 8
+};
 
 template <int N>
 struct TLaunch {
@@ -130,14 +138,14 @@ template <int N>
 struct TmaLayout {
   static constexpr int maxn(int a, int b) { return a > b ? a : b; }
   static constexpr int NO = maxn(maxn(Ord<N>::n(0), Ord<N>::n(2)), maxn(Ord<N>::n(4), Ord<N>::n(6)));
-  static constexpr int NXN = maxn(maxn(Ord<N>::n(4), Ord<N>::n(6)), maxn(Ord<N>::n(0), Ord<N>::n(2)));
-  static constexpr int NYN = NXN;
+  static constexpr int NXN = NO;
+  static constexpr int NYN = NO;
   static constexpr int al(int b) { return (b + 127) / 128 * 128; }
   static constexpr int OWN = 0;
-  static constexpr int XN = OWN + al(NO * PL4 * 4);
+  static constexpr int XN = OWN + al(NO * PLO * 4);
   static constexpr int YN = XN + al(NXN * PL4 * 4);
   static constexpr int RHO = YN + al(NYN * PL5 * 4);
-  static constexpr int ARG = RHO + al(MAXE * PL4 * 4);
+  static constexpr int ARG = RHO + al(MAXE * PLO * 4);
   static constexpr int TIL = ARG + (int)sizeof(ArgRow<N>);
   static constexpr int SOL = TIL + (int)sizeof(TTile);
   static constexpr int STAGE = al(SOL + (int)sizeof(TSolve));
@@ -196,6 +204,25 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+// shared -> global tensor stores (coordinates >= 0 only), tracked by the bulk async-group
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int c0, int c1, int c2, const void* src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+               ::"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
+  asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];"
+               ::"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the stores' shared-memory reads are done (the stage may be overwritten)
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
@@ -224,62 +251,70 @@ __device__ __forceinline__ int class_moments(int c) {
   }
 }
 
-// Issue the loads of tile t into stage `st` (one thread).
-// `tt` must be the tile record in global memory (it is also bulk-copied into the stage)
+// slots a sub-step reads its own values from, reads its neighbours from, and writes
+struct SubSlots {
+  int own, from, out;
+};
+
+__device__ __forceinline__ SubSlots sub_slots(int ns, int n_ck, int mode, int j, int sub, int K) {
+  const bool segment = mode == BM_RECOMPUTE;
+  const int m = j / K;
+  const int src = slot_index(ns, n_ck, j + 1, K, segment, m);
+  const int dst = slot_index(ns, n_ck, j, K, segment, m);
+  return SubSlots{(sub == 3) ? dst : src, (sub == 1) ? src : dst, dst};
+}
+
+// Issue the loads of a tile into stage `st` (one thread).  `tt` must be the tile record in
+// global memory (it is also bulk-copied into the stage).
 template <int N, bool ADJ>
 __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                           unsigned long long* bar) {
   using LY = TmaLayout<N>;
   const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
-  int own_slot = 0, from_slot = 0, row;
+  SubSlots sl{0, 0, 0};
+  int row;
   if (!ADJ) {
-    const bool segment = L.mode == BM_RECOMPUTE;
-    const int m = L.j / L.K;
-    const int src = slot_index(tt.ns, tt.n_ck, L.j + 1, L.K, segment, m);
-    const int dst = slot_index(tt.ns, tt.n_ck, L.j, L.K, segment, m);
-    own_slot = (L.sub == 3) ? dst : src;
-    from_slot = (L.sub == 1) ? src : dst;
+    sl = sub_slots(tt.ns, tt.n_ck, L.mode, L.j, L.sub, L.K);
     row = tt.arg_fwd + (tt.ns - L.j - 1);
   } else {
     row = tt.arg_adj + L.j;
   }
-  const unsigned bytes = 4u * (unsigned)(PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) +
+  const unsigned bytes = 4u * (unsigned)(PLO * n_own + PL4 * n_x + PL5 * n_y + PLO * tt.ne) +
                          (unsigned)(sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
   // the y box starts one row below the tile for a target odd in y (it reads rows j - 1 and j),
   // at the tile for one even in y (rows j and j + 1)
   const int ya = tt.y0 - ((c >> 1) & 1);
+  const int xa = tt.x0 - XO;
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
-  const int xa = tt.x0 - (tt.ext >> 16);
   if (ADJ) {
-    tma_load_3d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
-    if (n_x > 0) tma_load_3d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
-    if (n_y > 0) tma_load_3d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM5, xa, ya, 0, bar);
+    tma_load_3d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, 0, bar);
+    if (n_x > 0) tma_load_3d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM_X, xa, tt.y0, 0, bar);
+    if (n_y > 0) tma_load_3d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM_Y, xa, ya, 0, bar);
   } else {
-    tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST4, xa, tt.y0, 0, own_slot, bar);
-    if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST4, xa, tt.y0, 0, from_slot, bar);
-    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST5, xa, ya, 0, from_slot, bar);
+    tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, 0, sl.own, bar);
+    if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, 0, sl.from, bar);
+    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, 0, sl.from, bar);
   }
-  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
+  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, 0, bar);
   bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
 }
 
-// Ghost points of a face tile, computed into its staged halo boxes (ghost_fill's arithmetic).  A
-// class even along an axis reads, at the faces of that axis, a ghost point of the switched class;
-// its value depends on the target's values at the face cell (own box) and on the switched class's
-// first interior point (halo box), both staged.  No other tile reads these ghosts, so they are
-// never written to global memory.  All threads call this; the caller syncs before reading.
-//   own: [n(C)][TY][BW], xb: [n(C^4)][TY][BW] (x halo), yb: [n(C^2)][TY+1][BW] (y halo)
+// Ghost points of a face tile, computed into its staged neighbour boxes (ghost_fill's arithmetic).
+// A class even along an axis reads, at the faces of that axis, a ghost point of the switched class;
+// its value depends on the target's values at the face cell (target box) and on the switched
+// class's first interior point (neighbour box), both staged.  No other tile reads these ghosts, so
+// they are never written to memory.  All threads call this; the caller syncs before reading.
+//   own: [n(C)][TY][TX], xb: [n(C^4)][TY][BW] (from x0 - 4), yb: [n(C^2)][TY+1][BW]
 template <int N, int C, int KIND>
 __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, const float* own,
                                             float* xb, float* yb, double bc) {
   constexpr bool ADJ = KIND == 1;
   constexpr int nt = Ord<N>::n(C);
-  const int xo = tt.ext >> 16;
-  const int ex = tt.ext & 255, ey = (tt.ext >> 8) & 255;
+  const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
   const double bc_scaled = bc * S.scale_g;
   if constexpr (!((C >> 2) & 1)) {   // even in x: ghosts of C ^ 4 at x = 0 and x = n_C
     constexpr int F = C ^ 4;
@@ -289,19 +324,19 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
       const double* B = ADJ ? I.bmat_a[0][F] : I.bmat_f[0][F];
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
-        if (left ? tt.x0 != 0 : tt.x0 + ex != ncx) continue;
-        // a face tile: the boundary blocks and the beam face come from the full descriptor
-        // columns (the own and halo boxes start at the same xa = x0 - xo): the face cell, F's
-        // ghost (index 0 on the left, n_C on the right), F's first interior point (1, n_C - 1)
-        const int cc = left ? xo : ex - 1 + xo;
-        const int gcol = left ? xo : ex + xo;
-        const int icol = left ? xo + 1 : ex + xo - 1;
+        if (left ? tt.x0 != 0 : tt.x0 + xv1 != ncx) continue;
+        // a face tile: the boundary blocks and the beam face come from the full descriptor.
+        // Columns: the face cell in the target box; F's ghost (index 0 / n_C) and first interior
+        // point (1 / n_C - 1) in the neighbour box, which starts at x0 - 4
+        const int cc = left ? 0 : ncx - 1 - tt.x0;
+        const int gcol = left ? XO : ncx - tt.x0 + XO;
+        const int icol = left ? XO + 1 : ncx - 1 - tt.x0 + XO;
         const bool src = !ADJ && !left;
         for (int w = threadIdx.x; w < ey * nf; w += BLOCK) {
           const int ty = w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
-          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PL4 + ty * BW + cc], bv);
+          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + ty * TX + cc], bv);
           const int j = tt.y0 + ty;
           const float gval = src ? float(I.beam[F][(long long)j * nf + r] * bc_scaled) : 0.0f;
           const float interior = xb[r * PL4 + ty * BW + icol];
@@ -316,26 +351,28 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
     if constexpr (nt > 0 && nf > 0) {
       const int ncy = S.n1[C];
       const double* B = ADJ ? I.bmat_a[1][F] : I.bmat_f[1][F];
+      const int nx = xv1 - xv0;
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
         if (left ? tt.y0 != 0 : tt.y0 + ey != ncy) continue;
-        const int crow = left ? 0 : ey - 1;   // the face cells' row in the own box
+        const int crow = left ? 0 : ey - 1;   // the face cells' row in the target box
         const int grow = left ? 0 : ey;       // the ghost row in the y box
         const int irow = left ? 1 : ey - 1;   // the first interior row of F
-        for (int w = threadIdx.x; w < ex * nf; w += BLOCK) {
-          const int tx = w % ex, r = w / ex;
+        for (int w = threadIdx.x; w < nx * nf; w += BLOCK) {
+          const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
-          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PL4 + crow * BW + tx + xo], bv);
-          const float interior = yb[r * PL5 + irow * BW + tx + xo];
-          yb[r * PL5 + grow * BW + tx + xo] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
+          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + crow * TX + tx], bv);
+          const float interior = yb[r * PL5 + irow * BW + tx + XO];
+          yb[r * PL5 + grow * BW + tx + XO] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
         }
       }
     }
   }
 }
 
-// One cell of a staged tile: substep_cell's arithmetic with operands from shared memory.
+// One cell of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
+// values replace the old ones in the target box.
 template <int N, int C, bool ADJ>
 __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                          double (&red)[BLOCK / 32][MAXR]) {
@@ -343,21 +380,20 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
+  float* own = reinterpret_cast<float*>(st + LY::OWN);
   {
     const ArgRow<N>& ar0 = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, ADJ ? 1 : 0>(L.inst[tt.inst], I, tt, reinterpret_cast<const float*>(st + LY::OWN),
-                                   reinterpret_cast<float*>(st + LY::XN), reinterpret_cast<float*>(st + LY::YN),
-                                   ADJ ? 0.0 : ar0.bc);
+    tile_ghosts<N, C, ADJ ? 1 : 0>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                                   reinterpret_cast<float*>(st + LY::YN), ADJ ? 0.0 : ar0.bc);
     __syncthreads();
   }
-  const float* own = reinterpret_cast<const float*>(st + LY::OWN);
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
   const ArgRow<N>& ar = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-  const int xo = tt.ext >> 16;
-  const bool valid = tx < (tt.ext & 255) && ty < ((tt.ext >> 8) & 255);
+  const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
+  const bool valid = tx >= xv0 && tx < xv1 && ty < ey;
   const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
   double part[MAXR];
 #pragma unroll
@@ -365,9 +401,9 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   if constexpr (n > 0) {
     if (valid) {
       const int i = tt.x0 + tx, j = tt.y0 + ty;
-      const int lo = ty * BW + tx + xo;                       // the cell in the own / density boxes
-      const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;         // x neighbours: i, i - 1 (odd) or i + 1, i
-      const int yr = (ty + 1) * BW + tx + xo, yl = yr - BW;    // rows j, j - 1 (odd) or j + 1, j of the y box
+      const int lo = ty * TX + tx;                              // the cell in the target / density boxes
+      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
+      const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;     // rows j, j - 1 (odd) or j + 1, j of the y box
       const float ihx = I.inv_h[0], ihy = I.inv_h[1];
       float acc[n];
 #pragma unroll
@@ -408,7 +444,7 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
       float S = 0.0f;
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
-        rr[e] = e < tt.ne ? rh[e * PL4 + lo] : 0.0f;
+        rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
         S = fmaf(rr[e], ar.s[e], S);
       }
       const float invS = recip(S);
@@ -438,24 +474,15 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
           q = q - ar.sig[r] * I.acs[ce * I.nr + r] * I.noa[ce * I.ne + I.xel[r]] * I.ibar[r];
         q0 = float(q);
       }
-      float* base;
-      if (ADJ) {
-        base = I.lam;
-      } else {
-        const bool segment = L.mode == BM_RECOMPUTE;
-        base = I.slots + (long long)slot_index(tt.ns, tt.n_ck, L.j, L.K, segment, L.j / L.K) * I.slot_elems;
-      }
-      float* un = base + I.dev_off[C] + (long long)j * I.px[C] + i;
-      const long long ms = I.ms[C];
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
-        const float u = own[m * PL4 + lo];
+        const float u = own[m * PLO + lo];
         const float q = (m == 0) ? q0 : 0.0f;
         const float num = (q - acc[m]) - Cl[l] * u;
         const float du = num * invS * ph[l];
         const float unew = u + dt * du;
-        un[m * ms] = unew;
+        own[m * PLO + lo] = unew;
         if constexpr (C == 0 && !ADJ) {
           if (m == 0 && want_part) {
 #pragma unroll
@@ -482,7 +509,18 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
       for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
       L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
     }
-    __syncthreads();
+  }
+  __syncthreads();   // the target box holds the new values
+  if (threadIdx.x == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const CUtensorMap* mp = L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS;
+    if (ADJ) {
+      tma_store_3d(mp + TM_LAM_T, tt.x0, tt.y0, 0, own);
+    } else {
+      const SubSlots sl = sub_slots(tt.ns, tt.n_ck, L.mode, L.j, L.sub, L.K);
+      tma_store_4d(mp + TM_ST_T, tt.x0, tt.y0, 0, sl.out, own);
+    }
+    bulk_commit();
   }
 }
 
@@ -511,11 +549,11 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       if (t < L.n_tiles) tma_issue<N, ADJ>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
     }
   for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
-    const int t = t0 + k * G;
     const int s = k % TSTAGES;
     const int ka = k + TSTAGES - 1;   // tile issued now, into the stage freed by iteration k - 1
     const int ta = t0 + ka * G;
     if (ta < L.n_tiles && threadIdx.x == 0) {
+      bulk_wait_read();   // the stores issued from that stage have read it
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_issue<N, ADJ>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
@@ -526,6 +564,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
         // let the copies still in flight land before the CTA's shared memory is released
         for (int kk = k; kk <= ka; ++kk)
           if (t0 + kk * G < L.n_tiles) mbar_wait_bounded(&full[kk % TSTAGES], (unsigned)((kk / TSTAGES) & 1));
+        bulk_wait_all();
       }
       __syncthreads();
       return;
@@ -538,8 +577,8 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
       case 4: tma_cell<N, 4, ADJ>(L, tt, st, red); break;
       default: tma_cell<N, 6, ADJ>(L, tt, st, red); break;
     }
-    __syncthreads();   // stage s is free for the loads issued in the next iteration
   }
+  if (threadIdx.x == 0) bulk_wait_all();   // every store of this CTA has landed
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -562,12 +601,12 @@ template <int N>
 struct TmaIntLayout {
   using B = TmaLayout<N>;
   static constexpr int OWN = 0;
-  static constexpr int LAM = OWN + B::al(B::NO * PL4 * 4);
-  static constexpr int XN = LAM + B::al(B::NO * PL4 * 4);
+  static constexpr int LAM = OWN + B::al(B::NO * PLO * 4);
+  static constexpr int XN = LAM + B::al(B::NO * PLO * 4);
   static constexpr int YN = XN + B::al(B::NXN * PL4 * 4);
   static constexpr int RHO = YN + B::al(B::NYN * PL5 * 4);
-  static constexpr int RBAR = RHO + B::al(MAXE * PL4 * 4);   // FP64
-  static constexpr int ARG = RBAR + B::al(MAXE * PL4 * 8);
+  static constexpr int RBAR = RHO + B::al(MAXE * PLO * 4);   // FP64
+  static constexpr int ARG = RBAR + B::al(MAXE * PLO * 8);
   static constexpr int TIL = ARG + (int)sizeof(IntRow<N>);
   static constexpr int SOL = TIL + (int)sizeof(TTile);
   static constexpr int STAGE = B::al(SOL + (int)sizeof(TSolve));
@@ -581,18 +620,18 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
-  const unsigned bytes = 4u * (unsigned)(2 * PL4 * n_own + PL4 * n_x + PL5 * n_y + PL4 * tt.ne) +
-                         8u * (unsigned)(PL4 * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
+  const unsigned bytes = 4u * (unsigned)(2 * PLO * n_own + PL4 * n_x + PL5 * n_y + PLO * tt.ne) +
+                         8u * (unsigned)(PLO * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
   const int ya = tt.y0 - ((c >> 1) & 1);
+  const int xa = tt.x0 - XO;
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
-  const int xa = tt.x0 - (tt.ext >> 16);
-  tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST4, xa, tt.y0, 0, slot, bar);
-  tma_load_3d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM4, xa, tt.y0, 0, bar);
-  if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST4, xa, tt.y0, 0, slot, bar);
-  if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST5, xa, ya, 0, slot, bar);
-  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, xa, tt.y0, 0, bar);
-  tma_load_3d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, xa, tt.y0, 0, bar);
+  tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, 0, slot, bar);
+  tma_load_3d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, 0, bar);
+  if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, 0, slot, bar);
+  if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, 0, slot, bar);
+  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, 0, bar);
+  tma_load_3d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, tt.x0, tt.y0, 0, bar);
   bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
@@ -604,108 +643,113 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
+  const float* own = reinterpret_cast<const float*>(st + LY::OWN);
+  double* rbs = reinterpret_cast<double*>(st + LY::RBAR);
   {
     const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, 2>(L.inst[tt.inst], I, tt, reinterpret_cast<const float*>(st + LY::OWN),
-                         reinterpret_cast<float*>(st + LY::XN), reinterpret_cast<float*>(st + LY::YN), ar0.bc);
+    tile_ghosts<N, C, 2>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                         reinterpret_cast<float*>(st + LY::YN), ar0.bc);
     __syncthreads();
   }
   if constexpr (n > 0) {
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
-    const int xo = tt.ext >> 16;
-    if (!(tx < (tt.ext & 255) && ty < ((tt.ext >> 8) & 255))) return;
-    const float* own = reinterpret_cast<const float*>(st + LY::OWN);
-    const float* lam = reinterpret_cast<const float*>(st + LY::LAM);
-    const float* xn = reinterpret_cast<const float*>(st + LY::XN);
-    const float* yn = reinterpret_cast<const float*>(st + LY::YN);
-    const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
-    const double* rbs = reinterpret_cast<const double*>(st + LY::RBAR);
-    const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    const int i = tt.x0 + tx, j = tt.y0 + ty;
-    const int lo = ty * BW + tx + xo;
-    const int xr = lo + (oddx ? 0 : 1), xl = xr - 1;
-    const int yr = (ty + 1) * BW + tx + xo, yl = yr - BW;
-    const float ihx = I.inv_h[0], ihy = I.inv_h[1];
-    float acc[n];
+    const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
+    if (tx >= xv0 && tx < xv1 && ty < ey) {
+      const float* lam = reinterpret_cast<const float*>(st + LY::LAM);
+      const float* xn = reinterpret_cast<const float*>(st + LY::XN);
+      const float* yn = reinterpret_cast<const float*>(st + LY::YN);
+      const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
+      const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
+      const int i = tt.x0 + tx, j = tt.y0 + ty;
+      const int lo = ty * TX + tx;
+      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
+      const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;
+      const float ihx = I.inv_h[0], ihy = I.inv_h[1];
+      float acc[n];
 #pragma unroll
-    for (int m = 0; m < n; ++m) acc[m] = 0.0f;
-    {
-      constexpr int F = C ^ 4;
-      if constexpr (Ord<N>::n(F) > 0) {
-        auto diff = [&](int q) -> float { return (xn[q * PL4 + xr] - xn[q * PL4 + xl]) * ihx; };
-        auto coef = [&](int kk, double lit) -> float {
-          (void)kk;
-          return float(lit);
-        };
-        Adv<N, C, 0>::template apply<float>(acc, diff, coef);
+      for (int m = 0; m < n; ++m) acc[m] = 0.0f;
+      {
+        constexpr int F = C ^ 4;
+        if constexpr (Ord<N>::n(F) > 0) {
+          auto diff = [&](int q) -> float { return (xn[q * PL4 + xr] - xn[q * PL4 + xl]) * ihx; };
+          auto coef = [&](int kk, double lit) -> float {
+            (void)kk;
+            return float(lit);
+          };
+          Adv<N, C, 0>::template apply<float>(acc, diff, coef);
+        }
+      }
+      {
+        constexpr int F = C ^ 2;
+        if constexpr (Ord<N>::n(F) > 0) {
+          auto diff = [&](int q) -> float { return (yn[q * PL5 + yr] - yn[q * PL5 + yl]) * ihy; };
+          auto coef = [&](int kk, double lit) -> float {
+            (void)kk;
+            return float(lit);
+          };
+          Adv<N, C, 1>::template apply<float>(acc, diff, coef);
+        }
+      }
+      float rr[MAXE];
+      float S = 0.0f;
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
+        S = fmaf(rr[e], ar.s[e], S);
+      }
+      const float invS = recip(S);
+      constexpr unsigned mask = Ord<N>::deg_mask(C);
+      float Cl[N + 1];
+#pragma unroll
+      for (int l = 0; l <= N; ++l) {
+        float cc = 0.0f;
+        if ((mask >> l) & 1u) {
+#pragma unroll
+          for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
+        }
+        Cl[l] = cc;
+      }
+      float P = 0.0f;
+      float R[N + 1];
+#pragma unroll
+      for (int l = 0; l <= N; ++l) R[l] = 0.0f;
+#pragma unroll
+      for (int m = 0; m < n; ++m) {
+        const int l = degree_of<N, C>(m);
+        const float u = own[m * PLO + lo];
+        const float lm = lam[m * PLO + lo];
+        const float du = (-acc[m] - Cl[l] * u) * invS;
+        P = fmaf(lm, du, P);
+        R[l] = fmaf(lm, u, R[l]);
+      }
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        if (e < tt.ne) {
+          double v = double(ar.s[e]) * double(P);
+#pragma unroll
+          for (int l = 0; l <= N; ++l)
+            if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
+          const double old = rbs[e * PLO + lo];   // this cell's rho_bar, staged with the tile
+          rbs[e * PLO + lo] = old + v * ar.wfac;
+        }
+      }
+      if constexpr (C == 0) {
+        const long long ce = (long long)j * I.n0[0] + i;
+        const double u0 = double(own[lo]);
+        for (int r = 0; r < I.nr; ++r) {
+          const double cr = ar.coef[r] * I.ibar[r];
+          const int el = I.xel[r];
+          I.acs_bar[ce * I.nr + r] += I.noa[ce * I.ne + el] * u0 * cr;
+          I.noa_bar[ce * I.ne + el] += I.acs[ce * I.nr + r] * u0 * cr;
+        }
       }
     }
-    {
-      constexpr int F = C ^ 2;
-      if constexpr (Ord<N>::n(F) > 0) {
-        auto diff = [&](int q) -> float { return (yn[q * PL5 + yr] - yn[q * PL5 + yl]) * ihy; };
-        auto coef = [&](int kk, double lit) -> float {
-          (void)kk;
-          return float(lit);
-        };
-        Adv<N, C, 1>::template apply<float>(acc, diff, coef);
-      }
-    }
-    float rr[MAXE];
-    float S = 0.0f;
-#pragma unroll
-    for (int e = 0; e < MAXE; ++e) {
-      rr[e] = e < tt.ne ? rh[e * PL4 + lo] : 0.0f;
-      S = fmaf(rr[e], ar.s[e], S);
-    }
-    const float invS = recip(S);
-    constexpr unsigned mask = Ord<N>::deg_mask(C);
-    float Cl[N + 1];
-#pragma unroll
-    for (int l = 0; l <= N; ++l) {
-      float cc = 0.0f;
-      if ((mask >> l) & 1u) {
-#pragma unroll
-        for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
-      }
-      Cl[l] = cc;
-    }
-    float P = 0.0f;
-    float R[N + 1];
-#pragma unroll
-    for (int l = 0; l <= N; ++l) R[l] = 0.0f;
-#pragma unroll
-    for (int m = 0; m < n; ++m) {
-      const int l = degree_of<N, C>(m);
-      const float u = own[m * PL4 + lo];
-      const float lm = lam[m * PL4 + lo];
-      const float du = (-acc[m] - Cl[l] * u) * invS;
-      P = fmaf(lm, du, P);
-      R[l] = fmaf(lm, u, R[l]);
-    }
-    double* rb = I.rbar[C] + (long long)j * I.px[C] + i;
-    const long long ms = I.ms[C];
-#pragma unroll
-    for (int e = 0; e < MAXE; ++e) {
-      if (e < tt.ne) {
-        double v = double(ar.s[e]) * double(P);
-#pragma unroll
-        for (int l = 0; l <= N; ++l)
-          if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
-        const double old = rbs[e * PL4 + lo];   // this cell's rho_bar, staged with the tile
-        rb[e * ms] = old + v * ar.wfac;
-      }
-    }
-    if constexpr (C == 0) {
-      const long long ce = (long long)j * I.n0[0] + i;
-      const double u0 = double(own[lo]);
-      for (int r = 0; r < I.nr; ++r) {
-        const double cr = ar.coef[r] * I.ibar[r];
-        const int el = I.xel[r];
-        I.acs_bar[ce * I.nr + r] += I.noa[ce * I.ne + el] * u0 * cr;
-        I.noa_bar[ce * I.ne + el] += I.acs[ce * I.nr + r] * u0 * cr;
-      }
-    }
+  }
+  __syncthreads();   // the rho_bar box holds the new values
+  if (threadIdx.x == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma_store_3d(L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS + TM_RBAR, tt.x0, tt.y0, 0, rbs);
+    bulk_commit();
   }
 }
 
@@ -731,11 +775,11 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       if (t < L.n_tiles) tma_issue_int<N>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
     }
   for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
-    const int t = t0 + k * G;
     const int s = k % TSTAGES;
     const int ka = k + TSTAGES - 1;
     const int ta = t0 + ka * G;
     if (ta < L.n_tiles && threadIdx.x == 0) {
+      bulk_wait_read();
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_issue_int<N>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
@@ -745,6 +789,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
         atomicExch(L.status, (int)PN_ERR_TIMEOUT);
         for (int kk = k; kk <= ka; ++kk)
           if (t0 + kk * G < L.n_tiles) mbar_wait_bounded(&full[kk % TSTAGES], (unsigned)((kk / TSTAGES) & 1));
+        bulk_wait_all();
       }
       __syncthreads();
       return;
@@ -757,8 +802,8 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
       case 4: tma_int_cell<N, 4>(L, tt, st); break;
       default: tma_int_cell<N, 6>(L, tt, st); break;
     }
-    __syncthreads();
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // ---------------------------------------------------------------------------------------------
