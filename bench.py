@@ -460,7 +460,7 @@ def run_ours(args):
                              "forward_roofline": {"bound": "hbm", "achieved": fp32_fwd_gbs, "peak": peak,
                                                   "unit": "GB/s", "frac": fp32_fwd_gbs / peak,
                                                   "peak_source": peak_source,
-                                                  "kernel": "batch_tma2d_kernel<11> (with its ghost kernels), forward sweep",
+                                                  "kernel": "batch_tma2d_kernel<11>, forward sweep",
                                                   "note": "algorithmic bytes of all forward sub-steps of the 60 solves / forward time"},
                              "kernels_per_step": binfo.forward_kernels + binfo.adjoint_kernels,
                              "form": "one pn_batch: one launch per sub-step covers all 60 solves"},

@@ -152,6 +152,8 @@ struct BSub {
   double sig_src[MAXR];
   const double* wint;
   T inv_h[3];
+  T* cache[8];        // unused by the batched kernels (cache_mode 0)
+  int cache_mode;
 };
 
 template <class T, int N>
@@ -250,6 +252,7 @@ __device__ __forceinline__ void fill_sub(BSub<T, N>& a, const BInst<T>& I, const
     a.ibar = I.ibar;
     a.wint = I.wint;
     a.adjoint_source = ADJ ? 1 : 0;
+    a.cache_mode = 0;
     a.bc = ADJ ? 0.0 : I.fwd_bc[row];
     for (int r = 0; r < MAXR; ++r) a.xel[r] = I.xel[r];
   } else if (tid >= 16 && tid < 16 + MAXR) {

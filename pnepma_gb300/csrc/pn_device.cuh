@@ -88,6 +88,10 @@ struct SubArgs {
   // intensity partial sums of the new eee moment 0 (forward, even sub-step)
   const double* wint;         // [cell][r] = ACS * NOA
   double* partial;            // [block][r]
+  // right-hand-side factors of the odd classes, shared by the two half sub-steps of one step
+  // (same coefficients, densities and dt): planes 1/S, C_0..C_N, phi1_0..phi1_N per class
+  T* cache[8];
+  int cache_mode;             // 0 none, 1 compute and store, 2 load
   Seg seg[MAXSEG];
   T tab[Ord<N>::n_tab];       // advection nnz values divided by the grid step
 };
@@ -407,29 +411,51 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
     for (int m = 0; m < n; ++m) acc[m] = T(0);
     advection_sum<T, N, C, ADJ, LIT, DIMS>(acc, a, rd, i, j, k);
 
-    const T* rho = a.rho[C] + p;
-    T rr[MAXE];
-    T S = T(0);
-#pragma unroll
-    for (int e = 0; e < MAXE; ++e) {
-      rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
-      S = fma(rr[e], a.s[e], S);
-    }
-    const T invS = recip(S);
     constexpr unsigned mask = Ord<N>::deg_mask(C);
+    T invS;
     T Cl[N + 1];
     T ph[N + 1];
+    if (a.cache_mode == 2) {
+      // the first half sub-step of this energy step left the factors of this cell
+      const T* cp = a.cache[C] + p;
 #pragma unroll
-    for (int l = 0; l <= N; ++l) {
-      if ((mask >> l) & 1u) {
-        T cc = T(0);
+      for (int l = 0; l <= N; ++l) {
+        Cl[l] = ((mask >> l) & 1u) ? cp[(1 + l) * gt.ms] : T(0);
+        ph[l] = ((mask >> l) & 1u) ? cp[(2 + N + l) * gt.ms] : T(1);
+      }
+      invS = cp[0];
+    } else {
+      const T* rho = a.rho[C] + p;
+      T rr[MAXE];
+      T S = T(0);
 #pragma unroll
-        for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
-        Cl[l] = cc;
-        ph[l] = phi1(-cc * invS * a.dt);
-      } else {
-        Cl[l] = T(0);
-        ph[l] = T(1);
+      for (int e = 0; e < MAXE; ++e) {
+        rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
+        S = fma(rr[e], a.s[e], S);
+      }
+      invS = recip(S);
+#pragma unroll
+      for (int l = 0; l <= N; ++l) {
+        if ((mask >> l) & 1u) {
+          T cc = T(0);
+#pragma unroll
+          for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
+          Cl[l] = cc;
+          ph[l] = phi1(-cc * invS * a.dt);
+        } else {
+          Cl[l] = T(0);
+          ph[l] = T(1);
+        }
+      }
+      if (a.cache_mode == 1) {
+        T* cp = a.cache[C] + p;
+        cp[0] = invS;
+#pragma unroll
+        for (int l = 0; l <= N; ++l)
+          if ((mask >> l) & 1u) {
+            cp[(1 + l) * gt.ms] = Cl[l];
+            cp[(2 + N + l) * gt.ms] = ph[l];
+          }
       }
     }
     const T* uo = a.rd[C] + p;

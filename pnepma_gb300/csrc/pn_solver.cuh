@@ -74,6 +74,8 @@ class Solver : public SolverBase {
   T* slots = nullptr;
   T* lam = nullptr;
   T* sstate = nullptr;      // state of the pn_step interface
+  T* cache_d = nullptr;     // right-hand-side factors of the odd classes (see launch_substep)
+  T* cache_cls[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   T* rho_d = nullptr;
   double* rbar_d = nullptr;
   double* noa_d = nullptr;
@@ -283,6 +285,21 @@ class Solver : public SolverBase {
     if ((rc = alloc(bf_d, L.n_bnd))) return rc;
     if ((rc = alloc(ba_d, L.n_bnd))) return rc;
     if ((rc = alloc(beam_d, std::max<long long>(L.n_beam, 1)))) return rc;
+    {
+      // factor cache of the odd classes: planes 1/S, C_0..C_N, phi1_0..phi1_N with each class's geometry
+      long long n_cache = 0;
+      for (int cl = 0; cl < 8; ++cl)
+        if (L.active[cl] && class_parity(cl) == 1) n_cache += (long long)(2 * N + 3) * L.ms[cl];
+      if (n_cache > 0) {
+        if ((rc = alloc(cache_d, n_cache))) return rc;
+        long long o = 0;
+        for (int cl = 0; cl < 8; ++cl)
+          if (L.active[cl] && class_parity(cl) == 1) {
+            cache_cls[cl] = cache_d + o;
+            o += (long long)(2 * N + 3) * L.ms[cl];
+          }
+      }
+    }
     if ((rc = alloc(xel_d, std::max(nr, 1)))) return rc;
     if ((rc = alloc(stage_d, std::max(L.n_rho, L.n_state)))) return rc;
     if ((rc = alloc(flag_d, 1))) return rc;
@@ -413,7 +430,7 @@ class Solver : public SolverBase {
   // one sub-step for the classes of parity `par`; own_rd/own_wr are the target slot pointers, from_rd
   // the slot holding the other parity
   int launch_substep(int par, bool adj, double dt, const double* s, const double* c, double bc, T* own_rd,
-                     T* own_wr, T* from_rd, double* partial, const double* sig_src) {
+                     T* own_wr, T* from_rd, double* partial, const double* sig_src, int cache_mode = 0) {
     SubArgs<T, N> a;
     std::memset(&a, 0, sizeof(a));
     common_geom(a.g);
@@ -449,6 +466,8 @@ class Solver : public SolverBase {
     a.adjoint_source = (adj && sig_src != nullptr) ? 1 : 0;
     a.wint = wint_d;
     a.partial = partial;
+    a.cache_mode = (par == 1 && cache_d != nullptr) ? cache_mode : 0;
+    for (int cl = 0; cl < 8; ++cl) a.cache[cl] = cache_cls[cl];
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
     const int nb = nblk_par[par];
     if (adj)
@@ -510,10 +529,12 @@ class Solver : public SolverBase {
     const double bc = fwd_bc[i - 1];
     const double dt2 = dE / 2;
     int rc;
-    if ((rc = launch_substep(1, false, dt2, s, c, bc, src, dst, src, nullptr, nullptr))) return rc;
+    // the two half sub-steps share coefficients, densities and dt: the first stores the
+    // right-hand-side factors of the odd classes, the second loads them
+    if ((rc = launch_substep(1, false, dt2, s, c, bc, src, dst, src, nullptr, nullptr, 1))) return rc;
     double* part = with_partial ? partial_d + (long long)i * nblk_par[0] * L.nr : nullptr;
     if ((rc = launch_substep(0, false, dE, s, c, bc, src, dst, dst, part, nullptr))) return rc;
-    if ((rc = launch_substep(1, false, dt2, s, c, bc, dst, dst, dst, nullptr, nullptr))) return rc;
+    if ((rc = launch_substep(1, false, dt2, s, c, bc, dst, dst, dst, nullptr, nullptr, 2))) return rc;
     return PN_OK;
   }
 
@@ -524,9 +545,9 @@ class Solver : public SolverBase {
     const double* sg = adj_src_sigma.data() + (long long)j * L.nr;
     const double dt2 = dE / 2;
     int rc;
-    if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg))) return rc;
+    if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 1))) return rc;
     if ((rc = launch_substep(0, true, dE, s, c, 0.0, lam, lam, lam, nullptr, sg))) return rc;
-    if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg))) return rc;
+    if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 2))) return rc;
     return PN_OK;
   }
 
