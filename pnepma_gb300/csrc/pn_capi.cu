@@ -2,7 +2,10 @@
 // No C++ exception and no abort crosses this boundary: every entry point returns a pn_status.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -10,6 +13,7 @@
 #include "generated/pn_orders.h"
 #include "pn_layout.h"
 #include "pn_solver_base.h"
+#include "pn_tape_pool.h"
 
 namespace pn {
 
@@ -46,6 +50,20 @@ static thread_local std::string g_last_error;
 
 namespace pn {
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+TapePool& tape_pool(int device) {
+  static std::mutex mu;
+  static std::map<int, TapePool*> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  TapePool*& p = pools[device];
+  if (!p) p = new TapePool;   // lives until the process exits
+  return *p;
+}
+
+unsigned long long next_handle_id() {
+  static std::atomic<unsigned long long> id{0};
+  return ++id;
+}
 }  // namespace pn
 
 static int fail(const std::string& msg, int code) {

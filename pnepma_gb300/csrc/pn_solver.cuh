@@ -18,6 +18,7 @@
 
 #include "pn_device.cuh"
 #include "pn_layout.h"
+#include "pn_tape_pool.h"
 #include "pn_solver_base.h"
 #include "pn_util.cuh"
 
@@ -110,12 +111,89 @@ class Solver : public SolverBase {
   cudaGraphExec_t g_fwd = nullptr, g_adj = nullptr;
   bool have_forward = false;
   bool have_state = false;
+  // full tape in the device's shared tape buffer (pn_tape_pool.h) instead of own checkpoints
+  bool pool_user = false;
+  int device = 0;
+  unsigned long long hid = 0;          // this handle's id
+  unsigned long long pool_epoch = 0;   // buffer address the graphs were captured with
+  unsigned long long my_gen = 0;       // generation of this handle's last recorded tape
 
   ~Solver() override {
     if (g_fwd) cudaGraphExecDestroy(g_fwd);
     if (g_adj) cudaGraphExecDestroy(g_adj);
+    if (pool_user) {
+      TapePool& P = tape_pool(device);
+      std::lock_guard<std::mutex> lk(P.mu);
+      if (P.owner == hid) P.owner = 0;
+      if (--P.users == 0 && P.base) {
+        if (P.last) cudaEventSynchronize(P.last);
+        cudaFree(P.base);
+        P.base = nullptr;
+        P.bytes = 0;
+        ++P.epoch;
+        P.owner = 0;
+      }
+    }
     if (stream) cudaStreamDestroy(stream);
     for (void* p : allocs) cudaFree(p);
+  }
+
+  // With the pool lock held: point `slots` at a buffer that holds this handle's full tape,
+  // growing it if needed; re-capture the graphs when the address changed.  Returns false when
+  // the tape does not fit (the handle then checkpoints with its own slots).
+  bool pool_acquire(TapePool& P) {
+    const size_t need = (size_t)(n_ck + n_work) * (size_t)L.slot_elems * sizeof(T);
+    if (P.bytes < need) {
+      if (P.base) {
+        if (P.last) cudaEventSynchronize(P.last);
+        cudaFree(P.base);
+        P.base = nullptr;
+        P.bytes = 0;
+        ++P.epoch;
+        P.owner = 0;
+      }
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess || need > fr / 10 * 8) {
+        cudaGetLastError();
+        return false;
+      }
+      void* q = nullptr;
+      if (cudaMalloc(&q, need) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      P.base = (char*)q;
+      P.bytes = need;
+      ++P.epoch;
+      P.owner = 0;
+    }
+    if (!P.last && cudaEventCreateWithFlags(&P.last, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (pool_epoch != P.epoch) {
+      slots = (T*)P.base;
+      if (g_fwd) { cudaGraphExecDestroy(g_fwd); g_fwd = nullptr; }
+      if (g_adj) { cudaGraphExecDestroy(g_adj); g_adj = nullptr; }
+      pool_epoch = P.epoch;
+    }
+    return true;
+  }
+
+  // leave the pool for good: own checkpoints every ceil(sqrt(n_steps)) states
+  int pool_leave(TapePool& P) {
+    pool_user = false;
+    --P.users;
+    if (P.owner == hid) P.owner = 0;
+    K = std::max(2, (int)std::ceil(std::sqrt((double)L.ns)));
+    if (K > L.ns) K = L.ns;
+    n_ck = L.ns / K + 1 + ((L.ns % K) ? 1 : 0);
+    n_work = std::max(2, K - 1);
+    if (g_fwd) { cudaGraphExecDestroy(g_fwd); g_fwd = nullptr; }
+    if (g_adj) { cudaGraphExecDestroy(g_adj); g_adj = nullptr; }
+    int rc;
+    if ((rc = alloc(slots, (long long)(n_ck + n_work) * L.slot_elems))) return rc;
+    return PN_OK;
   }
 
   long long device_bytes() const override { return bytes; }
@@ -243,8 +321,10 @@ class Solver : public SolverBase {
     K = d->checkpoint_stride;
     if (K < 0) { err = "checkpoint_stride must be >= 0"; return PN_ERR_INVALID; }
     if (K == 0) {
+      // a full tape up to 2 GiB of its own; beyond, a full tape in the device's shared buffer
       const long long budget = 2LL << 30;
-      K = ((long long)(ns + 1) * slot_bytes <= budget) ? 1 : std::max(2, (int)std::ceil(std::sqrt((double)ns)));
+      K = 1;
+      if ((long long)(ns + 1) * slot_bytes > budget) pool_user = true;
     }
     if (K > ns) K = ns;
     n_ck = ns / K + 1 + ((ns % K) ? 1 : 0);
@@ -264,9 +344,17 @@ class Solver : public SolverBase {
       err = "cudaStreamCreate failed";
       return PN_ERR_CUDA;
     }
-    // allocations
+    // allocations (a pool user takes its tape from the shared buffer at its first forward)
     const int nslots = n_ck + n_work;
-    if ((rc = alloc(slots, (long long)nslots * L.slot_elems))) return rc;
+    PN_CUDA(cudaGetDevice(&device));
+    hid = next_handle_id();
+    if (pool_user) {
+      TapePool& P = tape_pool(device);
+      std::lock_guard<std::mutex> lk(P.mu);
+      ++P.users;
+    } else if ((rc = alloc(slots, (long long)nslots * L.slot_elems))) {
+      return rc;
+    }
     if ((rc = alloc(lam, L.slot_elems))) return rc;
     if ((rc = alloc(sstate, L.slot_elems))) return rc;
     if ((rc = alloc(rho_d, L.rho_elems))) return rc;
@@ -304,7 +392,7 @@ class Solver : public SolverBase {
     if ((rc = alloc(stage_d, std::max(L.n_rho, L.n_state)))) return rc;
     if ((rc = alloc(flag_d, 1))) return rc;
     if ((rc = alloc(out_mul_d, 1))) return rc;
-    PN_CUDA(cudaMemsetAsync(slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems, stream));
+    if (!pool_user) PN_CUDA(cudaMemsetAsync(slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems, stream));
     PN_CUDA(cudaMemsetAsync(sstate, 0, sizeof(T) * (size_t)L.slot_elems, stream));
     PN_CUDA(cudaMemsetAsync(rho_d, 0, sizeof(T) * (size_t)L.rho_elems, stream));
     PN_CUDA(cudaMemcpyAsync(bf_d, d->boundary_fwd, sizeof(double) * L.n_bnd, cudaMemcpyHostToDevice, stream));
@@ -328,8 +416,10 @@ class Solver : public SolverBase {
     }
     if ((rc = build_segments())) return rc;
     PN_CUDA(cudaStreamSynchronize(stream));
-    if ((rc = capture(g_fwd, true))) return rc;
-    if ((rc = capture(g_adj, false))) return rc;
+    if (!pool_user) {
+      if ((rc = capture(g_fwd, true))) return rc;
+      if ((rc = capture(g_adj, false))) return rc;
+    }
     return PN_OK;
   }
 
@@ -599,6 +689,7 @@ class Solver : public SolverBase {
   int capture(cudaGraphExec_t& exec, bool fwd) {
     cudaGraph_t graph = nullptr;
     n_launch = 0;
+    PN_CUDA(cudaStreamSynchronize(stream));   // no earlier work pending on the capture stream
     PN_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     int rc = fwd ? record_forward() : record_adjoint();
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
@@ -637,11 +728,64 @@ class Solver : public SolverBase {
     return PN_OK;
   }
 
+  // The forward graph on stream s; a pool user records its tape into the shared buffer after the
+  // previous user of the buffer is done with it.
+  int launch_forward_graph(cudaStream_t s) {
+    int rc;
+    if (pool_user) {
+      TapePool& P = tape_pool(device);
+      std::unique_lock<std::mutex> lk(P.mu);
+      if (!pool_acquire(P)) {
+        if ((rc = pool_leave(P))) return rc;
+      } else {
+        if (!g_fwd && (rc = capture(g_fwd, true))) return rc;
+        PN_CUDA(cudaStreamWaitEvent(s, P.last, 0));
+        P.owner = hid;
+        my_gen = ++P.gen;
+        PN_CUDA(cudaGraphLaunch(g_fwd, s));
+        PN_CUDA(cudaEventRecord(P.last, s));
+        return PN_OK;
+      }
+    }
+    if (!g_fwd && (rc = capture(g_fwd, true))) return rc;
+    PN_CUDA(cudaGraphLaunch(g_fwd, s));
+    return PN_OK;
+  }
+
+  // The adjoint graph on stream s; a pool user whose tape was overwritten by another handle (or
+  // lost when the buffer grew) first records it again with its forward graph.
+  int launch_adjoint_graph(cudaStream_t s) {
+    int rc;
+    if (pool_user) {
+      TapePool& P = tape_pool(device);
+      std::unique_lock<std::mutex> lk(P.mu);
+      if (!pool_acquire(P)) {
+        if ((rc = pool_leave(P))) return rc;
+        lk.unlock();
+        if ((rc = launch_forward_graph(s))) return rc;
+      } else {
+        if (!g_fwd && (rc = capture(g_fwd, true))) return rc;
+        if (!g_adj && (rc = capture(g_adj, false))) return rc;
+        PN_CUDA(cudaStreamWaitEvent(s, P.last, 0));
+        if (P.owner != hid || P.gen != my_gen) {
+          P.owner = hid;
+          my_gen = ++P.gen;
+          PN_CUDA(cudaGraphLaunch(g_fwd, s));
+        }
+        PN_CUDA(cudaGraphLaunch(g_adj, s));
+        PN_CUDA(cudaEventRecord(P.last, s));
+        return PN_OK;
+      }
+    }
+    if (!g_adj && (rc = capture(g_adj, false))) return rc;
+    PN_CUDA(cudaGraphLaunch(g_adj, s));
+    return PN_OK;
+  }
+
   int forward(const double* rho, const double* noa, const double* acs, double* I, cudaStream_t st,
               bool dev) override {
     int rc;
     if (!rho || !noa || !acs || (L.nr && !I)) { err = "NULL buffer"; return PN_ERR_INVALID; }
-    if (!g_fwd && (rc = capture(g_fwd, true))) return rc;
     cudaStream_t s = st ? st : stream;
     if ((rc = load_rho(rho, dev, s))) return rc;
     const long long ncell = L.n_eee_cells;
@@ -652,7 +796,7 @@ class Solver : public SolverBase {
       wint_kernel<<<grid_for(ncell * L.nr), 256, 0, s>>>(acs_d, noa_d, xel_d, wint_d, ncell, L.nr, L.ne);
       PN_CUDA(cudaGetLastError());
     }
-    PN_CUDA(cudaGraphLaunch(g_fwd, s));
+    if ((rc = launch_forward_graph(s))) return rc;
     if (L.nr) {
       PN_CUDA(cudaMemcpyAsync(I, I_d, sizeof(double) * L.nr, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
     }
@@ -672,7 +816,6 @@ class Solver : public SolverBase {
     int rc;
     if (!have_forward) { err = "pn_adjoint needs a preceding pn_forward on this handle"; return PN_ERR_STATE; }
     if ((L.nr && !ibar) || !rho_bar || !noa_bar || (L.nr && !acs_bar)) { err = "NULL buffer"; return PN_ERR_INVALID; }
-    if (!g_adj && (rc = capture(g_adj, false))) return rc;
     cudaStream_t s = st ? st : stream;
     double* mul_d = out_mul_d;
     if (L.nr) {
@@ -690,7 +833,7 @@ class Solver : public SolverBase {
       const double one = 1.0 / scale_g;
       PN_CUDA(cudaMemcpyAsync(mul_d, &one, sizeof(double), cudaMemcpyHostToDevice, s));
     }
-    PN_CUDA(cudaGraphLaunch(g_adj, s));
+    if ((rc = launch_adjoint_graph(s))) return rc;
     // rho_bar to the caller layout (zeros on ghost points and inactive classes)
     PN_CUDA(cudaMemsetAsync(stage_d, 0, sizeof(double) * (size_t)L.n_rho, s));
     for (int c = 0; c < 8; ++c) {

@@ -146,3 +146,31 @@ def test_fp32_against_fp64_oracle(gpu_lib, oracle):
     assert rel(nb, nb_o) < 1e-3
     assert rel(ab, ab_o) < 1e-3
     h.close()
+
+
+def test_shared_tape_buffer_gives_the_checkpointed_results(gpu_lib):
+    """Handles whose full tape exceeds 2 GiB keep it in the device's shared buffer.  Interleaving
+    two of them (the second forward overwrites the first tape before the first adjoint, which then
+    records it again) gives bit for bit the results of handles that checkpoint every 7 states."""
+    from pnepma_gb300 import workloads
+    solves = workloads.config2(n_positions=2, energies=(15.0,))
+    outs = {}
+    for label, stride in (("pool", 0), ("ck7", 7)):
+        hs, ins = [], []
+        for s in solves:
+            s.problem.checkpoint_stride = stride
+            d, k = s.problem.descriptor(s.x_rays)
+            h = capi.Handle(d, k)
+            assert h.info().checkpoint_stride == (1 if stride == 0 else 7)
+            hs.append(h)
+            ins.append(s.inputs())
+        I = [h.forward(*x) for h, x in zip(hs, ins)]
+        grads = [h.adjoint(1.0 / np.abs(Ii)) for h, Ii in zip(hs, I)]
+        outs[label] = (I, grads)
+        for h in hs:
+            h.close()
+    for a, b in zip(outs["pool"][0], outs["ck7"][0]):
+        assert np.array_equal(a, b)
+    for ga, gb in zip(outs["pool"][1], outs["ck7"][1]):
+        for x, y in zip(ga, gb):
+            assert np.array_equal(x, y)
