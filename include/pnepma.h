@@ -237,7 +237,11 @@ typedef struct pn_batch_options {
 enum pn_batch_flags {
   /* FP32 2D groups stage their box tiles with TMA unless this is set; the generic kernels give
      bit-identical results (for comparison and diagnosis) */
-  PN_BATCH_GENERIC_KERNELS = 1
+  PN_BATCH_GENERIC_KERNELS = 1,
+  /* issue the kernels of every sweep on the caller's stream instead of capturing the sweeps as
+     CUDA graphs at creation: cheaper for a batch that runs once (each call then launches ~3
+     kernels per energy step from the host) */
+  PN_BATCH_DIRECT_LAUNCH = 2
 };
 
 typedef struct pn_batch_info {

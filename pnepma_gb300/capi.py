@@ -28,6 +28,7 @@ class PnHandleInfo(ctypes.Structure):
 
 
 PN_BATCH_GENERIC_KERNELS = 1
+PN_BATCH_DIRECT_LAUNCH = 2
 
 
 class PnBatchOptions(ctypes.Structure):

@@ -18,6 +18,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -576,6 +579,7 @@ class BatchGroup : public BatchGroupBase {
   // FP32 2D: box tiles through the TMA kernel, face tiles through the generic one
   bool use_tma = false;
   std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
+  std::vector<double> checked_advection;   // coupling blocks already checked against the stencil
   std::vector<TTile> ttl[3];     // per list: 0 / 1 parity targets, 2 every class (density integral)
   std::vector<int> tend[3];   // per solve: end of its tiles (solve-major lists)
   TTile* dttl[3] = {nullptr, nullptr, nullptr};
@@ -586,15 +590,29 @@ class BatchGroup : public BatchGroupBase {
   void* drows = nullptr;
   int* dstatus = nullptr;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
+  // Creation never waits for the device: tables go up on `up`, whose event the first forward or
+  // adjoint waits on in stream order, and the tape / density zeroing is enqueued with the first
+  // forward; graphs are captured on `cap`, which has no work of its own.
+  cudaStream_t up = nullptr;
+  cudaEvent_t ev_up = nullptr;
+  // stream the recorded launches go to: `cap` while capturing the graphs, the caller's stream
+  // with PN_BATCH_DIRECT_LAUNCH (no graphs: a group run once, as a served wave is, gains nothing
+  // from them, and instantiating them can wait on the device)
+  cudaStream_t ls = nullptr;
+  bool direct = false;
+  std::vector<std::pair<void*, size_t>> zero_ranges;
+  bool zeroed = false;
 
   ~BatchGroup() override {
     if (gf) cudaGraphExecDestroy(gf);
     if (ga) cudaGraphExecDestroy(ga);
-    if (cap) {
+    if (up) {
       // arena ranges are reused at once: let uploads still in flight land first
-      if (arena) cudaStreamSynchronize(cap);
-      cudaStreamDestroy(cap);
+      if (arena) cudaStreamSynchronize(up);
+      cudaStreamDestroy(up);
     }
+    if (ev_up) cudaEventDestroy(ev_up);
+    if (cap) cudaStreamDestroy(cap);
     for (void* p : allocs) {
       if (arena) arena->free(p);
       else cudaFree(p);
@@ -612,7 +630,7 @@ class BatchGroup : public BatchGroupBase {
     return v;
   }
   int wait_created() override {
-    PN_CUDA(cudaStreamSynchronize(cap));
+    PN_CUDA(cudaGetLastError());   // launch-time errors only: creation enqueues, it does not wait
     return PN_OK;
   }
 
@@ -640,12 +658,53 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
+  // Small per-solve tables: bump-allocated from device chunks whose bytes are mirrored on the
+  // host and copied with one transfer per chunk when the group is complete (flush_staged), so a
+  // wave of hundreds of solves does not cost thousands of small transfers.
+  struct StageChunk {
+    char* dev;
+    std::vector<char> host;
+    size_t cap;
+  };
+  std::vector<StageChunk> stage_chunks;
+
+  template <class U>
+  int stage(U*& dst, const std::vector<U>& v) {
+    const size_t b = ((std::max<size_t>(v.size(), 1) * sizeof(U)) + 255) & ~(size_t)255;
+    if (stage_chunks.empty() || stage_chunks.back().host.size() + b > stage_chunks.back().cap) {
+      // chunks double from 64 KiB to 16 MiB: small groups stay small, large ones take few copies
+      const size_t prev = stage_chunks.empty() ? ((size_t)32 << 10) : stage_chunks.back().cap;
+      const size_t cap = std::max<size_t>(b, std::min<size_t>(2 * prev, (size_t)16 << 20));
+      char* d = nullptr;
+      int rc = alloc(d, (long long)cap);
+      if (rc) return rc;
+      stage_chunks.push_back(StageChunk{d, {}, cap});
+      stage_chunks.back().host.reserve(cap);
+    }
+    StageChunk& c = stage_chunks.back();
+    const size_t off = c.host.size();
+    c.host.resize(off + b, 0);
+    if (!v.empty()) std::memcpy(c.host.data() + off, v.data(), v.size() * sizeof(U));
+    dst = reinterpret_cast<U*>(c.dev + off);
+    return PN_OK;
+  }
+
+  int flush_staged() {
+    for (StageChunk& c : stage_chunks) {
+      // pageable source: the call returns once the bytes are staged, so the mirror may go
+      if (!c.host.empty()) PN_CUDA(cudaMemcpyAsync(c.dev, c.host.data(), c.host.size(), cudaMemcpyHostToDevice, up));
+      std::vector<char>().swap(c.host);
+    }
+    stage_chunks.clear();
+    return PN_OK;
+  }
+
   template <class U>
   int upload(U*& dst, const std::vector<U>& v) {
     int rc = alloc(dst, (long long)v.size());
     if (rc) return rc;
     // pageable source: the call returns once the data is staged, so temporaries may be passed
-    if (!v.empty()) PN_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, cap));
+    if (!v.empty()) PN_CUDA(cudaMemcpyAsync(dst, v.data(), sizeof(U) * v.size(), cudaMemcpyHostToDevice, up));
     return PN_OK;
   }
 
@@ -706,15 +765,25 @@ class BatchGroup : public BatchGroupBase {
     for (int q = 0; q < n; ++q) cur_descs[q] = d[members[q]];
     int rc;
     PN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    PN_CUDA(cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking));
+    PN_CUDA(cudaEventCreateWithFlags(&ev_up, cudaEventDisableTiming));
     {
       int dev = 0;
       PN_CUDA(cudaGetDevice(&dev));
       PN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     }
+    // PN_TRACE set in the environment: host time of each phase of the group's creation on stderr
+    const bool trace = std::getenv("PN_TRACE") != nullptr;
+    auto clk = [] { return std::chrono::steady_clock::now(); };
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    const auto t0 = clk();
     for (int q = 0; q < n; ++q) {
       std::memset(&hinst[q], 0, sizeof(BInst<T>));
       if ((rc = build_instance(q, d[members[q]]))) return rc;
     }
+    const auto t1 = clk();
     // partial slots: the eee tiles of list 0, numbered per solve in tile order
     n_ptiles = 0;
     pr = 1;
@@ -746,12 +815,28 @@ class BatchGroup : public BatchGroupBase {
     } else {
       (void)flags;
     }
+    const auto t2 = clk();
+    if ((rc = flush_staged())) return rc;
     if ((rc = upload(dinst, hinst))) return rc;
     if ((rc = alloc(dio, n))) return rc;
     if ((rc = alloc(partial, (long long)max_ns * std::max(n_ptiles, 1) * pr))) return rc;
-    PN_CUDA(cudaStreamSynchronize(cap));
-    if ((rc = capture(gf, true))) return rc;
-    if ((rc = capture(ga, false))) return rc;
+    PN_CUDA(cudaEventRecord(ev_up, up));
+    const auto t3 = clk();
+    direct = (flags & PN_BATCH_DIRECT_LAUNCH) != 0;
+    if (!direct) {
+      if ((rc = capture(gf, true))) return rc;
+      if ((rc = capture(ga, false))) return rc;
+    } else {
+      // count the launches of one sweep without issuing them
+      nl = 0;
+      nl_f = nl_a = 0;
+    }
+    if (trace) {
+      const auto t4 = clk();
+      std::fprintf(stderr, "[pn] group N=%d dims=%d solves=%d tma=%d: instances %.1f ms, lists+maps %.1f ms, "
+                   "uploads %.1f ms, graphs %.1f ms (%lld + %lld launches)\n",
+                   N, DIMS, n, use_tma ? 1 : 0, ms(t0, t1), ms(t1, t2), ms(t2, t3), ms(t3, t4), nl_f, nl_a);
+    }
     return PN_OK;
   }
 
@@ -899,7 +984,7 @@ class BatchGroup : public BatchGroupBase {
       }
       if ((rc = upload(dsolves, hs))) return rc;
       if ((rc = alloc(dstatus, 1))) return rc;
-      PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), cap));
+      PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), up));
       // tiles over every target cell per list; partial slots are the eee tiles of list 0 in tile order
       n_ptiles = 0;
       for (int q = 0; q < n; ++q) {
@@ -990,7 +1075,7 @@ class BatchGroup : public BatchGroupBase {
     const int nslots = 1 + I.n_ck + n_work_for(K);
     if ((rc = alloc(I.slots, (long long)nslots * L.slot_elems))) return rc;
     if ((rc = alloc(I.lam, L.slot_elems))) return rc;
-    PN_CUDA(cudaMemsetAsync(I.slots, 0, sizeof(T) * (size_t)nslots * L.slot_elems, cap));
+    zero_ranges.emplace_back((void*)I.slots, sizeof(T) * (size_t)nslots * L.slot_elems);
     for (int c = 0; c < 8; ++c) {
       I.active[c] = L.active[c];
       I.dev_off[c] = L.dev_off[c];
@@ -1011,7 +1096,7 @@ class BatchGroup : public BatchGroupBase {
     double* rbar_d;
     if ((rc = alloc(rho_d, L.rho_elems))) return rc;
     if ((rc = alloc(rbar_d, L.rho_elems))) return rc;
-    PN_CUDA(cudaMemsetAsync(rho_d, 0, sizeof(T) * (size_t)L.rho_elems, cap));
+    zero_ranges.emplace_back((void*)rho_d, sizeof(T) * (size_t)L.rho_elems);
     for (int c = 0; c < 8; ++c) {
       I.rho[c] = L.active[c] ? rho_d + L.rho_off[c] : nullptr;
       I.rbar[c] = L.active[c] ? rbar_d + L.rho_off[c] : nullptr;
@@ -1034,25 +1119,25 @@ class BatchGroup : public BatchGroupBase {
     const double* dp;
     T* tw;
     double* dw;
-    if ((rc = upload(tw, conv(d->fwd_s, (long long)ns * ne)))) return rc; I.fwd_s = tw;
-    if ((rc = upload(tw, conv(d->fwd_c, (long long)ns * ne * N1)))) return rc; I.fwd_c = tw;
-    if ((rc = upload(dw, cpd(d->fwd_bc, ns)))) return rc; I.fwd_bc = dw;
-    if ((rc = upload(dw, cpd(d->fwd_sigma, (long long)(ns + 1) * nr)))) return rc; I.fwd_sigma = dw;
-    if ((rc = upload(dw, cpd(d->fwd_weight, ns + 1)))) return rc; I.fwd_weight = dw;
-    if ((rc = upload(tw, conv(d->adj_s, (long long)ns * ne)))) return rc; I.adj_s = tw;
-    if ((rc = upload(tw, conv(d->adj_c, (long long)ns * ne * N1)))) return rc; I.adj_c = tw;
-    if ((rc = upload(dw, cpd(d->adj_src_sigma, (long long)ns * nr)))) return rc; I.adj_src = dw;
-    if ((rc = upload(tw, conv(d->adj_int_s, (long long)(ns + 1) * ne)))) return rc; I.int_s = tw;
-    if ((rc = upload(tw, conv(d->adj_int_c, (long long)(ns + 1) * ne * N1)))) return rc; I.int_c = tw;
-    if ((rc = upload(dw, cpd(d->adj_int_bc, ns + 1)))) return rc; I.int_bc = dw;
+    if ((rc = stage(tw, conv(d->fwd_s, (long long)ns * ne)))) return rc; I.fwd_s = tw;
+    if ((rc = stage(tw, conv(d->fwd_c, (long long)ns * ne * N1)))) return rc; I.fwd_c = tw;
+    if ((rc = stage(dw, cpd(d->fwd_bc, ns)))) return rc; I.fwd_bc = dw;
+    if ((rc = stage(dw, cpd(d->fwd_sigma, (long long)(ns + 1) * nr)))) return rc; I.fwd_sigma = dw;
+    if ((rc = stage(dw, cpd(d->fwd_weight, ns + 1)))) return rc; I.fwd_weight = dw;
+    if ((rc = stage(tw, conv(d->adj_s, (long long)ns * ne)))) return rc; I.adj_s = tw;
+    if ((rc = stage(tw, conv(d->adj_c, (long long)ns * ne * N1)))) return rc; I.adj_c = tw;
+    if ((rc = stage(dw, cpd(d->adj_src_sigma, (long long)ns * nr)))) return rc; I.adj_src = dw;
+    if ((rc = stage(tw, conv(d->adj_int_s, (long long)(ns + 1) * ne)))) return rc; I.int_s = tw;
+    if ((rc = stage(tw, conv(d->adj_int_c, (long long)(ns + 1) * ne * N1)))) return rc; I.int_c = tw;
+    if ((rc = stage(dw, cpd(d->adj_int_bc, ns + 1)))) return rc; I.int_bc = dw;
     {
       std::vector<double> coef((size_t)(ns + 1) * nr), wf((size_t)(ns + 1));
       for (int j = 0; j <= ns; ++j) {
         wf[j] = d->dvol * d->delta_e * d->adj_weight[j];
         for (int r = 0; r < nr; ++r) coef[(size_t)j * nr + r] = d->delta_e * d->dvol * d->adj_sigma[(long long)j * nr + r] * d->adj_weight[j];
       }
-      if ((rc = upload(dw, coef))) return rc; I.int_coef = dw;
-      if ((rc = upload(dw, wf))) return rc; I.int_wfac = dw;
+      if ((rc = stage(dw, coef))) return rc; I.int_coef = dw;
+      if ((rc = stage(dw, wf))) return rc; I.int_wfac = dw;
     }
     (void)tp;
     (void)dp;
@@ -1063,8 +1148,13 @@ class BatchGroup : public BatchGroupBase {
       if (d->xray_element[r] < 0 || d->xray_element[r] >= ne) { err = "xray_element out of range"; return PN_ERR_INVALID; }
       I.xel[r] = d->xray_element[r];
     }
-    // coupling: the literal stencil must match the caller's blocks (values as well as sparsity)
-    {
+    // coupling: the literal stencil must match the caller's blocks (values as well as sparsity);
+    // blocks equal to a set already checked in this group need no second check
+    bool coupling_checked = false;
+    if (!checked_advection.empty() && (long long)checked_advection.size() == L.n_adv &&
+        std::memcmp(checked_advection.data(), d->advection, sizeof(double) * (size_t)L.n_adv) == 0)
+      coupling_checked = true;
+    if (!coupling_checked) {
       const double* pa = d->advection;
       for (int k = 0; k < 3; ++k)
         for (int c = 0; c < 8; ++c) {
@@ -1083,10 +1173,11 @@ class BatchGroup : public BatchGroupBase {
           }
           pa += (long long)nrow * ncol;
         }
+      checked_advection.assign(d->advection, d->advection + L.n_adv);
     }
     double *bf, *ba, *bm;
-    if ((rc = upload(bf, cpd(d->boundary_fwd, L.n_bnd)))) return rc;
-    if ((rc = upload(ba, cpd(d->boundary_adj, L.n_bnd)))) return rc;
+    if ((rc = stage(bf, cpd(d->boundary_fwd, L.n_bnd)))) return rc;
+    if ((rc = stage(ba, cpd(d->boundary_adj, L.n_bnd)))) return rc;
     std::vector<double> beam = cpd(d->beam_face, L.n_beam);
     // FP32: scale the beam source so the state stays near unity (a power of two: exact)
     I.scale_g = 1.0;
@@ -1098,7 +1189,7 @@ class BatchGroup : public BatchGroupBase {
       const double m = gmax * bmax;
       if (m > 0.0 && std::isfinite(m)) I.scale_g = std::ldexp(1.0, -(int)std::lround(std::log2(m)));
     }
-    if ((rc = upload(bm, beam.empty() ? std::vector<double>(1, 0.0) : beam))) return rc;
+    if ((rc = stage(bm, beam.empty() ? std::vector<double>(1, 0.0) : beam))) return rc;
     {
       long long o = 0;
       for (int k = 0; k < 3; ++k)
@@ -1135,20 +1226,26 @@ class BatchGroup : public BatchGroupBase {
         else { ilo[k] = 0; ihi[k] = nn; t.lo[k] = 1; t.ext[k] = std::max(0, nn - 2); }
       }
       t.f0 = (int)faces.size();
+      // cells on a face of an axis along which the class is even, in row-major order: whole
+      // rows on a z or y face plane, only the x end points elsewhere (O(surface), not O(volume))
+      auto on_face = [&](int k, int v) {
+        return L.act[k] && !class_bit(c, k) && (v == 0 || v == L.shape[c][k] - 1);
+      };
       for (int kz = ilo[2]; kz < ihi[2]; ++kz)
-        for (int jy = ilo[1]; jy < ihi[1]; ++jy)
-          for (int ix = ilo[0]; ix < ihi[0]; ++ix) {
-            const int cc[3] = {ix, jy, kz};
-            bool f = false;
-            for (int k = 0; k < 3; ++k)
-              if (L.act[k] && !class_bit(c, k) && (cc[k] == 0 || cc[k] == L.shape[c][k] - 1)) f = true;
-            if (f) faces.push_back(pack_cell(ix, jy, kz));
+        for (int jy = ilo[1]; jy < ihi[1]; ++jy) {
+          if (on_face(2, kz) || on_face(1, jy)) {
+            for (int ix = ilo[0]; ix < ihi[0]; ++ix) faces.push_back(pack_cell(ix, jy, kz));
+          } else if (L.act[0] && !class_bit(c, 0)) {
+            const int last = L.shape[c][0] - 1;
+            if (ilo[0] <= 0 && 0 < ihi[0]) faces.push_back(pack_cell(0, jy, kz));
+            if (last > 0 && ilo[0] <= last && last < ihi[0]) faces.push_back(pack_cell(last, jy, kz));
           }
+        }
       t.nf = (int)faces.size() - t.f0;
       per.push_back(t);
     }
     int* fd;
-    if ((rc = upload(fd, faces.empty() ? std::vector<int>(1, 0) : faces))) return rc;
+    if ((rc = stage(fd, faces.empty() ? std::vector<int>(1, 0) : faces))) return rc;
     int nblk[3] = {0, 0, 0};
     for (const Tmp& t : per) {
       for (int list = 0; list < 3; ++list) {
@@ -1205,11 +1302,11 @@ class BatchGroup : public BatchGroupBase {
     a.tpb = tiles_per_block(nt);
     const int grid = (nt + a.tpb - 1) / a.tpb;
     if (integ)
-      batch_integrate_kernel<T, N, DIMS><<<grid, BLOCK, 0, cap>>>(a);
+      batch_integrate_kernel<T, N, DIMS><<<grid, BLOCK, 0, ls>>>(a);
     else if (adj)
-      batch_substep_kernel<T, N, true, DIMS><<<grid, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, true, DIMS><<<grid, BLOCK, 0, ls>>>(a);
     else
-      batch_substep_kernel<T, N, false, DIMS><<<grid, BLOCK, 0, cap>>>(a);
+      batch_substep_kernel<T, N, false, DIMS><<<grid, BLOCK, 0, ls>>>(a);
     PN_CUDA(cudaGetLastError());
     ++nl;
     return PN_OK;
@@ -1240,9 +1337,9 @@ class BatchGroup : public BatchGroupBase {
         a.K = K;
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
         if (adj)
-          batch_tma2d_kernel<N, true><<<grid, BLOCK, TmaLayout<N>::SMEM, cap>>>(a);
+          batch_tma2d_kernel<N, true><<<grid, BLOCK, TmaLayout<N>::SMEM, ls>>>(a);
         else
-          batch_tma2d_kernel<N, false><<<grid, BLOCK, TmaLayout<N>::SMEM, cap>>>(a);
+          batch_tma2d_kernel<N, false><<<grid, BLOCK, TmaLayout<N>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
@@ -1271,7 +1368,7 @@ class BatchGroup : public BatchGroupBase {
         a.n_tiles = nb;
         a.it = j;
         a.K = K;
-        batch_tma2d_int_kernel<N><<<std::min(nb, tma_int_grid), BLOCK, TmaIntLayout<N>::SMEM, cap>>>(a);
+        batch_tma2d_int_kernel<N><<<std::min(nb, tma_int_grid), BLOCK, TmaIntLayout<N>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
@@ -1293,19 +1390,19 @@ class BatchGroup : public BatchGroupBase {
     int rc;
     dim3 gz(64, n);
     if (fwd) {
-      batch_zero_kernel<T><<<gz, 256, 0, cap>>>(dinst, 0);
+      batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 0);
       PN_CUDA(cudaGetLastError());
       for (int t = 1; t <= max_ns; ++t) {
         const int j = max_ns - t;
         double* part = partial + (long long)(t - 1) * n_ptiles * pr;
         if ((rc = fwd_step(j, BM_FORWARD, part))) return rc;
       }
-      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, cap>>>(dinst, partial, max_ns, n_ptiles, pr);
-      batch_final_kernel<T><<<n, 32, 0, cap>>>(dinst);
+      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, ls>>>(dinst, partial, max_ns, n_ptiles, pr);
+      batch_final_kernel<T><<<n, 32, 0, ls>>>(dinst);
       PN_CUDA(cudaGetLastError());
       nl += 3;
     } else {
-      batch_zero_kernel<T><<<gz, 256, 0, cap>>>(dinst, 1);
+      batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 1);
       PN_CUDA(cudaGetLastError());
       nl += 1;
       for (int m = 0; m * K < max_ns; ++m) {
@@ -1329,6 +1426,7 @@ class BatchGroup : public BatchGroupBase {
     cudaGraph_t graph = nullptr;
     nl = 0;
     PN_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+    ls = cap;
     int rc = record(fwd);
     cudaError_t e = cudaStreamEndCapture(cap, &graph);
     if (rc) {
@@ -1356,12 +1454,30 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
+  // order `s` after the creation uploads; zero the tapes and densities once
+  int prepare(cudaStream_t s) {
+    PN_CUDA(cudaStreamWaitEvent(s, ev_up, 0));
+    if (!zeroed) {
+      for (auto& z : zero_ranges) PN_CUDA(cudaMemsetAsync(z.first, 0, z.second, s));
+      zeroed = true;
+    }
+    return PN_OK;
+  }
+
   int forward(const BIo* io_host, cudaStream_t s) override {
     int rc;
+    if ((rc = prepare(s))) return rc;
     if ((rc = put_io(io_host, s))) return rc;
     batch_load_kernel<T><<<dim3(256, n), 256, 0, s>>>(dinst, dio);
     PN_CUDA(cudaGetLastError());
-    PN_CUDA(cudaGraphLaunch(gf, s));
+    if (direct) {
+      ls = s;
+      nl = 0;
+      if ((rc = record(true))) return rc;
+      nl_f = nl;
+    } else {
+      PN_CUDA(cudaGraphLaunch(gf, s));
+    }
     batch_copy_I_kernel<T><<<n, 32, 0, s>>>(dinst, dio);
     PN_CUDA(cudaGetLastError());
     return PN_OK;
@@ -1369,10 +1485,18 @@ class BatchGroup : public BatchGroupBase {
 
   int adjoint(const BIo* io_host, cudaStream_t s) override {
     int rc;
+    if ((rc = prepare(s))) return rc;
     if ((rc = put_io(io_host, s))) return rc;
     batch_prep_ibar_kernel<T><<<n, 32, 0, s>>>(dinst, dio, sizeof(T) == 4 ? 1 : 0);
     PN_CUDA(cudaGetLastError());
-    PN_CUDA(cudaGraphLaunch(ga, s));
+    if (direct) {
+      ls = s;
+      nl = 0;
+      if ((rc = record(false))) return rc;
+      nl_a = nl;
+    } else {
+      PN_CUDA(cudaGraphLaunch(ga, s));
+    }
     batch_store_kernel<T><<<dim3(256, n), 256, 0, s>>>(dinst, dio);
     PN_CUDA(cudaGetLastError());
     return PN_OK;

@@ -20,6 +20,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -166,6 +168,8 @@ int alloc_out(pn::Arena* arena, Wave* w, long long cnt, double*& out, std::strin
 // Build the wave's batch in the arena, upload its inputs and queue its work; called without the
 // lock.  On failure everything the wave holds is released and the code returned.
 int pn_server::launch_wave(Wave* w) {
+  const bool trace = std::getenv("PN_TRACE") != nullptr;
+  const auto t_begin = Clock::now();
   std::vector<const pn_desc*> descs;
   for (Request* r : w->reqs) descs.insert(descs.end(), r->descs.begin(), r->descs.end());
   const int n = (int)descs.size();
@@ -217,6 +221,7 @@ int pn_server::launch_wave(Wave* w) {
         }
       }
     }
+  const auto t_io = Clock::now();
   // tapes: first a fair share of what is free among the wave slots still open.  "Does not fit"
   // from the stride search wants a larger budget, a full arena (tables and tiles come on top of
   // the tapes) a smaller one, i.e. a longer checkpoint stride.
@@ -228,7 +233,11 @@ int pn_server::launch_wave(Wave* w) {
   int rc = PN_ERR_NO_MEMORY;
   for (long long budget : tries) {
     std::string err;
+    const auto t_try = Clock::now();
     rc = pn::batch_create(descs.data(), n, budget, K, 0, arena.get(), &w->b, err);
+    if (trace)
+      std::fprintf(stderr, "[pn] wave %d: %d solves, budget %.1f GB: %s (%.1f ms)\n", w->id, n, budget / 1e9,
+                   rc == PN_OK ? "built" : err.c_str(), ms_between(t_try, Clock::now()));
     if (rc == PN_OK) break;
     w->err = err;
     if (rc != PN_ERR_NO_MEMORY) break;
@@ -246,6 +255,9 @@ int pn_server::launch_wave(Wave* w) {
     release();
     return rc;
   }
+  if (trace)
+    std::fprintf(stderr, "[pn] wave %d: inputs %.1f ms, build+launch %.1f ms, arena %.1f / %.1f GB\n", w->id,
+                 ms_between(t_begin, t_io), ms_between(t_io, Clock::now()), arena->used() / 1e9, arena->size() / 1e9);
   auto* arg = new std::pair<pn_server*, Wave*>(this, w);
   if (cudaLaunchHostFunc(w->st, wave_done, arg) != cudaSuccess) {
     delete arg;

@@ -143,3 +143,15 @@ def test_tma_tiles_against_the_oracle(gpu_lib, oracle):
         I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[q])
         assert rel(I[q], I_o) < 1e-4
         assert rel(rb[q], rb_o) < 1e-3
+
+
+def test_direct_launches_match_the_graphs(gpu_lib):
+    """PN_BATCH_DIRECT_LAUNCH issues the same kernels from the host instead of replaying the
+    captured graphs: identical results."""
+    torch = pytest.importorskip("torch")
+    solves = mixed_solves(PN_FP32) + tma_solves()[:2]
+    ref = run_batch(torch, solves)
+    got = run_batch(torch, solves, flags=capi.PN_BATCH_DIRECT_LAUNCH, ibar=ref[1])
+    for a, b in zip(got[:5], ref[:5]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
