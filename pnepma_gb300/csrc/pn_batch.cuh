@@ -313,12 +313,15 @@ __global__ void PN_BATCH_BOUNDS batch_substep_kernel(const __grid_constant__ BLa
     }
     if (L.partial != nullptr && one.cls == 0) {   // block-uniform: only eee tiles carry intensity
       const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      // only the group's lines: FP64 adds are scarce on this GPU (2 per SM per clock)
 #pragma unroll
       for (int r = 0; r < MAXR; ++r) {
-        double v = part[r];
+        if (r < L.pr) {
+          double v = part[r];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[w][r] = v;
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+          if (lane == 0) red[w][r] = v;
+        }
       }
       __syncthreads();
       if (threadIdx.x < L.pr) {

@@ -495,12 +495,15 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   }
   if (want_part && tt.pslot >= 0) {   // block-uniform
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    // only the group's lines: FP64 adds are scarce on this GPU (2 per SM per clock)
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) {
-      double v = part[r];
+      if (r < L.pr) {
+        double v = part[r];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if (lane == 0) red[w][r] = v;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[w][r] = v;
+      }
     }
     __syncthreads();
     if (threadIdx.x < L.pr) {
@@ -725,12 +728,13 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
         if (e < tt.ne) {
-          double v = double(ar.s[e]) * double(P);
+          // this step's increment in FP32, accumulated in FP64 (integrate_cell's arithmetic)
+          float v = ar.s[e] * P;
 #pragma unroll
           for (int l = 0; l <= N; ++l)
-            if ((mask >> l) & 1u) v += double(ar.c[e][l]) * double(R[l]);
+            if ((mask >> l) & 1u) v += ar.c[e][l] * R[l];
           const double old = rbs[e * PLO + lo];   // this cell's rho_bar, staged with the tile
-          rbs[e * PLO + lo] = old + v * ar.wfac;
+          rbs[e * PLO + lo] = old + double(v) * ar.wfac;
         }
       }
       if constexpr (C == 0) {

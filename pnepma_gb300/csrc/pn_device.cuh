@@ -611,11 +611,12 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
 #pragma unroll
     for (int e = 0; e < MAXE; ++e) {
       if (e < a.ne) {
-        double v = double(a.s[e]) * double(P);
+        // this step's increment in the state's precision, accumulated in FP64
+        T v = a.s[e] * P;
 #pragma unroll
         for (int l = 0; l <= N; ++l)
-          if ((mask >> l) & 1u) v += double(a.c[e][l]) * double(R[l]);
-        rb[e * gt.ms] += v * a.wfac;
+          if ((mask >> l) & 1u) v += a.c[e][l] * R[l];
+        rb[e * gt.ms] += double(v) * a.wfac;
       }
     }
     if constexpr (C == 0) {
