@@ -460,7 +460,7 @@ def run_ours(args):
                              "forward_roofline": {"bound": "hbm", "achieved": fp32_fwd_gbs, "peak": peak,
                                                   "unit": "GB/s", "frac": fp32_fwd_gbs / peak,
                                                   "peak_source": peak_source,
-                                                  "kernel": "batch_tma2d_kernel<11>, forward sweep",
+                                                  "kernel": "batch_tma_kernel<11, forward, 2D>, forward sweep",
                                                   "note": "algorithmic bytes of all forward sub-steps of the 60 solves / forward time"},
                              "kernels_per_step": binfo.forward_kernels + binfo.adjoint_kernels,
                              "form": "one pn_batch: one launch per sub-step covers all 60 solves"},
@@ -826,7 +826,10 @@ def run_config4(args):
                        "forward_roofline": {"bound": "hbm", "achieved": fwd_bytes * ns / (fwd_ms / 1e3) / 1e9,
                                             "peak": peak, "unit": "GB/s",
                                             "frac": fwd_bytes * ns / (fwd_ms / 1e3) / 1e9 / peak,
-                                            "kernel": "batch_substep_kernel<float,7,*,7> (generic 3D), forward sweep"},
+                                            "kernel": ("batch_tma_kernel<7, forward, 3D>" if binfo.tma_groups
+                                                       else "batch_substep_kernel<float,7,*,7> (generic 3D)")
+                                                      + ", forward sweep"},
+                       "tma_groups": binfo.tma_groups,
                        "moment_cell_updates_per_s": 2 * ns * m_active / ((fwd_ms + float(np.mean(ad))) / 1e3)},
         "fp64_plain": {"forward_ms": fp64_fwd_ms, "adjoint_ms": fp64_adj_ms},
         "fp32_vs_fp64": {"max_rel_err_intensity": float(np.max(np.abs(I32h - I64) / np.abs(I64))),

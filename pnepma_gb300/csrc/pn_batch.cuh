@@ -579,7 +579,7 @@ class BatchGroup : public BatchGroupBase {
   cudaStream_t cap = nullptr;
   long long nl_f = 0, nl_a = 0, nl = 0;
   int sms = 152;
-  // FP32 2D: box tiles through the TMA kernel, face tiles through the generic one
+  // FP32 2D (x, y) and 3D groups: every sub-step and density integral through the TMA tile kernels
   bool use_tma = false;
   std::vector<const pn_desc*> cur_descs;   // the group's descriptors while create() runs
   std::vector<double> checked_advection;   // coupling blocks already checked against the stencil
@@ -812,7 +812,7 @@ class BatchGroup : public BatchGroupBase {
       }
       if ((rc = upload(dtiles[list], tiles[list]))) return rc;
     }
-    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       if (!(flags & PN_BATCH_GENERIC_KERNELS))
         if ((rc = build_tma())) return rc;
     } else {
@@ -843,12 +843,13 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  // TMA path of an FP32 2D group: box/face tile lists, tensor maps, coefficient rows.  Leaves
-  // use_tma false (generic kernels) when a class grid is smaller than a box or the driver lacks
+  // TMA path of an FP32 2D (x, y) or 3D group: tile lists, tensor maps, coefficient rows.  Leaves
+  // use_tma false (generic kernels) when a class grid is narrower than a box or the driver lacks
   // the tensor-map encoder.
   int build_tma() {
-    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
-      using LY = TmaLayout<N>;
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
+      using LY = TmaLayout<N, DIMS>;
+      using LI = TmaIntLayout<N, DIMS>;
       if (!encode_tiled_fn()) return PN_OK;
       for (int q = 0; q < n; ++q)
         for (int c = 0; c < 8; ++c)
@@ -861,17 +862,20 @@ class BatchGroup : public BatchGroupBase {
       PN_CUDA(cudaGetDevice(&dev));
       PN_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
       if (LY::SMEM + 2048 > smem_optin) return PN_OK;
-      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
-      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM));
-      PN_CUDA(cudaFuncSetAttribute(batch_tma2d_int_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   TmaIntLayout<N>::SMEM));
+      if (LI::SMEM + 2048 > smem_optin) return PN_OK;
+      PN_CUDA(cudaFuncSetAttribute(batch_tma_kernel<N, false, DIMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   LY::SMEM));
+      PN_CUDA(cudaFuncSetAttribute(batch_tma_kernel<N, true, DIMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   LY::SMEM));
+      PN_CUDA(cudaFuncSetAttribute(batch_tma_int_kernel<N, DIMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   LI::SMEM));
       int occ_i = 0;
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_i, batch_tma2d_int_kernel<N>, BLOCK, TmaIntLayout<N>::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_i, batch_tma_int_kernel<N, DIMS>, TB, LI::SMEM));
       if (occ_i < 1) return PN_OK;
       tma_int_grid = occ_i * sms;
       int occ_f = 0, occ_a = 0;
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma2d_kernel<N, false>, BLOCK, LY::SMEM));
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma2d_kernel<N, true>, BLOCK, LY::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, TB, LY::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, TB, LY::SMEM));
       if (occ_f < 1 || occ_a < 1) return PN_OK;
       tma_grid[0] = occ_f * sms;
       tma_grid[1] = occ_a * sms;
@@ -937,19 +941,24 @@ class BatchGroup : public BatchGroupBase {
           const int nm = I.g[c].nm;
           if (!I.active[c] || nm == 0) continue;
           CUtensorMap* m = &maps[((size_t)q * 8 + c) * TM_KINDS];
-          const long long st_dims[4] = {I.shape[c][0], I.shape[c][1], nm, nslots};
-          const long long st_str[4] = {1, I.px[c], I.g[c].ms, I.slot_elems};
-          const int boxt[4] = {TX, TY, nm, 1}, boxx[4] = {BW, TY, nm, 1}, boxy[4] = {BW, TY + 1, nm, 1};
-          bool ok = encode_f32(&m[TM_ST_T], I.slots + I.dev_off[c], 4, st_dims, st_str, boxt) &&
-                    encode_f32(&m[TM_ST_X], I.slots + I.dev_off[c], 4, st_dims, st_str, boxx) &&
-                    encode_f32(&m[TM_ST_Y], I.slots + I.dev_off[c], 4, st_dims, st_str, boxy) &&
-                    encode_f32(&m[TM_LAM_T], I.lam + I.dev_off[c], 3, st_dims, st_str, boxt) &&
-                    encode_f32(&m[TM_LAM_X], I.lam + I.dev_off[c], 3, st_dims, st_str, boxx) &&
-                    encode_f32(&m[TM_LAM_Y], I.lam + I.dev_off[c], 3, st_dims, st_str, boxy);
-          const long long rho_dims[3] = {I.shape[c][0], I.shape[c][1], I.ne};
-          const int boxr[3] = {TX, TY, I.ne};
-          ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 3, rho_dims, st_str, boxr);
-          ok = ok && encode_tensor(&m[TM_RBAR], I.rbar[c], 3, rho_dims, st_str, boxr, 8);
+          // (x, y, z, moment, slot); a 2D grid has z extent 1
+          const long long st_dims[5] = {I.shape[c][0], I.shape[c][1], I.shape[c][2], nm, nslots};
+          const long long st_str[5] = {1, I.px[c], (long long)I.px[c] * I.shape[c][1], I.g[c].ms, I.slot_elems};
+          const int boxt[5] = {TX, TY, 1, nm, 1}, boxx[5] = {BW, TY, 1, nm, 1}, boxy[5] = {BW, TY + 1, 1, nm, 1};
+          const int boxz[5] = {TX, TY, 2, nm, 1};
+          bool ok = encode_f32(&m[TM_ST_T], I.slots + I.dev_off[c], 5, st_dims, st_str, boxt) &&
+                    encode_f32(&m[TM_ST_X], I.slots + I.dev_off[c], 5, st_dims, st_str, boxx) &&
+                    encode_f32(&m[TM_ST_Y], I.slots + I.dev_off[c], 5, st_dims, st_str, boxy) &&
+                    encode_f32(&m[TM_LAM_T], I.lam + I.dev_off[c], 4, st_dims, st_str, boxt) &&
+                    encode_f32(&m[TM_LAM_X], I.lam + I.dev_off[c], 4, st_dims, st_str, boxx) &&
+                    encode_f32(&m[TM_LAM_Y], I.lam + I.dev_off[c], 4, st_dims, st_str, boxy);
+          if (DIMS == 7)
+            ok = ok && encode_f32(&m[TM_ST_Z], I.slots + I.dev_off[c], 5, st_dims, st_str, boxz) &&
+                 encode_f32(&m[TM_LAM_Z], I.lam + I.dev_off[c], 4, st_dims, st_str, boxz);
+          const long long rho_dims[4] = {I.shape[c][0], I.shape[c][1], I.shape[c][2], I.ne};
+          const int boxr[4] = {TX, TY, 1, I.ne};
+          ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 4, rho_dims, st_str, boxr);
+          ok = ok && encode_tensor(&m[TM_RBAR], I.rbar[c], 4, rho_dims, st_str, boxr, 8);
           if (!ok) return PN_OK;   // generic kernels for this group
         }
       }
@@ -976,10 +985,10 @@ class BatchGroup : public BatchGroupBase {
           S.px[c] = I.g[c].px;
           S.n0[c] = I.g[c].n[0];
           S.n1[c] = I.g[c].n[1];
+          S.n2[c] = I.g[c].n[2];
         }
         for (int r = 0; r < MAXR; ++r) S.xel[r] = I.xel[r];
-        S.inv_h[0] = I.inv_h[0];
-        S.inv_h[1] = I.inv_h[1];
+        for (int k = 0; k < 3; ++k) S.inv_h[k] = I.inv_h[k];
         S.dE = I.dE;
         S.nr = I.nr;
         S.ne = I.ne;
@@ -1001,13 +1010,14 @@ class BatchGroup : public BatchGroupBase {
           if (list == 0) hinst[q].ptile0 = n_ptiles;
           for (int c = 0; c < 8; ++c) {
             if (!I.active[c] || (list < 2 && class_parity(c) != list) || class_moments_host(c) == 0) continue;
-            int lo3[2], hi3[2];
-            for (int k = 0; k < 2; ++k) {
+            int lo3[3], hi3[3];
+            for (int k = 0; k < 3; ++k) {
               const int nn = I.shape[c][k];
               lo3[k] = class_bit(c, k) ? 1 : 0;
               hi3[k] = class_bit(c, k) ? nn - 1 : nn;
             }
             // x0 = 32 bx over the class's points; target lanes [lo - x0, hi - x0) within the tile
+            for (int z = lo3[2]; z < hi3[2]; ++z)
             for (int y0 = lo3[1]; y0 < hi3[1]; y0 += TY)
               for (int x0 = 0; x0 < hi3[0]; x0 += TX) {
                 const int xv0 = std::max(lo3[0] - x0, 0), xv1 = std::min(hi3[0] - x0, TX);
@@ -1026,6 +1036,7 @@ class BatchGroup : public BatchGroupBase {
                 tt.arg_fwd = arg_fwd[q];
                 tt.arg_adj = arg_adj[q];
                 tt.arg_int = arg_int[q];
+                tt.z = z;
                 ttl[list].push_back(tt);
               }
           }
@@ -1285,7 +1296,7 @@ class BatchGroup : public BatchGroupBase {
 
   // --------------------------------------------------------------------------------------------
   int launch(int list, int mode, int j, int sub, double* part, bool adj, bool integ) {
-    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       if (use_tma) return integ ? launch_tma_int(j) : launch_tma(list, mode, j, sub, part, adj);
     }
     const int x = integ ? j - 1 : j;   // integrate at iteration j includes the solves with ns == j
@@ -1317,7 +1328,7 @@ class BatchGroup : public BatchGroupBase {
 
   // TMA path of a sub-step: every target cell (face tiles compute their ghosts in place)
   int launch_tma(int list, int mode, int j, int sub, double* part, bool adj) {
-    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       int last = -1;
       for (int q = 0; q < n; ++q)
         if (hinst[q].ns > j) last = q;
@@ -1340,9 +1351,9 @@ class BatchGroup : public BatchGroupBase {
         a.K = K;
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
         if (adj)
-          batch_tma2d_kernel<N, true><<<grid, BLOCK, TmaLayout<N>::SMEM, ls>>>(a);
+          batch_tma_kernel<N, true, DIMS><<<grid, TB, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
         else
-          batch_tma2d_kernel<N, false><<<grid, BLOCK, TmaLayout<N>::SMEM, ls>>>(a);
+          batch_tma_kernel<N, false, DIMS><<<grid, TB, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
@@ -1354,7 +1365,7 @@ class BatchGroup : public BatchGroupBase {
 
   // TMA path of the density integral at iteration j: every cell of every class
   int launch_tma_int(int j) {
-    if constexpr (std::is_same<T, float>::value && DIMS == 3) {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       int last = -1;
       for (int q = 0; q < n; ++q)
         if (hinst[q].ns >= j) last = q;   // the integral at iteration j includes solves with ns == j
@@ -1371,7 +1382,7 @@ class BatchGroup : public BatchGroupBase {
         a.n_tiles = nb;
         a.it = j;
         a.K = K;
-        batch_tma2d_int_kernel<N><<<std::min(nb, tma_int_grid), BLOCK, TmaIntLayout<N>::SMEM, ls>>>(a);
+        batch_tma_int_kernel<N, DIMS><<<std::min(nb, tma_int_grid), TB, TmaIntLayout<N, DIMS>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }

@@ -1,16 +1,17 @@
-// pn_batch_tma.cuh -- FP32 2D sub-steps and density integral of the batched engine with TMA tiles.
+// pn_batch_tma.cuh -- FP32 2D/3D sub-steps and density integral of the batched engine with TMA tiles.
 //
 // The same arithmetic as batch_substep_kernel / batch_integrate_kernel (compiled coupling blocks,
-// x then y), so states and gradients are bit-identical; only the way operands move differs:
+// x, then y, then z), so states and gradients are bit-identical; only the way operands move differs:
 //
 //   * persistent CTAs walk the tiles of a launch in grid-stride order, so the CTAs resident at
 //     any time work on neighbouring tiles;
-//   * a tile is 32 x 4 points of one target class starting at x0 = 32 bx: lanes outside the
+//   * a tile is 32 x 4 points of one plane of one target class, starting at x0 = 32 bx: lanes outside the
 //     class's target cells (its ghost points, or points past the grid) keep the values they
 //     were loaded with;
 //   * one thread issues, on one mbarrier, cp.async.bulk.tensor loads of the target class's
 //     moments (32 x 4 box), the x- and y-neighbour classes with their one-cell halo (40 x 4 and
-//     40 x 5 boxes from x0 - 4, the first tile's negative start reading zeros) and the densities,
+//     40 x 5 boxes from x0 - 4, the first tile's negative start reading zeros), in 3D the
+//     z-neighbour class's two planes either side of the tile's plane (32 x 4 x 2), the densities,
 //     plus cp.async.bulk copies of the step's coefficient row, the tile record and the solve's
 //     arguments; every operand then sits at a compile-time shared-memory offset;
 //   * results overwrite the target box in shared memory and go back with one cp.async.bulk.tensor
@@ -33,7 +34,12 @@
 namespace pn {
 
 constexpr int TX = 32;              // tile width (points)
-constexpr int TY = BLOCK / TX;      // tile height (rows)
+// tile height (rows); one thread per point, TB threads per CTA
+#ifndef PN_TMA_TY
+#define PN_TMA_TY 4
+#endif
+constexpr int TY = PN_TMA_TY;
+constexpr int TB = TX * TY;
 constexpr int BW = TX + 8;          // neighbour box width: x0 - 4 .. x0 + 35 (a multiple of 4 floats)
 constexpr int XO = 4;               // the tile's first point in a neighbour box
 constexpr int PLO = TX * TY;        // floats per moment plane of a target / density box
@@ -67,11 +73,11 @@ struct IntRow {
   double bc;
 };
 
-// One 32 x 4 tile of a target class (48 bytes): points x0 .. x0 + 31 (x0 = 32 bx), rows
-// y0 .. y0 + 3; target lanes xv0 <= tx < xv1, rows ty < ey.
+// One tile of a target class (64 bytes): points x0 .. x0 + 31 (x0 = 32 bx), rows y0 .. y0 + TY - 1,
+// plane z; target lanes xv0 <= tx < xv1, rows ty < ey.
 struct TTile {
   int inst;     // solve (group order)
-  int cls;      // target class (z-even in 2D)
+  int cls;      // target class
   int x0, y0;
   int ext;      // xv0 | xv1 << 8 | ey << 16
   int pslot;    // partial slot of an eee tile, else -1
@@ -81,6 +87,8 @@ struct TTile {
   int arg_fwd;  // index of the solve's first forward ArgRow
   int arg_adj;  // ... adjoint ArgRow
   int arg_int;  // ... IntRow (n_steps + 1 rows)
+  int z;        // plane (0 in 2D)
+  int pad_[3];
 };
 
 // The fields of a solve the cell code reads, copied to shared memory with every tile so that no
@@ -101,23 +109,26 @@ struct TSolve {
   int px[8];
   int n0[8];
   int n1[8];
+  int n2[8];
   int xel[MAXR];
-  float inv_h[2];
+  float inv_h[3];
   float dE;
   int nr;
   int ne;
-  int pad_[3];
   double scale_g;
+  double pad_;
 };
 static_assert(sizeof(TSolve) % 16 == 0, "TSolve must be a 16-byte multiple");
 static_assert(sizeof(TTile) % 16 == 0, "TTile must be a 16-byte multiple");
 
-// tensor maps per (solve, class): state (x, y, moment, slot) and adjoint state (x, y, moment) as
-// target boxes and as x / y neighbour boxes; densities; rho_bar (FP64)
+constexpr int PLZ = 2 * PLO;        // floats per moment plane of a z-neighbour box (two planes)
+
+// tensor maps per (solve, class): state (x, y, z, moment, slot) and adjoint state (x, y, z, moment)
+// as target boxes and as x / y / z neighbour boxes; densities; rho_bar (FP64)
 enum {
-  TM_ST_T = 0, TM_ST_X = 1, TM_ST_Y = 2,
-  TM_LAM_T = 3, TM_LAM_X = 4, TM_LAM_Y = 5,
-  TM_RHO = 6, TM_RBAR = 7, TM_KINDS = 8
+  TM_ST_T = 0, TM_ST_X = 1, TM_ST_Y = 2, TM_ST_Z = 3,
+  TM_LAM_T = 4, TM_LAM_X = 5, TM_LAM_Y = 6, TM_LAM_Z = 7,
+  TM_RHO = 8, TM_RBAR = 9, TM_KINDS = 10
 };
 
 template <int N>
@@ -134,17 +145,24 @@ struct TLaunch {
   int mode, j, sub, K;
 };
 
-template <int N>
-struct TmaLayout {
+// the classes a launch updates: z-even ones in 2D (DIMS = 3), all in 3D (DIMS = 7)
+template <int N, int DIMS>
+struct TmaClasses {
   static constexpr int maxn(int a, int b) { return a > b ? a : b; }
-  static constexpr int NO = maxn(maxn(Ord<N>::n(0), Ord<N>::n(2)), maxn(Ord<N>::n(4), Ord<N>::n(6)));
-  static constexpr int NXN = NO;
-  static constexpr int NYN = NO;
+  static constexpr int n_even_z = maxn(maxn(Ord<N>::n(0), Ord<N>::n(2)), maxn(Ord<N>::n(4), Ord<N>::n(6)));
+  static constexpr int n_odd_z = maxn(maxn(Ord<N>::n(1), Ord<N>::n(3)), maxn(Ord<N>::n(5), Ord<N>::n(7)));
+  static constexpr int NO = DIMS == 7 ? maxn(n_even_z, n_odd_z) : n_even_z;
+};
+
+template <int N, int DIMS>
+struct TmaLayout {
+  static constexpr int NO = TmaClasses<N, DIMS>::NO;
   static constexpr int al(int b) { return (b + 127) / 128 * 128; }
   static constexpr int OWN = 0;
   static constexpr int XN = OWN + al(NO * PLO * 4);
-  static constexpr int YN = XN + al(NXN * PL4 * 4);
-  static constexpr int RHO = YN + al(NYN * PL5 * 4);
+  static constexpr int YN = XN + al(NO * PL4 * 4);
+  static constexpr int ZN = YN + al(NO * PL5 * 4);
+  static constexpr int RHO = ZN + (DIMS == 7 ? al(NO * PLZ * 4) : 0);
   static constexpr int ARG = RHO + al(MAXE * PLO * 4);
   static constexpr int TIL = ARG + (int)sizeof(ArgRow<N>);
   static constexpr int SOL = TIL + (int)sizeof(TTile);
@@ -188,14 +206,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* b, unsigne
   }
 }
 
-__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
-                                            unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-      ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-      : "memory");
-}
-
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                             unsigned long long* bar) {
   asm volatile(
@@ -204,16 +214,25 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// shared -> global tensor stores (coordinates >= 0 only), tracked by the bulk async-group
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int c0, int c1, int c2, const void* src) {
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
-               ::"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(src))
-               : "memory");
+__device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
+      : "memory");
 }
 
+// shared -> global tensor stores (coordinates >= 0 only), tracked by the bulk async-group
 __device__ __forceinline__ void tma_store_4d(const CUtensorMap* map, int c0, int c1, int c2, int c3, const void* src) {
   asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];"
                ::"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+               : "memory");
+}
+
+__device__ __forceinline__ void tma_store_5d(const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                             const void* src) {
+  asm volatile("cp.async.bulk.tensor.5d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4, %5}], [%6];"
+               ::"l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(src))
                : "memory");
 }
 
@@ -266,12 +285,13 @@ __device__ __forceinline__ SubSlots sub_slots(int ns, int n_ck, int mode, int j,
 
 // Issue the loads of a tile into stage `st` (one thread).  `tt` must be the tile record in
 // global memory (it is also bulk-copied into the stage).
-template <int N, bool ADJ>
+template <int N, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                           unsigned long long* bar) {
-  using LY = TmaLayout<N>;
-  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
+  using LY = TmaLayout<N, DIMS>;
+  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2, cz = c ^ 1;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
+  const int n_z = DIMS == 7 ? class_moments<N>(cz) : 0;
   SubSlots sl{0, 0, 0};
   int row;
   if (!ADJ) {
@@ -280,24 +300,27 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   } else {
     row = tt.arg_adj + L.j;
   }
-  const unsigned bytes = 4u * (unsigned)(PLO * n_own + PL4 * n_x + PL5 * n_y + PLO * tt.ne) +
+  const unsigned bytes = 4u * (unsigned)(PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
                          (unsigned)(sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
-  // the y box starts one row below the tile for a target odd in y (it reads rows j - 1 and j),
-  // at the tile for one even in y (rows j and j + 1)
+  // the y (z) box starts one row (plane) below the tile for a target odd in y (z): it reads j - 1
+  // and j; at the tile for one even in y (z): j and j + 1
   const int ya = tt.y0 - ((c >> 1) & 1);
+  const int za = tt.z - (c & 1);
   const int xa = tt.x0 - XO;
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
   if (ADJ) {
-    tma_load_3d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, 0, bar);
-    if (n_x > 0) tma_load_3d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM_X, xa, tt.y0, 0, bar);
-    if (n_y > 0) tma_load_3d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM_Y, xa, ya, 0, bar);
+    tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
+    if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM_X, xa, tt.y0, tt.z, 0, bar);
+    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM_Y, xa, ya, tt.z, 0, bar);
+    if (n_z > 0) tma_load_4d(st + LY::ZN, mp + cz * TM_KINDS + TM_LAM_Z, tt.x0, tt.y0, za, 0, bar);
   } else {
-    tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, 0, sl.own, bar);
-    if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, 0, sl.from, bar);
-    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, 0, sl.from, bar);
+    tma_load_5d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
+    if (n_x > 0) tma_load_5d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, tt.z, 0, sl.from, bar);
+    if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, tt.z, 0, sl.from, bar);
+    if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, sl.from, bar);
   }
-  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, 0, bar);
+  tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
   bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
@@ -308,10 +331,11 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
 // its value depends on the target's values at the face cell (target box) and on the switched
 // class's first interior point (neighbour box), both staged.  No other tile reads these ghosts, so
 // they are never written to memory.  All threads call this; the caller syncs before reading.
-//   own: [n(C)][TY][TX], xb: [n(C^4)][TY][BW] (from x0 - 4), yb: [n(C^2)][TY+1][BW]
-template <int N, int C, int KIND>
+//   own: [n(C)][TY][TX], xb: [n(C^4)][TY][BW] (from x0 - 4), yb: [n(C^2)][TY+1][BW],
+//   zb: [n(C^1)][2][TY][TX]
+template <int N, int C, int KIND, int DIMS>
 __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, const float* own,
-                                            float* xb, float* yb, double bc) {
+                                            float* xb, float* yb, float* zb, double bc) {
   constexpr bool ADJ = KIND == 1;
   constexpr int nt = Ord<N>::n(C);
   const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
@@ -332,13 +356,14 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
         const int gcol = left ? XO : ncx - tt.x0 + XO;
         const int icol = left ? XO + 1 : ncx - 1 - tt.x0 + XO;
         const bool src = !ADJ && !left;
-        for (int w = threadIdx.x; w < ey * nf; w += BLOCK) {
+        for (int w = threadIdx.x; w < ey * nf; w += TB) {
           const int ty = w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
           for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + ty * TX + cc], bv);
           const int j = tt.y0 + ty;
-          const float gval = src ? float(I.beam[F][(long long)j * nf + r] * bc_scaled) : 0.0f;
+          const float gval =
+              src ? float(I.beam[F][((long long)tt.z * S.n1[F] + j) * nf + r] * bc_scaled) : 0.0f;
           const float interior = xb[r * PL4 + ty * BW + icol];
           xb[r * PL4 + ty * BW + gcol] = left ? 2.0f * (gval - bv) - interior : 2.0f * (bv + gval) - interior;
         }
@@ -358,7 +383,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
         const int crow = left ? 0 : ey - 1;   // the face cells' row in the target box
         const int grow = left ? 0 : ey;       // the ghost row in the y box
         const int irow = left ? 1 : ey - 1;   // the first interior row of F
-        for (int w = threadIdx.x; w < nx * nf; w += BLOCK) {
+        for (int w = threadIdx.x; w < nx * nf; w += TB) {
           const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
@@ -369,26 +394,110 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
       }
     }
   }
+  if constexpr (DIMS == 7 && !(C & 1)) {   // even in z: ghosts of C ^ 1 at z = 0 and z = n_C (the z box starts at z)
+    constexpr int F = C ^ 1;
+    constexpr int nf = Ord<N>::n(F);
+    if constexpr (nt > 0 && nf > 0) {
+      const int ncz = S.n2[C];
+      const double* B = ADJ ? I.bmat_a[2][F] : I.bmat_f[2][F];
+      const int nx = xv1 - xv0;
+      for (int side = 0; side < 2; ++side) {
+        const bool left = side == 0;
+        if (left ? tt.z != 0 : tt.z != ncz - 1) continue;
+        // every target point of the tile is on the face; the ghost plane and F's first interior
+        // plane are the two planes of the z box
+        const int gpl = left ? 0 : 1, ipl = left ? 1 : 0;
+        for (int w = threadIdx.x; w < ey * nx * nf; w += TB) {
+          const int r = w / (ey * nx), rest = w % (ey * nx);
+          const int ty = rest / nx, tx = xv0 + rest % nx;
+          float bv = 0.0f;
+#pragma unroll
+          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + ty * TX + tx], bv);
+          const float interior = zb[r * PLZ + ipl * PLO + ty * TX + tx];
+          zb[r * PLZ + gpl * PLO + ty * TX + tx] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
+        }
+      }
+    }
+  }
 }
 
-// One cell of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
+// the advection sum of one point from the staged boxes: x, then y, then z (advection_sum's order)
+template <int N, int C, bool NEG, int DIMS>
+__device__ __forceinline__ void staged_advection(float* acc, const float* xn, const float* yn, const float* zn,
+                                                 int xr, int xl, int yr, int yl, int zo, const TSolve& I) {
+  {
+    constexpr int F = C ^ 4;
+    if constexpr (Ord<N>::n(F) > 0) {
+      const float ih = I.inv_h[0];
+      auto diff = [&](int q) -> float {
+        const float a = xn[q * PL4 + xr];
+        const float b = xn[q * PL4 + xl];
+        const float d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> float {
+        (void)kk;
+        return float(lit);
+      };
+      Adv<N, C, 0>::template apply<float>(acc, diff, coef);
+    }
+  }
+  {
+    constexpr int F = C ^ 2;
+    if constexpr (Ord<N>::n(F) > 0) {
+      const float ih = I.inv_h[1];
+      auto diff = [&](int q) -> float {
+        const float a = yn[q * PL5 + yr];
+        const float b = yn[q * PL5 + yl];
+        const float d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> float {
+        (void)kk;
+        return float(lit);
+      };
+      Adv<N, C, 1>::template apply<float>(acc, diff, coef);
+    }
+  }
+  if constexpr (DIMS == 7) {
+    constexpr int F = C ^ 1;
+    if constexpr (Ord<N>::n(F) > 0) {
+      const float ih = I.inv_h[2];
+      auto diff = [&](int q) -> float {   // planes: 1 = j (odd) / j + 1 (even), 0 = j - 1 / j
+        const float a = zn[q * PLZ + PLO + zo];
+        const float b = zn[q * PLZ + zo];
+        const float d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> float {
+        (void)kk;
+        return float(lit);
+      };
+      Adv<N, C, 2>::template apply<float>(acc, diff, coef);
+    }
+  }
+}
+
+// One point of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
 // values replace the old ones in the target box.
-template <int N, int C, bool ADJ>
+template <int N, int C, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[BLOCK / 32][MAXR]) {
-  using LY = TmaLayout<N>;
+                                         double (&red)[TB / 32][MAXR]) {
+  using LY = TmaLayout<N, DIMS>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   float* own = reinterpret_cast<float*>(st + LY::OWN);
   {
     const ArgRow<N>& ar0 = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, ADJ ? 1 : 0>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
-                                   reinterpret_cast<float*>(st + LY::YN), ADJ ? 0.0 : ar0.bc);
+    tile_ghosts<N, C, ADJ ? 1 : 0, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                                         reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
+                                         ADJ ? 0.0 : ar0.bc);
     __syncthreads();
   }
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
+  const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
   const ArgRow<N>& ar = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
@@ -401,45 +510,13 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   if constexpr (n > 0) {
     if (valid) {
       const int i = tt.x0 + tx, j = tt.y0 + ty;
-      const int lo = ty * TX + tx;                              // the cell in the target / density boxes
+      const int lo = ty * TX + tx;                              // the point in the target / density / z boxes
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
       const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;     // rows j, j - 1 (odd) or j + 1, j of the y box
-      const float ihx = I.inv_h[0], ihy = I.inv_h[1];
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
-      {
-        constexpr int F = C ^ 4;
-        if constexpr (Ord<N>::n(F) > 0) {
-          auto diff = [&](int q) -> float {
-            const float a = xn[q * PL4 + xr];
-            const float b = xn[q * PL4 + xl];
-            const float d = ADJ ? (b - a) : (a - b);
-            return d * ihx;
-          };
-          auto coef = [&](int kk, double lit) -> float {
-            (void)kk;
-            return float(lit);
-          };
-          Adv<N, C, 0>::template apply<float>(acc, diff, coef);
-        }
-      }
-      {
-        constexpr int F = C ^ 2;
-        if constexpr (Ord<N>::n(F) > 0) {
-          auto diff = [&](int q) -> float {
-            const float a = yn[q * PL5 + yr];
-            const float b = yn[q * PL5 + yl];
-            const float d = ADJ ? (b - a) : (a - b);
-            return d * ihy;
-          };
-          auto coef = [&](int kk, double lit) -> float {
-            (void)kk;
-            return float(lit);
-          };
-          Adv<N, C, 1>::template apply<float>(acc, diff, coef);
-        }
-      }
+      staged_advection<N, C, ADJ, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
       float rr[MAXE];
       float S = 0.0f;
 #pragma unroll
@@ -467,7 +544,7 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
       }
       float q0 = 0.0f;
       long long ce = 0;
-      if constexpr (C == 0) ce = (long long)j * I.n0[0] + i;
+      if constexpr (C == 0) ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
       if constexpr (ADJ && C == 0) {
         double q = 0.0;
         for (int r = 0; r < I.nr; ++r)
@@ -509,7 +586,7 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
     if (threadIdx.x < L.pr) {
       double v = 0.0;
 #pragma unroll
-      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+      for (int q = 0; q < TB / 32; ++q) v += red[q][threadIdx.x];
       L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
     }
   }
@@ -518,21 +595,45 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     const CUtensorMap* mp = L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS;
     if (ADJ) {
-      tma_store_3d(mp + TM_LAM_T, tt.x0, tt.y0, 0, own);
+      tma_store_4d(mp + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, own);
     } else {
       const SubSlots sl = sub_slots(tt.ns, tt.n_ck, L.mode, L.j, L.sub, L.K);
-      tma_store_4d(mp + TM_ST_T, tt.x0, tt.y0, 0, sl.out, own);
+      tma_store_5d(mp + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.out, own);
     }
     bulk_commit();
   }
 }
 
-template <int N, bool ADJ>
-__global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_constant__ TLaunch<N> L) {
-  using LY = TmaLayout<N>;
+template <int N, bool ADJ, int DIMS>
+__device__ __forceinline__ void tma_cell_of(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
+                                            double (&red)[TB / 32][MAXR]) {
+  if constexpr (DIMS == 7) {
+    switch (tt.cls) {
+      case 0: tma_cell<N, 0, ADJ, DIMS>(L, tt, st, red); break;
+      case 1: tma_cell<N, 1, ADJ, DIMS>(L, tt, st, red); break;
+      case 2: tma_cell<N, 2, ADJ, DIMS>(L, tt, st, red); break;
+      case 3: tma_cell<N, 3, ADJ, DIMS>(L, tt, st, red); break;
+      case 4: tma_cell<N, 4, ADJ, DIMS>(L, tt, st, red); break;
+      case 5: tma_cell<N, 5, ADJ, DIMS>(L, tt, st, red); break;
+      case 6: tma_cell<N, 6, ADJ, DIMS>(L, tt, st, red); break;
+      default: tma_cell<N, 7, ADJ, DIMS>(L, tt, st, red); break;
+    }
+  } else {
+    switch (tt.cls) {
+      case 0: tma_cell<N, 0, ADJ, DIMS>(L, tt, st, red); break;
+      case 2: tma_cell<N, 2, ADJ, DIMS>(L, tt, st, red); break;
+      case 4: tma_cell<N, 4, ADJ, DIMS>(L, tt, st, red); break;
+      default: tma_cell<N, 6, ADJ, DIMS>(L, tt, st, red); break;
+    }
+  }
+}
+
+template <int N, bool ADJ, int DIMS>
+__global__ void __launch_bounds__(TB, 2) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
+  using LY = TmaLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
-  __shared__ double red[BLOCK / 32][MAXR];
+  __shared__ double red[TB / 32][MAXR];
   // tensor copies need 128-byte aligned destinations: refuse (uniformly) rather than fault
   if ((smem_u32(smem) & 127u) != 0u) {
     if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
@@ -549,7 +650,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
   if (threadIdx.x == 0)
     for (int k = 0; k < TSTAGES - 1; ++k) {
       const int t = t0 + k * G;
-      if (t < L.n_tiles) tma_issue<N, ADJ>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
+      if (t < L.n_tiles) tma_issue<N, ADJ, DIMS>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
     }
   for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
     const int s = k % TSTAGES;
@@ -558,7 +659,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
     if (ta < L.n_tiles && threadIdx.x == 0) {
       bulk_wait_read();   // the stores issued from that stage have read it
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tma_issue<N, ADJ>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
+      tma_issue<N, ADJ, DIMS>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
     const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
     if (__syncthreads_or(!ok)) {
@@ -574,18 +675,13 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_kernel(const __grid_cons
     }
     unsigned char* st = smem + s * LY::STAGE;
     const TTile& tt = *reinterpret_cast<const TTile*>(st + LY::TIL);
-    switch (tt.cls) {
-      case 0: tma_cell<N, 0, ADJ>(L, tt, st, red); break;
-      case 2: tma_cell<N, 2, ADJ>(L, tt, st, red); break;
-      case 4: tma_cell<N, 4, ADJ>(L, tt, st, red); break;
-      default: tma_cell<N, 6, ADJ>(L, tt, st, red); break;
-    }
+    tma_cell_of<N, ADJ, DIMS>(L, tt, st, red);
   }
   if (threadIdx.x == 0) bulk_wait_all();   // every store of this CTA has landed
 }
 
 // ---------------------------------------------------------------------------------------------
-// density integral of the adjoint (integrate_cell's arithmetic), every class of a 2D solve
+// density integral of the adjoint (integrate_cell's arithmetic), every class of a solve
 // ---------------------------------------------------------------------------------------------
 template <int N>
 struct TILaunch {
@@ -600,14 +696,16 @@ struct TILaunch {
   int K;
 };
 
-template <int N>
+template <int N, int DIMS>
 struct TmaIntLayout {
-  using B = TmaLayout<N>;
+  using B = TmaLayout<N, DIMS>;
+  static constexpr int NO = B::NO;
   static constexpr int OWN = 0;
-  static constexpr int LAM = OWN + B::al(B::NO * PLO * 4);
-  static constexpr int XN = LAM + B::al(B::NO * PLO * 4);
-  static constexpr int YN = XN + B::al(B::NXN * PL4 * 4);
-  static constexpr int RHO = YN + B::al(B::NYN * PL5 * 4);
+  static constexpr int LAM = OWN + B::al(NO * PLO * 4);
+  static constexpr int XN = LAM + B::al(NO * PLO * 4);
+  static constexpr int YN = XN + B::al(NO * PL4 * 4);
+  static constexpr int ZN = YN + B::al(NO * PL5 * 4);
+  static constexpr int RHO = ZN + (DIMS == 7 ? B::al(NO * PLZ * 4) : 0);
   static constexpr int RBAR = RHO + B::al(MAXE * PLO * 4);   // FP64
   static constexpr int ARG = RBAR + B::al(MAXE * PLO * 8);
   static constexpr int TIL = ARG + (int)sizeof(IntRow<N>);
@@ -616,33 +714,36 @@ struct TmaIntLayout {
   static constexpr int SMEM = TSTAGES * STAGE;
 };
 
-template <int N>
+template <int N, int DIMS>
 __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile& tt, unsigned char* st,
                                               unsigned long long* bar) {
-  using LY = TmaIntLayout<N>;
-  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2;
+  using LY = TmaIntLayout<N, DIMS>;
+  const int c = tt.cls, cx = c ^ 4, cy = c ^ 2, cz = c ^ 1;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
+  const int n_z = DIMS == 7 ? class_moments<N>(cz) : 0;
   const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
-  const unsigned bytes = 4u * (unsigned)(2 * PLO * n_own + PL4 * n_x + PL5 * n_y + PLO * tt.ne) +
+  const unsigned bytes = 4u * (unsigned)(2 * PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
                          8u * (unsigned)(PLO * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
   const int ya = tt.y0 - ((c >> 1) & 1);
+  const int za = tt.z - (c & 1);
   const int xa = tt.x0 - XO;
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
-  tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, 0, slot, bar);
-  tma_load_3d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, 0, bar);
-  if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, 0, slot, bar);
-  if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, 0, slot, bar);
-  tma_load_3d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, 0, bar);
-  tma_load_3d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, tt.x0, tt.y0, 0, bar);
+  tma_load_5d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, bar);
+  tma_load_4d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
+  if (n_x > 0) tma_load_5d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, tt.z, 0, slot, bar);
+  if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, tt.z, 0, slot, bar);
+  if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, slot, bar);
+  tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
+  tma_load_4d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, tt.x0, tt.y0, tt.z, 0, bar);
   bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
 }
 
-template <int N, int C>
+template <int N, int C, int DIMS>
 __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& tt, unsigned char* st) {
-  using LY = TmaIntLayout<N>;
+  using LY = TmaIntLayout<N, DIMS>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
@@ -650,8 +751,8 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   double* rbs = reinterpret_cast<double*>(st + LY::RBAR);
   {
     const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, 2>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
-                         reinterpret_cast<float*>(st + LY::YN), ar0.bc);
+    tile_ghosts<N, C, 2, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                               reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN), ar0.bc);
     __syncthreads();
   }
   if constexpr (n > 0) {
@@ -661,38 +762,17 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const float* lam = reinterpret_cast<const float*>(st + LY::LAM);
       const float* xn = reinterpret_cast<const float*>(st + LY::XN);
       const float* yn = reinterpret_cast<const float*>(st + LY::YN);
+      const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
       const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
       const IntRow<N>& ar = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
       const int i = tt.x0 + tx, j = tt.y0 + ty;
       const int lo = ty * TX + tx;
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
       const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;
-      const float ihx = I.inv_h[0], ihy = I.inv_h[1];
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
-      {
-        constexpr int F = C ^ 4;
-        if constexpr (Ord<N>::n(F) > 0) {
-          auto diff = [&](int q) -> float { return (xn[q * PL4 + xr] - xn[q * PL4 + xl]) * ihx; };
-          auto coef = [&](int kk, double lit) -> float {
-            (void)kk;
-            return float(lit);
-          };
-          Adv<N, C, 0>::template apply<float>(acc, diff, coef);
-        }
-      }
-      {
-        constexpr int F = C ^ 2;
-        if constexpr (Ord<N>::n(F) > 0) {
-          auto diff = [&](int q) -> float { return (yn[q * PL5 + yr] - yn[q * PL5 + yl]) * ihy; };
-          auto coef = [&](int kk, double lit) -> float {
-            (void)kk;
-            return float(lit);
-          };
-          Adv<N, C, 1>::template apply<float>(acc, diff, coef);
-        }
-      }
+      staged_advection<N, C, false, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
       float rr[MAXE];
       float S = 0.0f;
 #pragma unroll
@@ -733,12 +813,12 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
 #pragma unroll
           for (int l = 0; l <= N; ++l)
             if ((mask >> l) & 1u) v += ar.c[e][l] * R[l];
-          const double old = rbs[e * PLO + lo];   // this cell's rho_bar, staged with the tile
+          const double old = rbs[e * PLO + lo];   // this point's rho_bar, staged with the tile
           rbs[e * PLO + lo] = old + double(v) * ar.wfac;
         }
       }
       if constexpr (C == 0) {
-        const long long ce = (long long)j * I.n0[0] + i;
+        const long long ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
         const double u0 = double(own[lo]);
         for (int r = 0; r < I.nr; ++r) {
           const double cr = ar.coef[r] * I.ibar[r];
@@ -752,14 +832,37 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   __syncthreads();   // the rho_bar box holds the new values
   if (threadIdx.x == 0) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tma_store_3d(L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS + TM_RBAR, tt.x0, tt.y0, 0, rbs);
+    tma_store_4d(L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS + TM_RBAR, tt.x0, tt.y0, tt.z, 0, rbs);
     bulk_commit();
   }
 }
 
-template <int N>
-__global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_constant__ TILaunch<N> L) {
-  using LY = TmaIntLayout<N>;
+template <int N, int DIMS>
+__device__ __forceinline__ void tma_int_cell_of(const TILaunch<N>& L, const TTile& tt, unsigned char* st) {
+  if constexpr (DIMS == 7) {
+    switch (tt.cls) {
+      case 0: tma_int_cell<N, 0, DIMS>(L, tt, st); break;
+      case 1: tma_int_cell<N, 1, DIMS>(L, tt, st); break;
+      case 2: tma_int_cell<N, 2, DIMS>(L, tt, st); break;
+      case 3: tma_int_cell<N, 3, DIMS>(L, tt, st); break;
+      case 4: tma_int_cell<N, 4, DIMS>(L, tt, st); break;
+      case 5: tma_int_cell<N, 5, DIMS>(L, tt, st); break;
+      case 6: tma_int_cell<N, 6, DIMS>(L, tt, st); break;
+      default: tma_int_cell<N, 7, DIMS>(L, tt, st); break;
+    }
+  } else {
+    switch (tt.cls) {
+      case 0: tma_int_cell<N, 0, DIMS>(L, tt, st); break;
+      case 2: tma_int_cell<N, 2, DIMS>(L, tt, st); break;
+      case 4: tma_int_cell<N, 4, DIMS>(L, tt, st); break;
+      default: tma_int_cell<N, 6, DIMS>(L, tt, st); break;
+    }
+  }
+}
+
+template <int N, int DIMS>
+__global__ void __launch_bounds__(TB, 2) batch_tma_int_kernel(const __grid_constant__ TILaunch<N> L) {
+  using LY = TmaIntLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
   if ((smem_u32(smem) & 127u) != 0u) {
@@ -776,7 +879,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
   if (threadIdx.x == 0)
     for (int k = 0; k < TSTAGES - 1; ++k) {
       const int t = t0 + k * G;
-      if (t < L.n_tiles) tma_issue_int<N>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
+      if (t < L.n_tiles) tma_issue_int<N, DIMS>(L, L.tiles[t], smem + k * LY::STAGE, &full[k]);
     }
   for (int k = 0; t0 + k * G < L.n_tiles; ++k) {
     const int s = k % TSTAGES;
@@ -785,7 +888,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
     if (ta < L.n_tiles && threadIdx.x == 0) {
       bulk_wait_read();
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      tma_issue_int<N>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
+      tma_issue_int<N, DIMS>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
     const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
     if (__syncthreads_or(!ok)) {
@@ -800,12 +903,7 @@ __global__ void __launch_bounds__(BLOCK, 2) batch_tma2d_int_kernel(const __grid_
     }
     unsigned char* st = smem + s * LY::STAGE;
     const TTile& tt = *reinterpret_cast<const TTile*>(st + LY::TIL);
-    switch (tt.cls) {
-      case 0: tma_int_cell<N, 0>(L, tt, st); break;
-      case 2: tma_int_cell<N, 2>(L, tt, st); break;
-      case 4: tma_int_cell<N, 4>(L, tt, st); break;
-      default: tma_int_cell<N, 6>(L, tt, st); break;
-    }
+    tma_int_cell_of<N, DIMS>(L, tt, st);
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }
@@ -832,13 +930,14 @@ inline EncodeTiledFn encode_tiled_fn() {
   return fn;
 }
 
-// tensor of rank 3 (x, y, plane) or 4 (x, y, plane, slot) of 4- or 8-byte floats; strides in elements
+// tensor of rank 4 (x, y, z, moment) or 5 (x, y, z, moment, slot) of 4- or 8-byte floats; strides
+// in elements
 inline bool encode_tensor(CUtensorMap* out, void* base, int rank, const long long* dims, const long long* strides,
                           const int* box, int elem_bytes) {
   EncodeTiledFn fn = encode_tiled_fn();
-  if (!fn) return false;
-  cuuint64_t gd[4], gs[3];
-  cuuint32_t bd[4], es[4];
+  if (!fn || rank < 1 || rank > 5) return false;
+  cuuint64_t gd[5], gs[4];
+  cuuint32_t bd[5], es[5];
   for (int d = 0; d < rank; ++d) {
     gd[d] = (cuuint64_t)dims[d];
     bd[d] = (cuuint32_t)box[d];

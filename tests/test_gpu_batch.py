@@ -113,16 +113,27 @@ def tma_solves():
     ]
 
 
+def tma_solves_3d():
+    """FP32 3D solves for the TMA tiles: every class, z faces on both sides, narrow z extents."""
+    return [
+        workloads.small_case(dims=3, N=3, shape=(36, 9, 6), n_steps=5, seed=21, precision=PN_FP32),
+        workloads.small_case(dims=3, N=5, shape=(40, 8, 5), n_steps=4, seed=22, precision=PN_FP32),
+        workloads.small_case(dims=3, N=7, shape=(33, 10, 4), n_steps=3, seed=23, precision=PN_FP32,
+                             elements=("Fe", "Cr", "Ni")),
+        workloads.small_case(dims=3, N=3, shape=(12, 5, 3), n_steps=6, seed=24, precision=PN_FP32),
+    ]
+
+
 @pytest.mark.parametrize("K", [1, 3])
 def test_tma_tiles_match_the_generic_kernels(gpu_lib, K):
     """Every cell update and ghost point is the same arithmetic on both paths, so states and
     gradients agree bit for bit; the intensity partial sums group the cells by the path's own
     tiles, so intensities agree to rounding."""
     torch = pytest.importorskip("torch")
-    solves = tma_solves()
+    solves = tma_solves() + tma_solves_3d()
     ref = run_batch(torch, solves, K=K, flags=capi.PN_BATCH_GENERIC_KERNELS)
     got = run_batch(torch, solves, K=K, ibar=ref[1])
-    assert got[5].tma_groups == got[5].n_groups == 4
+    assert got[5].tma_groups == got[5].n_groups == 7
     assert ref[5].tma_groups == 0
     for x, y in zip(got[0], ref[0]):
         assert rel(x, y) < 1e-13
@@ -145,11 +156,27 @@ def test_tma_tiles_against_the_oracle(gpu_lib, oracle):
         assert rel(rb[q], rb_o) < 1e-3
 
 
+def test_tma_tiles_3d_against_the_oracle(gpu_lib, oracle):
+    torch = pytest.importorskip("torch")
+    solves = [tma_solves_3d()[3]]
+    I, ib, rb, nb, ab, info = run_batch(torch, solves)
+    assert info.tma_groups == 1
+    s = solves[0]
+    rho, noa, acs = s.inputs()
+    s.problem.precision = PN_FP64
+    d, k = s.problem.descriptor(s.x_rays)
+    I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[0])
+    assert rel(I[0], I_o) < 1e-4
+    assert rel(rb[0], rb_o) < 1e-3
+    assert rel(nb[0], nb_o) < 1e-3
+    assert rel(ab[0], ab_o) < 1e-3
+
+
 def test_direct_launches_match_the_graphs(gpu_lib):
     """PN_BATCH_DIRECT_LAUNCH issues the same kernels from the host instead of replaying the
     captured graphs: identical results."""
     torch = pytest.importorskip("torch")
-    solves = mixed_solves(PN_FP32) + tma_solves()[:2]
+    solves = mixed_solves(PN_FP32) + tma_solves()[:2] + tma_solves_3d()[:1]
     ref = run_batch(torch, solves)
     got = run_batch(torch, solves, flags=capi.PN_BATCH_DIRECT_LAUNCH, ibar=ref[1])
     for a, b in zip(got[:5], ref[:5]):
