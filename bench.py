@@ -49,6 +49,8 @@ def parse():
                     help="run one 10 keV solve (FP64 twice, FP32 once) for a profiler, print nothing else")
     ap.add_argument("--profile-batch", action="store_true",
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
+    ap.add_argument("--profile-positions", type=int, default=16, help="beam positions of --profile-batch")
+    ap.add_argument("--profile-budget-gb", type=float, default=6.0, help="tape budget of --profile-batch")
     ap.add_argument("--serve", action="store_true",
                     help="served stream: Poisson requests (1D/2D/3D mix) through pn_server; prints its own line")
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -513,19 +515,19 @@ def run_profile(args):
 
 
 def run_profile_batch(args):
-    """FP32 batch of 16 beam positions at 10 keV (state 160 MB > L2), forward + adjoint twice, tapes
-    within 6 GiB."""
+    """FP32 batch of beam positions at 10 keV (16 positions: state 160 MB > L2), forward + adjoint
+    twice, tapes within the given budget (6 GiB by default)."""
     import torch
     from pnepma_gb300 import capi, workloads
     from pnepma_gb300.problem import PN_FP32
     torch.cuda.set_device(0)
-    solves = workloads.config2(n_positions=16, energies=(10.0,), precision=PN_FP32)
+    solves = workloads.config2(n_positions=args.profile_positions, energies=(10.0,), precision=PN_FP32)
     descs, keep = [], []
     for s in solves:
         d, k = s.problem.descriptor(s.x_rays)
         descs.append(d)
         keep.append(k)
-    b = capi.Batch(descs, keep, memory_budget=6 << 30)
+    b = capi.Batch(descs, keep, memory_budget=int(args.profile_budget_gb * (1 << 30)))
     rho, noa, acs = solves[0].inputs()
     dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)
