@@ -51,6 +51,12 @@ def parse():
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
     ap.add_argument("--profile-positions", type=int, default=16, help="beam positions of --profile-batch")
     ap.add_argument("--profile-budget-gb", type=float, default=6.0, help="tape budget of --profile-batch")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="energy steps of --profile-3d (0: the stable step count; fewer steps exceed the "
+                         "stable step, which leaves the kernels' work unchanged)")
+    ap.add_argument("--profile-3d", action="store_true",
+                    help="run the 3D 96x96x64 P7 FP32 solve once (forward + adjoint, tapes within "
+                         "--profile-budget-gb) for a profiler")
     ap.add_argument("--serve", action="store_true",
                     help="served stream: Poisson requests (1D/2D/3D mix) through pn_server; prints its own line")
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -75,8 +81,9 @@ def workload(positions):
 
 
 def algorithmic_bytes_per_step(solve, elem):
-    """Bytes one energy step moves in the sub-step kernels: s_u (4 M_even + 5 M_odd) +
-    8 n_e (2 C_odd + C_even), M = interior values, C = interior cells of each parity."""
+    """Bytes one energy step moves in the sub-step kernels: s (4 M_even + 5 M_odd) +
+    s n_e (2 C_odd + C_even), M = interior values, C = interior cells of each parity, s = the
+    element size of the state and the densities (both are stored in the solve's precision)."""
     g = solve.problem.gspec
     from pnepma_gb300.moments import class_sizes, parity
     nm = class_sizes(solve.problem.N)
@@ -90,7 +97,7 @@ def algorithmic_bytes_per_step(solve, elem):
         M[parity(c)] += cells * nm[c]
         C[parity(c)] += cells
     ne = len(solve.problem.elements)
-    return elem * (4 * M[0] + 5 * M[1]) + 8 * ne * (2 * C[1] + C[0]), M[0] + M[1]
+    return elem * (4 * M[0] + 5 * M[1]) + elem * ne * (2 * C[1] + C[0]), M[0] + M[1]
 
 
 class Clocks:
@@ -549,6 +556,40 @@ def run_profile_batch(args):
     info = b.info()
     print(json.dumps({"profile_batch": len(solves), "steps": solves[0].problem.N_steps,
                       "stride": info.checkpoint_stride, "bytes": info.device_bytes,
+                      "kernels": info.forward_kernels + info.adjoint_kernels}))
+    b.close()
+
+
+def run_profile_3d(args):
+    """The 3D 96 x 96 x 64 P7 solve (state 153 MB > L2) as a one-solve FP32 batch: forward and adjoint
+    once, tapes within the given budget."""
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.problem import PN_FP32
+    torch.cuda.set_device(0)
+    if args.profile_steps > 0:
+        s = workloads.config4(precision=PN_FP32, stabilise=False, n_steps=args.profile_steps)
+    else:
+        s = workloads.config4(precision=PN_FP32)
+    d, k = s.problem.descriptor(s.x_rays)
+    b = capi.Batch([d], [k], memory_budget=int(args.profile_budget_gb * (1 << 30)))
+    rho, noa, acs = s.inputs()
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)
+    nr = len(s.x_rays)
+    sz = capi.query_sizes(d)
+    I = torch.zeros(nr, dtype=torch.float64, device="cuda")
+    rb = torch.zeros(sz.n_rho, dtype=torch.float64, device="cuda")
+    nb = torch.zeros(sz.n_noa, dtype=torch.float64, device="cuda")
+    ab = torch.zeros(sz.n_acs, dtype=torch.float64, device="cuda")
+    b.forward([d_rho.data_ptr()], [d_noa.data_ptr()], [d_acs.data_ptr()], [I.data_ptr()])
+    torch.cuda.synchronize()
+    ib = 1.0 / I.abs()
+    b.adjoint([ib.data_ptr()], [rb.data_ptr()], [nb.data_ptr()], [ab.data_ptr()])
+    torch.cuda.synchronize()
+    info = b.info()
+    print(json.dumps({"profile_3d": 1, "steps": s.problem.N_steps, "stride": info.checkpoint_stride,
+                      "bytes": info.device_bytes, "tma_groups": info.tma_groups,
                       "kernels": info.forward_kernels + info.adjoint_kernels}))
     b.close()
 
@@ -1052,6 +1093,8 @@ def main():
         run_profile(args)
     elif args.profile_batch:
         run_profile_batch(args)
+    elif args.profile_3d:
+        run_profile_3d(args)
     elif args.serve:
         run_serve(args)
     elif args.config4:
