@@ -230,16 +230,19 @@ typedef struct pn_batch pn_batch;
 
 typedef struct pn_batch_options {
   int64_t memory_budget;      /* bytes of device memory for the tapes; 0 = half of the free memory */
-  int32_t checkpoint_stride;  /* 0 = smallest stride whose tapes fit the budget; K >= 1 forces K */
+  int32_t checkpoint_stride;  /* 0 = the tape that recomputes the fewest steps within the budget
+                                 (every state when it fits; else the first A states in full and
+                                 every K-th beyond them); K >= 1 forces stride K, no full head */
   int32_t flags;              /* pn_batch_flags */
 } pn_batch_options;
 
 enum pn_batch_flags {
-  /* FP32 2D groups stage their box tiles with TMA unless this is set; the generic kernels give
-     bit-identical results (for comparison and diagnosis) */
+  /* FP32 2D (x, y) and 3D groups run their sub-steps on TMA tiles (with sub-steps 3 and 1 of
+     consecutive energy steps fused into one launch) unless this is set; the generic kernels give
+     bit-identical states and gradients (for comparison and diagnosis) */
   PN_BATCH_GENERIC_KERNELS = 1,
   /* issue the kernels of every sweep on the caller's stream instead of capturing the sweeps as
-     CUDA graphs at creation: cheaper for a batch that runs once (each call then launches ~3
+     CUDA graphs at creation: cheaper for a batch that runs once (each call then launches 2-3
      kernels per energy step from the host) */
   PN_BATCH_DIRECT_LAUNCH = 2
 };
@@ -252,6 +255,7 @@ typedef struct pn_batch_info {
   int64_t device_bytes;
   int64_t forward_kernels;    /* kernel launches of one pn_batch_forward */
   int64_t adjoint_kernels;    /* kernel launches of one pn_batch_adjoint */
+  int64_t recomputed_steps;   /* forward energy steps one pn_batch_adjoint recomputes, all solves */
 } pn_batch_info;
 
 int pn_batch_create(const pn_desc* const* descs, int32_t n, const pn_batch_options* options, pn_batch** out);

@@ -40,7 +40,7 @@ class PnBatchInfo(ctypes.Structure):
     _fields_ = [("n_solves", ctypes.c_int32), ("n_groups", ctypes.c_int32),
                 ("checkpoint_stride", ctypes.c_int32), ("tma_groups", ctypes.c_int32),
                 ("device_bytes", ctypes.c_int64), ("forward_kernels", ctypes.c_int64),
-                ("adjoint_kernels", ctypes.c_int64)]
+                ("adjoint_kernels", ctypes.c_int64), ("recomputed_steps", ctypes.c_int64)]
 
 
 class PnServerOptions(ctypes.Structure):

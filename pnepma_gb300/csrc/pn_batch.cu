@@ -237,12 +237,14 @@ int pn_batch_query(const pn_batch* b, pn_batch_info* info) {
   info->device_bytes = 0;
   info->forward_kernels = 0;
   info->adjoint_kernels = 0;
+  info->recomputed_steps = 0;
   for (auto* g : b->groups) {
     info->checkpoint_stride = std::max(info->checkpoint_stride, g->stride());
     info->tma_groups += g->tma() ? 1 : 0;
     info->device_bytes += g->device_bytes();
     info->forward_kernels += g->launches_forward();
     info->adjoint_kernels += g->launches_adjoint();
+    info->recomputed_steps += g->recomputed_steps();
   }
   try {
     const int st = pn::batch_status(const_cast<pn_batch*>(b));

@@ -9,10 +9,18 @@
 // solves with n_steps == a).  So the solves active in any launch are a prefix of the sorted
 // list, and the tile list of each launch is a prefix of one fixed, solve-major tile list.
 //
-// Checkpoints.  With stride K, state j is kept when j % K == 0; the adjoint walks segments
-// [mK, (m+1)K) and first recomputes states mK+1 .. (m+1)K-1 from state (m+1)K (or from the zero
-// state).  Because the schedule is aligned in j, every solve checkpoints and recomputes at the
-// same launches.  K = 1 keeps every state.
+// Checkpoints.  States 0 .. A-1 (the first ones the adjoint needs, the last ones the forward
+// produces) are all kept; beyond them, with stride K, state j is kept when (j - A) % K == 0.  The
+// adjoint first walks iterations 0 .. A-1 on kept states, then segments [A + mK, A + (m+1)K), each
+// after recomputing its states A + mK + 1 .. A + (m+1)K - 1 from state A + (m+1)K (or from the
+// zero state).  Because the schedule is aligned in j, every solve checkpoints and recomputes at the
+// same launches.  K = 1 keeps every state; A and K are chosen together to recompute the fewest
+// steps within the memory budget.
+//
+// Fused sub-steps (TMA groups).  Sub-step 3 of step j and sub-step 1 of step j - 1 both update the
+// odd classes from the even classes of state j, which no launch changes in between; one launch
+// runs both on each tile (loads once, updates twice), so a march of n steps takes 2n + 1 launches
+// instead of 3n.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -54,8 +62,10 @@ struct BInst {
   Geom g[8];
   long long dev_off[8];
   long long slot_elems;
-  T* slots;               // [0] zero state, [1 .. n_ck] checkpoints, then work slots
+  T* slots;               // [0] zero state, [1 .. n_full] states 0 .. n_full - 1, then the
+                          // checkpoints of states n_full, n_full + K, ..., then work slots
   T* lam;
+  int n_full;             // states kept in full (the first the adjoint sweep needs)
   int n_ck;
   int ns, ne, nr, N1;
   int act[3];
@@ -183,12 +193,16 @@ struct BInt {
   T inv_h[3];
 };
 
+// Slot of state j: the zero state past the end of the march, a kept state, a checkpoint, or a
+// work slot (alternating in the forward sweep; one per state of a recomputed segment).
 template <class T>
-__device__ __forceinline__ T* bslot(const BInst<T>& I, int j, int K, bool segment, int m) {
+__device__ __forceinline__ T* bslot(const BInst<T>& I, int j, int K, bool segment) {
   if (j >= I.ns) return I.slots;
-  if (j % K == 0) return I.slots + (long long)(1 + j / K) * I.slot_elems;
-  const int w = segment ? (j - m * K - 1) : (j & 1);
-  return I.slots + (long long)(1 + I.n_ck + w) * I.slot_elems;
+  if (j < I.n_full) return I.slots + (long long)(1 + j) * I.slot_elems;
+  const int r = j - I.n_full;
+  if (r % K == 0) return I.slots + (long long)(1 + I.n_full + r / K) * I.slot_elems;
+  const int w = segment ? (r % K - 1) : (j & 1);
+  return I.slots + (long long)(1 + I.n_full + I.n_ck + w) * I.slot_elems;
 }
 
 // Words of a BInst before its segment tables: what a block stages (the segments are read from
@@ -221,9 +235,8 @@ __device__ __forceinline__ void fill_sub(BSub<T, N>& a, const BInst<T>& I, const
   T* from_rd;
   if (!ADJ) {
     const bool segment = L.mode == BM_RECOMPUTE;
-    const int m = L.j / L.K;
-    T* src = bslot(I, L.j + 1, L.K, segment, m);
-    T* dst = bslot(I, L.j, L.K, segment, m);
+    T* src = bslot(I, L.j + 1, L.K, segment);
+    T* dst = bslot(I, L.j, L.K, segment);
     own_rd = (L.sub == 3) ? dst : src;
     own_wr = dst;
     from_rd = (L.sub == 1) ? src : dst;
@@ -341,7 +354,7 @@ __device__ __forceinline__ void fill_int(BInt<T, N>& a, const BInst<T>& I, const
   const int tid = threadIdx.x;
   if (tid < 8) {
     const int c = tid;
-    T* u = bslot(I, it, L.K, true, it / L.K);
+    T* u = bslot(I, it, L.K, true);
     a.g[c] = I.g[c];
     a.u[c] = I.active[c] ? u + I.dev_off[c] : nullptr;
     a.lam[c] = I.active[c] ? I.lam + I.dev_off[c] : nullptr;
@@ -573,6 +586,8 @@ class BatchGroup : public BatchGroupBase {
   double* partial = nullptr;
   int n_ptiles = 0, pr = 1;   // compact partials: eee tiles of all solves, line stride
   int max_ns = 0, K = 1, n = 0;
+  int A = 0;                   // states 0 .. A-1 kept in full
+  long long recomputed = 0;    // forward steps one adjoint recomputes (all solves)
   std::vector<void*> allocs;
   long long bytes = 0;
   cudaGraphExec_t gf = nullptr, ga = nullptr;
@@ -625,6 +640,7 @@ class BatchGroup : public BatchGroupBase {
   long long launches_forward() const override { return nl_f + 2; }
   long long launches_adjoint() const override { return nl_a + 2; }
   int stride() const override { return K; }
+  long long recomputed_steps() const override { return recomputed; }
   bool tma() const override { return use_tma; }
   int device_status() override {
     if (!dstatus) return PN_OK;
@@ -719,7 +735,8 @@ class BatchGroup : public BatchGroupBase {
     return cnt;
   }
 
-  static int n_ck_for(int ns, int K) { return (ns - 1) / K + 1; }
+  // checkpoints of the states a .. ns - 1 beyond a kept head of a states
+  static int n_ck_for(int ns, int K, int a) { return ns > a ? (ns - a - 1) / K + 1 : 0; }
 
   // tiles per block: enough blocks to fill the GPU about twice (SMs x 5 resident blocks), at
   // most PN_BATCH_MAX_TPB tiles each
@@ -749,20 +766,49 @@ class BatchGroup : public BatchGroupBase {
       slot_total += Ls[q].slot_elems * (long long)sizeof(T);
       (void)fixed;
     }
-    // checkpoint stride: smallest K whose tapes fit the budget
-    auto need = [&](int k) {
+    // tape: the stride K and kept head A that recompute the fewest state values within the budget
+    // (K = 1 when every state fits); an explicit stride keeps no head
+    auto need = [&](int k, int a) {
       long long b = 0;
       for (int q = 0; q < n; ++q)
-        b += (long long)(1 + n_ck_for(Ls[q].ns, k) + n_work_for(k) + 1) * Ls[q].slot_elems * (long long)sizeof(T);
+        b += (long long)(1 + std::min(a, Ls[q].ns) + n_ck_for(Ls[q].ns, k, a) + n_work_for(k) + 1) *
+             Ls[q].slot_elems * (long long)sizeof(T);
       return b;
     };
-    if (Kreq > 0) K = Kreq;
-    else {
+    auto cost = [&](int k, int a) {   // recomputed state values
+      long long c = 0;
+      for (int q = 0; q < n; ++q)
+        if (Ls[q].ns > a) c += (long long)(Ls[q].ns - a - n_ck_for(Ls[q].ns, k, a)) * Ls[q].slot_elems;
+      return c;
+    };
+    if (Kreq > 0) {
+      K = std::min(Kreq, std::max(1, max_ns));
+      A = 0;
+    } else if (need(1, 0) <= budget) {
       K = 1;
-      while (K < max_ns && need(K) > budget) ++K;
-      if (need(K) > budget) { err = "the batch does not fit the memory budget"; return PN_ERR_NO_MEMORY; }
+      A = 0;
+    } else {
+      long long best = -1;
+      for (int k = 2; k <= std::max(2, max_ns); ++k) {
+        if (need(k, 0) > budget) continue;
+        int lo = 0, hi = max_ns;   // largest a with need(k, a) <= budget (need grows with a)
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) / 2;
+          if (need(k, mid) <= budget) lo = mid;
+          else hi = mid - 1;
+        }
+        const long long c = cost(k, lo);
+        if (best < 0 || c < best) {
+          best = c;
+          K = k;
+          A = lo;
+        }
+      }
+      if (best < 0) { err = "the batch does not fit the memory budget"; return PN_ERR_NO_MEMORY; }
     }
-    if (K > max_ns) K = max_ns;
+    recomputed = 0;
+    for (int q = 0; q < n; ++q)
+      if (Ls[q].ns > A) recomputed += Ls[q].ns - A - n_ck_for(Ls[q].ns, K, A);
     hinst.assign(n, BInst<T>());
     cur_descs.assign(n, nullptr);
     for (int q = 0; q < n; ++q) cur_descs[q] = d[members[q]];
@@ -936,7 +982,7 @@ class BatchGroup : public BatchGroupBase {
       std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
       for (int q = 0; q < n; ++q) {
         const BInst<T>& I = hinst[q];
-        const long long nslots = 1 + I.n_ck + n_work_for(K);
+        const long long nslots = 1 + I.n_full + I.n_ck + n_work_for(K);
         for (int c = 0; c < 8; ++c) {
           const int nm = I.g[c].nm;
           if (!I.active[c] || nm == 0) continue;
@@ -1032,6 +1078,7 @@ class BatchGroup : public BatchGroupBase {
                 tt.pslot = (list == 0 && c == 0) ? n_ptiles++ : -1;
                 tt.ns = I.ns;
                 tt.n_ck = I.n_ck;
+                tt.n_full = I.n_full;
                 tt.ne = I.ne;
                 tt.arg_fwd = arg_fwd[q];
                 tt.arg_adj = arg_adj[q];
@@ -1085,8 +1132,9 @@ class BatchGroup : public BatchGroupBase {
     const int ns = L.ns, ne = L.ne, nr = L.nr, N1 = N + 1;
     I.ns = ns; I.ne = ne; I.nr = nr; I.N1 = N1;
     I.slot_elems = L.slot_elems;
-    I.n_ck = n_ck_for(ns, K);
-    const int nslots = 1 + I.n_ck + n_work_for(K);
+    I.n_full = std::min(A, ns);
+    I.n_ck = n_ck_for(ns, K, A);
+    const int nslots = 1 + I.n_full + I.n_ck + n_work_for(K);
     if ((rc = alloc(I.slots, (long long)nslots * L.slot_elems))) return rc;
     if ((rc = alloc(I.lam, L.slot_elems))) return rc;
     zero_ranges.emplace_back((void*)I.slots, sizeof(T) * (size_t)nslots * L.slot_elems);
@@ -1329,9 +1377,11 @@ class BatchGroup : public BatchGroupBase {
   // TMA path of a sub-step: every target cell (face tiles compute their ghosts in place)
   int launch_tma(int list, int mode, int j, int sub, double* part, bool adj) {
     if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
+      // solves active at step j (a fused launch also runs step j - 1)
+      const int jmin = sub == 4 ? j - 1 : j;
       int last = -1;
       for (int q = 0; q < n; ++q)
-        if (hinst[q].ns > j) last = q;
+        if (hinst[q].ns > jmin) last = q;
       if (last < 0) return PN_OK;
       const int nb = tend[list][last];
       if (nb > 0) {
@@ -1392,11 +1442,34 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  int fwd_step(int j, int mode, double* part) {
+  // forward steps j = top down to bot (the forward sweep with intensity partials, or a recomputed
+  // segment): sub-steps 1, 2, 3 per step, or with TMA tiles sub-step 3 of each step fused with
+  // sub-step 1 of the next
+  int fwd_steps(int top, int bot, int mode, bool partials) {
     int rc;
-    if ((rc = launch(1, mode, j, 1, nullptr, false, false))) return rc;
-    if ((rc = launch(0, mode, j, 2, part, false, false))) return rc;
-    if ((rc = launch(1, mode, j, 3, nullptr, false, false))) return rc;
+    auto part = [&](int j) { return partials ? partial + (long long)(max_ns - j - 1) * n_ptiles * pr : nullptr; };
+    if (!use_tma) {
+      for (int j = top; j >= bot; --j) {
+        if ((rc = launch(1, mode, j, 1, nullptr, false, false))) return rc;
+        if ((rc = launch(0, mode, j, 2, part(j), false, false))) return rc;
+        if ((rc = launch(1, mode, j, 3, nullptr, false, false))) return rc;
+      }
+      return PN_OK;
+    }
+    if ((rc = launch(1, mode, top, 1, nullptr, false, false))) return rc;
+    for (int j = top; j >= bot; --j) {
+      if ((rc = launch(0, mode, j, 2, part(j), false, false))) return rc;
+      if ((rc = launch(1, mode, j, j > bot ? 4 : 3, nullptr, false, false))) return rc;
+    }
+    return PN_OK;
+  }
+
+  // adjoint iteration a: density integral on state a, then the three adjoint sub-steps
+  int adj_iter(int a) {
+    int rc;
+    if ((rc = launch(2, BM_ADJOINT, a, 0, nullptr, false, true))) return rc;
+    for (int sub = 1; sub <= 3; ++sub)
+      if ((rc = launch(sub == 2 ? 0 : 1, BM_ADJOINT, a, sub, nullptr, true, false))) return rc;
     return PN_OK;
   }
 
@@ -1406,11 +1479,7 @@ class BatchGroup : public BatchGroupBase {
     if (fwd) {
       batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 0);
       PN_CUDA(cudaGetLastError());
-      for (int t = 1; t <= max_ns; ++t) {
-        const int j = max_ns - t;
-        double* part = partial + (long long)(t - 1) * n_ptiles * pr;
-        if ((rc = fwd_step(j, BM_FORWARD, part))) return rc;
-      }
+      if ((rc = fwd_steps(max_ns - 1, 0, BM_FORWARD, true))) return rc;
       batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, ls>>>(dinst, partial, max_ns, n_ptiles, pr);
       batch_final_kernel<T><<<n, 32, 0, ls>>>(dinst);
       PN_CUDA(cudaGetLastError());
@@ -1419,19 +1488,16 @@ class BatchGroup : public BatchGroupBase {
       batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 1);
       PN_CUDA(cudaGetLastError());
       nl += 1;
-      for (int m = 0; m * K < max_ns; ++m) {
-        // recompute states (m+1)K-1 .. mK+1 of this segment
-        for (int j = std::min((m + 1) * K, max_ns) - 1; j >= m * K + 1; --j)
-          if ((rc = fwd_step(j, BM_RECOMPUTE, nullptr))) return rc;
-        for (int a = m * K; a < std::min((m + 1) * K, max_ns + 1); ++a) {
-          if ((rc = launch(2, BM_ADJOINT, a, 0, nullptr, false, true))) return rc;
-          for (int sub = 1; sub <= 3; ++sub)
-            if ((rc = launch(sub == 2 ? 0 : 1, BM_ADJOINT, a, sub, nullptr, true, false))) return rc;
-        }
+      // iterations on the kept head, then segments [s0, s0 + K) after recomputing s0 + 1 .. s0 + K - 1;
+      // iteration max_ns is the final accumulation of the longest solves on the zero state
+      for (int a = 0; a < std::min(A, max_ns + 1); ++a)
+        if ((rc = adj_iter(a))) return rc;
+      for (int s0 = A; s0 <= max_ns; s0 += K) {
+        const int top = std::min(s0 + K, max_ns) - 1;
+        if (top >= s0 + 1 && (rc = fwd_steps(top, s0 + 1, BM_RECOMPUTE, false))) return rc;
+        for (int a = s0; a < std::min(s0 + K, max_ns + 1); ++a)
+          if ((rc = adj_iter(a))) return rc;
       }
-      // final accumulation of the longest solves (ns == max_ns) when max_ns is a multiple of K
-      if (max_ns % K == 0)
-        if ((rc = launch(2, BM_ADJOINT, max_ns, 0, nullptr, false, true))) return rc;
     }
     return PN_OK;
   }

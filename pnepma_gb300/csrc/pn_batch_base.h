@@ -33,6 +33,7 @@ class BatchGroupBase {
   virtual long long launches_forward() const = 0;
   virtual long long launches_adjoint() const = 0;
   virtual int stride() const = 0;
+  virtual long long recomputed_steps() const { return 0; }
   // wait for the uploads create() issued on the group's own stream
   virtual int wait_created() = 0;
   // true when the group's sub-steps run through the TMA tile kernel

@@ -46,6 +46,12 @@ constexpr int PLO = TX * TY;        // floats per moment plane of a target / den
 constexpr int PL4 = BW * TY;        // ... of a 4-row neighbour box
 constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row neighbour box (y halo on the side the stencil reads)
 
+// minimum resident CTAs per SM the sub-step kernel is compiled for: 5 keeps the adjoint
+// instances within 96 registers, so that shared memory, not registers, bounds their occupancy
+#ifndef PN_TMA_MINB
+#define PN_TMA_MINB 5
+#endif
+
 // stages of the tile ring per CTA (1: no prefetch within a CTA, more CTAs per SM)
 #ifndef PN_TMA_STAGES
 #define PN_TMA_STAGES 1
@@ -88,7 +94,8 @@ struct TTile {
   int arg_adj;  // ... adjoint ArgRow
   int arg_int;  // ... IntRow (n_steps + 1 rows)
   int z;        // plane (0 in 2D)
-  int pad_[3];
+  int n_full;   // states 0 .. n_full - 1 are all kept (tape head)
+  int pad_[2];
 };
 
 // The fields of a solve the cell code reads, copied to shared memory with every tile so that no
@@ -142,7 +149,8 @@ struct TLaunch {
   int* status;
   int pr;
   int n_tiles;
-  int mode, j, sub, K;
+  int mode, j, K;
+  int sub;   // 1, 2, 3: that sub-step of energy step j; 4: sub-step 3 of step j, then sub-step 1 of j - 1
 };
 
 // the classes a launch updates: z-even ones in 2D (DIMS = 3), all in 3D (DIMS = 7)
@@ -163,8 +171,8 @@ struct TmaLayout {
   static constexpr int YN = XN + al(NO * PL4 * 4);
   static constexpr int ZN = YN + al(NO * PL5 * 4);
   static constexpr int RHO = ZN + (DIMS == 7 ? al(NO * PLZ * 4) : 0);
-  static constexpr int ARG = RHO + al(MAXE * PLO * 4);
-  static constexpr int TIL = ARG + (int)sizeof(ArgRow<N>);
+  static constexpr int ARG = RHO + al(MAXE * PLO * 4);      // two rows: steps j and j - 1 of a fused launch
+  static constexpr int TIL = ARG + 2 * (int)sizeof(ArgRow<N>);
   static constexpr int SOL = TIL + (int)sizeof(TTile);
   static constexpr int STAGE = al(SOL + (int)sizeof(TSolve));
   static constexpr int SMEM = TSTAGES * STAGE;
@@ -249,11 +257,21 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 }
 
 // slot of state j (the index form of bslot)
-__device__ __forceinline__ int slot_index(int ns, int n_ck, int j, int K, bool segment, int m) {
+__device__ __forceinline__ int slot_index(int ns, int n_full, int n_ck, int j, int K, bool segment) {
   if (j >= ns) return 0;
-  if (j % K == 0) return 1 + j / K;
-  const int w = segment ? (j - m * K - 1) : (j & 1);
-  return 1 + n_ck + w;
+  if (j < n_full) return 1 + j;
+  const int r = j - n_full;
+  if (r % K == 0) return 1 + n_full + r / K;
+  const int w = segment ? (r % K - 1) : (j & 1);
+  return 1 + n_full + n_ck + w;
+}
+
+// whether state j stays in memory after the forward launches that produce it: kept states (tape
+// head, checkpoints) and every state of a recomputed segment; the forward sweep's other states
+// are only read by the next step
+__device__ __forceinline__ bool state_kept(int ns, int n_full, int j, int K, bool segment) {
+  if (segment || j >= ns || j < n_full) return true;
+  return (j - n_full) % K == 0;
 }
 
 template <int N>
@@ -275,13 +293,17 @@ struct SubSlots {
   int own, from, out;
 };
 
-__device__ __forceinline__ SubSlots sub_slots(int ns, int n_ck, int mode, int j, int sub, int K) {
+__device__ __forceinline__ SubSlots sub_slots(const TTile& tt, int mode, int j, int sub, int K) {
   const bool segment = mode == BM_RECOMPUTE;
-  const int m = j / K;
-  const int src = slot_index(ns, n_ck, j + 1, K, segment, m);
-  const int dst = slot_index(ns, n_ck, j, K, segment, m);
+  const int src = slot_index(tt.ns, tt.n_full, tt.n_ck, j + 1, K, segment);
+  const int dst = slot_index(tt.ns, tt.n_full, tt.n_ck, j, K, segment);
   return SubSlots{(sub == 3) ? dst : src, (sub == 1) ? src : dst, dst};
 }
+
+// A fused launch (sub 4) runs sub-step 3 of step j (pass 0, solves with ns > j) and sub-step 1 of
+// step j - 1 (pass 1).  Both update the odd classes from the same even-class values (state j after
+// sub-step 2 of step j), so one load serves both: own and neighbour boxes come from state j's slot.
+__device__ __forceinline__ bool fused_first_pass(const TTile& tt, int j) { return j < tt.ns; }
 
 // Issue the loads of a tile into stage `st` (one thread).  `tt` must be the tile record in
 // global memory (it is also bulk-copied into the stage).
@@ -293,15 +315,30 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int n_z = DIMS == 7 ? class_moments<N>(cz) : 0;
   SubSlots sl{0, 0, 0};
-  int row;
+  int row, n_rows = 1;
+  unsigned arg_dst = 0;   // byte offset of the first copied row in the stage's two-row area
   if (!ADJ) {
-    sl = sub_slots(tt.ns, tt.n_ck, L.mode, L.j, L.sub, L.K);
-    row = tt.arg_fwd + (tt.ns - L.j - 1);
+    if (L.sub == 4) {
+      // pass 0 reads row (ns - j - 1), pass 1 the next one; a solve that starts at step j - 1
+      // has only pass 1
+      const int s = slot_index(tt.ns, tt.n_full, tt.n_ck, L.j, L.K, L.mode == BM_RECOMPUTE);
+      sl = SubSlots{s, s, s};
+      if (fused_first_pass(tt, L.j)) {
+        row = tt.arg_fwd + (tt.ns - L.j - 1);
+        n_rows = 2;
+      } else {
+        row = tt.arg_fwd + (tt.ns - L.j);
+        arg_dst = (unsigned)sizeof(ArgRow<N>);
+      }
+    } else {
+      sl = sub_slots(tt, L.mode, L.j, L.sub, L.K);
+      row = tt.arg_fwd + (tt.ns - L.j - 1);
+    }
   } else {
     row = tt.arg_adj + L.j;
   }
   const unsigned bytes = 4u * (unsigned)(PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
-                         (unsigned)(sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
+                         (unsigned)(n_rows * sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
   // the y (z) box starts one row (plane) below the tile for a target odd in y (z): it reads j - 1
   // and j; at the tile for one even in y (z): j and j + 1
   const int ya = tt.y0 - ((c >> 1) & 1);
@@ -321,7 +358,7 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
     if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, sl.from, bar);
   }
   tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
-  bulk_load(st + LY::ARG, L.rows + row, (unsigned)sizeof(ArgRow<N>), bar);
+  bulk_load(st + LY::ARG + arg_dst, L.rows + row, (unsigned)(n_rows * sizeof(ArgRow<N>)), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
 }
@@ -478,28 +515,28 @@ __device__ __forceinline__ void staged_advection(float* acc, const float* xn, co
   }
 }
 
-// One point of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
-// values replace the old ones in the target box.
-template <int N, int C, bool ADJ, int DIMS>
-__device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[TB / 32][MAXR]) {
+// One update of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
+// values replace the old ones in the target box.  `ar` holds the step's coefficients, `dt` its
+// (half or full) energy step.  `settle` (thread 0) runs after the ghosts are formed and before the
+// target box is written.
+template <int N, int C, bool ADJ, int DIMS, class Settle>
+__device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
+                                           double (&red)[TB / 32][MAXR], const ArgRow<N>& ar, float dt,
+                                           Settle settle) {
   using LY = TmaLayout<N, DIMS>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   float* own = reinterpret_cast<float*>(st + LY::OWN);
-  {
-    const ArgRow<N>& ar0 = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, ADJ ? 1 : 0, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
-                                         reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
-                                         ADJ ? 0.0 : ar0.bc);
-    __syncthreads();
-  }
+  tile_ghosts<N, C, ADJ ? 1 : 0, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                                       reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
+                                       ADJ ? 0.0 : ar.bc);
+  if (threadIdx.x == 0) settle();
+  __syncthreads();
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
   const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
-  const ArgRow<N>& ar = *reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
   const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
   const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
   const bool valid = tx >= xv0 && tx < xv1 && ty < ey;
@@ -525,7 +562,6 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
         S = fmaf(rr[e], ar.s[e], S);
       }
       const float invS = recip(S);
-      const float dt = L.sub == 2 ? I.dE : I.dE * 0.5f;
       constexpr unsigned mask = Ord<N>::deg_mask(C);
       float Cl[N + 1];
       float ph[N + 1];
@@ -591,16 +627,47 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
     }
   }
   __syncthreads();   // the target box holds the new values
-  if (threadIdx.x == 0) {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    const CUtensorMap* mp = L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS;
-    if (ADJ) {
-      tma_store_4d(mp + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, own);
-    } else {
-      const SubSlots sl = sub_slots(tt.ns, tt.n_ck, L.mode, L.j, L.sub, L.K);
-      tma_store_5d(mp + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.out, own);
+}
+
+// store the target box (thread 0): the adjoint state, or state slot `slot`
+template <int N, int C, bool ADJ, int DIMS>
+__device__ __forceinline__ void tma_store_target(const TLaunch<N>& L, const TTile& tt, unsigned char* st, int slot) {
+  using LY = TmaLayout<N, DIMS>;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const CUtensorMap* mp = L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS;
+  if (ADJ)
+    tma_store_4d(mp + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, st + LY::OWN);
+  else
+    tma_store_5d(mp + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, st + LY::OWN);
+  bulk_commit();
+}
+
+template <int N, int C, bool ADJ, int DIMS>
+__device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
+                                         double (&red)[TB / 32][MAXR]) {
+  using LY = TmaLayout<N, DIMS>;
+  const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
+  const ArgRow<N>* rows = reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
+  const float half = I.dE * 0.5f;
+  auto nothing = [] {};
+  if constexpr (ADJ) {
+    tma_update<N, C, true, DIMS>(L, tt, st, red, rows[0], L.sub == 2 ? I.dE : half, nothing);
+    if (threadIdx.x == 0) tma_store_target<N, C, true, DIMS>(L, tt, st, 0);
+  } else if (L.sub != 4) {
+    tma_update<N, C, false, DIMS>(L, tt, st, red, rows[0], L.sub == 2 ? I.dE : half, nothing);
+    if (threadIdx.x == 0) tma_store_target<N, C, false, DIMS>(L, tt, st, sub_slots(tt, L.mode, L.j, L.sub, L.K).out);
+  } else {
+    // fused: sub-step 3 of step j, then sub-step 1 of step j - 1 on the updated target box
+    const bool segment = L.mode == BM_RECOMPUTE;
+    if (fused_first_pass(tt, L.j)) {
+      tma_update<N, C, false, DIMS>(L, tt, st, red, rows[0], half, nothing);
+      if (threadIdx.x == 0 && state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
+        tma_store_target<N, C, false, DIMS>(L, tt, st, slot_index(tt.ns, tt.n_full, tt.n_ck, L.j, L.K, segment));
     }
-    bulk_commit();
+    // the second update overwrites the target box once the first store has read it
+    tma_update<N, C, false, DIMS>(L, tt, st, red, rows[1], half, [] { bulk_wait_read(); });
+    if (threadIdx.x == 0)
+      tma_store_target<N, C, false, DIMS>(L, tt, st, slot_index(tt.ns, tt.n_full, tt.n_ck, L.j - 1, L.K, segment));
   }
 }
 
@@ -629,7 +696,7 @@ __device__ __forceinline__ void tma_cell_of(const TLaunch<N>& L, const TTile& tt
 }
 
 template <int N, bool ADJ, int DIMS>
-__global__ void __launch_bounds__(TB, 2) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
+__global__ void __launch_bounds__(TB, PN_TMA_MINB) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
   using LY = TmaLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
@@ -721,7 +788,7 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   const int c = tt.cls, cx = c ^ 4, cy = c ^ 2, cz = c ^ 1;
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int n_z = DIMS == 7 ? class_moments<N>(cz) : 0;
-  const int slot = slot_index(tt.ns, tt.n_ck, L.it, L.K, true, L.it / L.K);
+  const int slot = slot_index(tt.ns, tt.n_full, tt.n_ck, L.it, L.K, true);
   const unsigned bytes = 4u * (unsigned)(2 * PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
                          8u * (unsigned)(PLO * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
   const int ya = tt.y0 - ((c >> 1) & 1);
