@@ -116,6 +116,10 @@ struct BInst {
   int n_ptile;            // its eee tiles: the leading tiles of list 0
   int nseg[3];
   Seg seg[3][MAXSEG];
+  // boundary blocks in the state precision (rounded once on the host), for the TMA tile kernels'
+  // face ghosts; after the segments so that the generic kernels' staged head stays as it is
+  const T* bmt_f[3][8];
+  const T* bmt_a[3][8];
 };
 
 struct BTile {
@@ -1238,8 +1242,11 @@ class BatchGroup : public BatchGroupBase {
       checked_advection.assign(d->advection, d->advection + L.n_adv);
     }
     double *bf, *ba, *bm;
+    T *btf, *bta;
     if ((rc = stage(bf, cpd(d->boundary_fwd, L.n_bnd)))) return rc;
     if ((rc = stage(ba, cpd(d->boundary_adj, L.n_bnd)))) return rc;
+    if ((rc = stage(btf, conv(d->boundary_fwd, L.n_bnd)))) return rc;
+    if ((rc = stage(bta, conv(d->boundary_adj, L.n_bnd)))) return rc;
     std::vector<double> beam = cpd(d->beam_face, L.n_beam);
     // FP32: scale the beam source so the state stays near unity (a power of two: exact)
     I.scale_g = 1.0;
@@ -1259,6 +1266,8 @@ class BatchGroup : public BatchGroupBase {
           if (class_bit(c, k)) {
             I.bmat_f[k][c] = bf + o;
             I.bmat_a[k][c] = ba + o;
+            I.bmt_f[k][c] = btf + o;
+            I.bmt_a[k][c] = bta + o;
             o += (long long)L.nm[c] * L.nm[class_switch(c, k)];
           }
       for (int c = 4; c < 8; ++c) I.beam[c] = bm + L.beam_off[c];

@@ -382,7 +382,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
     constexpr int nf = Ord<N>::n(F);
     if constexpr (nt > 0 && nf > 0) {
       const int ncx = S.n0[C];
-      const double* B = ADJ ? I.bmat_a[0][F] : I.bmat_f[0][F];
+      const float* B = ADJ ? I.bmt_a[0][F] : I.bmt_f[0][F];
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
         if (left ? tt.x0 != 0 : tt.x0 + xv1 != ncx) continue;
@@ -397,7 +397,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
           const int ty = w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
-          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + ty * TX + cc], bv);
+          for (int q = 0; q < nt; ++q) bv = fmaf(B[r * nt + q], own[q * PLO + ty * TX + cc], bv);
           const int j = tt.y0 + ty;
           const float gval =
               src ? float(I.beam[F][((long long)tt.z * S.n1[F] + j) * nf + r] * bc_scaled) : 0.0f;
@@ -412,7 +412,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
     constexpr int nf = Ord<N>::n(F);
     if constexpr (nt > 0 && nf > 0) {
       const int ncy = S.n1[C];
-      const double* B = ADJ ? I.bmat_a[1][F] : I.bmat_f[1][F];
+      const float* B = ADJ ? I.bmt_a[1][F] : I.bmt_f[1][F];
       const int nx = xv1 - xv0;
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
@@ -424,7 +424,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
           const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
-          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + crow * TX + tx], bv);
+          for (int q = 0; q < nt; ++q) bv = fmaf(B[r * nt + q], own[q * PLO + crow * TX + tx], bv);
           const float interior = yb[r * PL5 + irow * BW + tx + XO];
           yb[r * PL5 + grow * BW + tx + XO] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
         }
@@ -436,7 +436,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
     constexpr int nf = Ord<N>::n(F);
     if constexpr (nt > 0 && nf > 0) {
       const int ncz = S.n2[C];
-      const double* B = ADJ ? I.bmat_a[2][F] : I.bmat_f[2][F];
+      const float* B = ADJ ? I.bmt_a[2][F] : I.bmt_f[2][F];
       const int nx = xv1 - xv0;
       for (int side = 0; side < 2; ++side) {
         const bool left = side == 0;
@@ -449,7 +449,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
           const int ty = rest / nx, tx = xv0 + rest % nx;
           float bv = 0.0f;
 #pragma unroll
-          for (int q = 0; q < nt; ++q) bv = fmaf(float(B[r * nt + q]), own[q * PLO + ty * TX + tx], bv);
+          for (int q = 0; q < nt; ++q) bv = fmaf(B[r * nt + q], own[q * PLO + ty * TX + tx], bv);
           const float interior = zb[r * PLZ + ipl * PLO + ty * TX + tx];
           zb[r * PLZ + gpl * PLO + ty * TX + tx] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
         }
@@ -517,12 +517,12 @@ __device__ __forceinline__ void staged_advection(float* acc, const float* xn, co
 
 // One update of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
 // values replace the old ones in the target box.  `ar` holds the step's coefficients, `dt` its
-// (half or full) energy step.  `settle` (thread 0) runs after the ghosts are formed and before the
-// target box is written.
-template <int N, int C, bool ADJ, int DIMS, class Settle>
+// (half or full) energy step.  With `settle`, thread 0 waits for the reads of the tile's earlier
+// store after the ghosts are formed and before the target box is written.
+template <int N, int C, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                            double (&red)[TB / 32][MAXR], const ArgRow<N>& ar, float dt,
-                                           Settle settle) {
+                                           bool settle) {
   using LY = TmaLayout<N, DIMS>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
@@ -531,7 +531,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
   tile_ghosts<N, C, ADJ ? 1 : 0, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
                                        reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
                                        ADJ ? 0.0 : ar.bc);
-  if (threadIdx.x == 0) settle();
+  if (settle && threadIdx.x == 0) bulk_wait_read();
   __syncthreads();
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
@@ -649,25 +649,27 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   const ArgRow<N>* rows = reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
   const float half = I.dE * 0.5f;
-  auto nothing = [] {};
-  if constexpr (ADJ) {
-    tma_update<N, C, true, DIMS>(L, tt, st, red, rows[0], L.sub == 2 ? I.dE : half, nothing);
-    if (threadIdx.x == 0) tma_store_target<N, C, true, DIMS>(L, tt, st, 0);
-  } else if (L.sub != 4) {
-    tma_update<N, C, false, DIMS>(L, tt, st, red, rows[0], L.sub == 2 ? I.dE : half, nothing);
-    if (threadIdx.x == 0) tma_store_target<N, C, false, DIMS>(L, tt, st, sub_slots(tt, L.mode, L.j, L.sub, L.K).out);
-  } else {
-    // fused: sub-step 3 of step j, then sub-step 1 of step j - 1 on the updated target box
-    const bool segment = L.mode == BM_RECOMPUTE;
-    if (fused_first_pass(tt, L.j)) {
-      tma_update<N, C, false, DIMS>(L, tt, st, red, rows[0], half, nothing);
-      if (threadIdx.x == 0 && state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
-        tma_store_target<N, C, false, DIMS>(L, tt, st, slot_index(tt.ns, tt.n_full, tt.n_ck, L.j, L.K, segment));
-    }
+  // passes: one sub-step, or the two of a fused launch (the first skipped for a solve that starts
+  // at step j - 1); one copy of the update code serves all of them
+  const bool fused = !ADJ && L.sub == 4;
+  const bool segment = L.mode == BM_RECOMPUTE;
+  const int p0 = (fused && !fused_first_pass(tt, L.j)) ? 1 : 0;
+  const int p1 = fused ? 2 : 1;
+#pragma unroll 1
+  for (int pass = p0; pass < p1; ++pass) {
+    const bool second = pass == 1;
     // the second update overwrites the target box once the first store has read it
-    tma_update<N, C, false, DIMS>(L, tt, st, red, rows[1], half, [] { bulk_wait_read(); });
-    if (threadIdx.x == 0)
-      tma_store_target<N, C, false, DIMS>(L, tt, st, slot_index(tt.ns, tt.n_full, tt.n_ck, L.j - 1, L.K, segment));
+    tma_update<N, C, ADJ, DIMS>(L, tt, st, red, rows[pass], L.sub == 2 ? I.dE : half, second);
+    if (threadIdx.x == 0) {
+      if (ADJ) {
+        tma_store_target<N, C, ADJ, DIMS>(L, tt, st, 0);
+      } else if (!fused) {
+        tma_store_target<N, C, ADJ, DIMS>(L, tt, st, sub_slots(tt, L.mode, L.j, L.sub, L.K).out);
+      } else if (second || state_kept(tt.ns, tt.n_full, L.j, L.K, segment)) {
+        const int jj = second ? L.j - 1 : L.j;
+        tma_store_target<N, C, ADJ, DIMS>(L, tt, st, slot_index(tt.ns, tt.n_full, tt.n_ck, jj, L.K, segment));
+      }
+    }
   }
 }
 
