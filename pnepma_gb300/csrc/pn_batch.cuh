@@ -81,8 +81,7 @@ struct BInst {
   double* acs;            // [cell][r] device copies of the inputs
   double* noa;            // [cell][e]
   double* wint;           // [cell][r]
-  double* acs_bar;
-  double* noa_bar;
+  double* wsum;           // [cell][r] sum over adjoint iterations of coef_r u0 (eee moment 0)
   double* ibar;           // scaled cotangent [r]
   double* out_mul;        // factor undoing the scaling of the adjoint outputs
   double* I;              // [r] intensities of the last forward
@@ -187,14 +186,11 @@ struct BInt {
   double bc, scale_g, wfac;
   T s[MAXE];
   T c[MAXE][N + 1];
-  const double* acs;
-  const double* noa;
-  const double* ibar;
-  double* acs_bar;
-  double* noa_bar;
+  double* wsum;           // [cell][line] sum over iterations of coef_r u0
   int xel[MAXR];
   double coef[MAXR];
   T inv_h[3];
+  static constexpr bool line_sums = true;
 };
 
 // Slot of state j: the zero state past the end of the march, a kept state, a checkpoint, or a
@@ -376,11 +372,7 @@ __device__ __forceinline__ void fill_int(BInt<T, N>& a, const BInst<T>& I, const
     a.bc = I.int_bc[it];
     a.scale_g = I.scale_g;
     a.wfac = I.int_wfac[it];
-    a.acs = I.acs;
-    a.noa = I.noa;
-    a.ibar = I.ibar;
-    a.acs_bar = I.acs_bar;
-    a.noa_bar = I.noa_bar;
+    a.wsum = I.wsum;
     for (int r = 0; r < MAXR; ++r) a.xel[r] = I.xel[r];
   } else if (tid >= 16 && tid < 16 + MAXR) {
     const int r = tid - 16;
@@ -476,8 +468,7 @@ __global__ void batch_zero_kernel(const BInst<T>* __restrict__ inst, int which) 
     for (int c = 0; c < 8; ++c)
       if (I.active[c])
         for (long long q = t0; q < I.g[c].ms * I.ne; q += stride) I.rbar[c][q] = 0.0;
-    for (long long q = t0; q < I.n_eee * I.nr; q += stride) I.acs_bar[q] = 0.0;
-    for (long long q = t0; q < I.n_eee * I.ne; q += stride) I.noa_bar[q] = 0.0;
+    for (long long q = t0; q < I.n_eee * I.nr; q += stride) I.wsum[q] = 0.0;
   }
 }
 
@@ -561,8 +552,21 @@ __global__ void batch_store_kernel(const BInst<T>* __restrict__ inst, const BIo*
     }
     o.rho_bar[q] = v;
   }
-  for (long long q = t0; q < I.n_eee * I.ne; q += stride) o.noa_bar[q] = I.noa_bar[q] * mul;
-  for (long long q = t0; q < I.n_eee * I.nr; q += stride) o.acs_bar[q] = I.acs_bar[q] * mul;
+  // acs_bar(cell, r) = noa(cell, e_r) ibar_r W_r;  noa_bar(cell, e) = sum over the lines r of
+  // element e of acs(cell, r) ibar_r W_r
+  for (long long q = t0; q < I.n_eee * I.ne; q += stride) {
+    const long long ce = q / I.ne;
+    const int e = (int)(q - ce * I.ne);
+    double v = 0.0;
+    for (int r = 0; r < I.nr; ++r)
+      if (I.xel[r] == e) v += I.acs[ce * I.nr + r] * I.wsum[ce * I.nr + r] * I.ibar[r];
+    o.noa_bar[q] = v * mul;
+  }
+  for (long long q = t0; q < I.n_eee * I.nr; q += stride) {
+    const long long ce = q / I.nr;
+    const int r = (int)(q - ce * I.nr);
+    o.acs_bar[q] = I.noa[ce * I.ne + I.xel[r]] * I.wsum[q] * I.ibar[r] * mul;
+  }
 }
 
 }  // namespace pn
@@ -1026,8 +1030,7 @@ class BatchGroup : public BatchGroupBase {
         S.acs = I.acs;
         S.noa = I.noa;
         S.ibar = I.ibar;
-        S.acs_bar = I.acs_bar;
-        S.noa_bar = I.noa_bar;
+        S.wsum = I.wsum;
         for (int c = 0; c < 8; ++c) {
           S.rbar[c] = I.rbar[c];
           S.dev_off[c] = I.dev_off[c];
@@ -1275,8 +1278,7 @@ class BatchGroup : public BatchGroupBase {
     if ((rc = alloc(I.acs, L.n_eee_cells * nr))) return rc;
     if ((rc = alloc(I.noa, L.n_eee_cells * ne))) return rc;
     if ((rc = alloc(I.wint, L.n_eee_cells * nr))) return rc;
-    if ((rc = alloc(I.acs_bar, L.n_eee_cells * nr))) return rc;
-    if ((rc = alloc(I.noa_bar, L.n_eee_cells * ne))) return rc;
+    if ((rc = alloc(I.wsum, L.n_eee_cells * nr))) return rc;
     if ((rc = alloc(I.ibar, nr))) return rc;
     if ((rc = alloc(I.out_mul, 1))) return rc;
     if ((rc = alloc(I.I, nr))) return rc;

@@ -108,8 +108,8 @@ struct TSolve {
   const double* acs;
   const double* noa;
   const double* ibar;
-  double* acs_bar;
-  double* noa_bar;
+  double* wsum;
+  double* pad0_;
   double* rbar[8];
   long long dev_off[8];
   long long ms[8];
@@ -889,12 +889,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       if constexpr (C == 0) {
         const long long ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
         const double u0 = double(own[lo]);
-        for (int r = 0; r < I.nr; ++r) {
-          const double cr = ar.coef[r] * I.ibar[r];
-          const int el = I.xel[r];
-          I.acs_bar[ce * I.nr + r] += I.noa[ce * I.ne + el] * u0 * cr;
-          I.noa_bar[ce * I.ne + el] += I.acs[ce * I.nr + r] * u0 * cr;
-        }
+        for (int r = 0; r < I.nr; ++r) I.wsum[ce * I.nr + r] += ar.coef[r] * u0;
       }
     }
   }

@@ -120,6 +120,7 @@ struct IntArgs {
   double* noa_bar;
   int xel[MAXR];
   double coef[MAXR];          // dE * dvol * sigma_r * w   (times ibar_r in the kernel)
+  static constexpr bool line_sums = false;   // accumulate acs_bar / noa_bar directly
   Seg seg[MAXSEG];
   T tab[Ord<N>::n_tab];
 };
@@ -622,11 +623,16 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
     if constexpr (C == 0) {
       const long long ce = eee_cell(gt, i, j, k);
       const double u0 = double(uu[0]);
-      for (int r = 0; r < a.nr; ++r) {
-        const double cr = a.coef[r] * a.ibar[r];
-        const int el = a.xel[r];
-        a.acs_bar[ce * a.nr + r] += a.noa[ce * a.ne + el] * u0 * cr;
-        a.noa_bar[ce * a.ne + el] += a.acs[ce * a.nr + r] * u0 * cr;
+      if constexpr (A::line_sums) {
+        // W_r(cell) += coef_r u0; acs_bar and noa_bar are formed from W once, after the sweep
+        for (int r = 0; r < a.nr; ++r) a.wsum[ce * a.nr + r] += a.coef[r] * u0;
+      } else {
+        for (int r = 0; r < a.nr; ++r) {
+          const double cr = a.coef[r] * a.ibar[r];
+          const int el = a.xel[r];
+          a.acs_bar[ce * a.nr + r] += a.noa[ce * a.ne + el] * u0 * cr;
+          a.noa_bar[ce * a.ne + el] += a.acs[ce * a.nr + r] * u0 * cr;
+        }
       }
     }
   }
