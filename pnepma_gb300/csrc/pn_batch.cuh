@@ -82,6 +82,7 @@ struct BInst {
   double* noa;            // [cell][e]
   double* wint;           // [cell][r]
   double* wsum;           // [cell][r] sum over adjoint iterations of coef_r u0 (eee moment 0)
+  double* wsrc;           // [cell][r] acs noa ibar_r: the adjoint source weights of one sweep
   double* ibar;           // scaled cotangent [r]
   double* out_mul;        // factor undoing the scaling of the adjoint outputs
   double* I;              // [r] intensities of the last forward
@@ -161,11 +162,10 @@ struct BSub {
   double bc, scale_g;
   T s[MAXE];
   T c[MAXE][N + 1];
-  const double* acs;
-  const double* noa;
-  const double* ibar;
+  const double* wsrc;     // [cell][r] acs noa ibar_r (adjoint source weights)
   int xel[MAXR];
   double sig_src[MAXR];
+  static constexpr bool line_src = true;
   const double* wint;
   T inv_h[3];
   T* cache[8];        // unused by the batched kernels (cache_mode 0)
@@ -263,9 +263,7 @@ __device__ __forceinline__ void fill_sub(BSub<T, N>& a, const BInst<T>& I, const
     a.nr = I.nr;
     a.dt = L.sub == 2 ? I.dE : I.dE * T(0.5);
     a.scale_g = I.scale_g;
-    a.acs = I.acs;
-    a.noa = I.noa;
-    a.ibar = I.ibar;
+    a.wsrc = I.wsrc;
     a.wint = I.wint;
     a.adjoint_source = ADJ ? 1 : 0;
     a.cache_mode = 0;
@@ -526,6 +524,18 @@ __global__ void batch_prep_ibar_kernel(const BInst<T>* __restrict__ inst, const 
   if (fp32 && q > 0.0 && isfinite(q)) sc = ldexp(1.0, -(int)llrint(log2(q)));
   for (int r = 0; r < I.nr; ++r) I.ibar[r] = in[r] * sc;
   I.out_mul[0] = 1.0 / (I.scale_g * sc);
+}
+
+// adjoint source weights acs(cell, r) noa(cell, e_r) ibar_r of every solve (after the scaled ibar)
+template <class T>
+__global__ void batch_prep_src_kernel(const BInst<T>* __restrict__ inst) {
+  const BInst<T>& I = inst[blockIdx.y];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < I.n_eee * I.nr; q += stride) {
+    const long long ce = q / I.nr;
+    const int r = (int)(q - ce * I.nr);
+    I.wsrc[q] = I.acs[q] * I.noa[ce * I.ne + I.xel[r]] * I.ibar[r];
+  }
 }
 
 template <class T>
@@ -1027,9 +1037,7 @@ class BatchGroup : public BatchGroupBase {
         S.lam = I.lam;
         S.slot_elems = I.slot_elems;
         S.wint = I.wint;
-        S.acs = I.acs;
-        S.noa = I.noa;
-        S.ibar = I.ibar;
+        S.wsrc = I.wsrc;
         S.wsum = I.wsum;
         for (int c = 0; c < 8; ++c) {
           S.rbar[c] = I.rbar[c];
@@ -1279,6 +1287,7 @@ class BatchGroup : public BatchGroupBase {
     if ((rc = alloc(I.noa, L.n_eee_cells * ne))) return rc;
     if ((rc = alloc(I.wint, L.n_eee_cells * nr))) return rc;
     if ((rc = alloc(I.wsum, L.n_eee_cells * nr))) return rc;
+    if ((rc = alloc(I.wsrc, L.n_eee_cells * nr))) return rc;
     if ((rc = alloc(I.ibar, nr))) return rc;
     if ((rc = alloc(I.out_mul, 1))) return rc;
     if ((rc = alloc(I.I, nr))) return rc;
@@ -1579,6 +1588,7 @@ class BatchGroup : public BatchGroupBase {
     if ((rc = prepare(s))) return rc;
     if ((rc = put_io(io_host, s))) return rc;
     batch_prep_ibar_kernel<T><<<n, 32, 0, s>>>(dinst, dio, sizeof(T) == 4 ? 1 : 0);
+    batch_prep_src_kernel<T><<<dim3(64, n), 256, 0, s>>>(dinst);
     PN_CUDA(cudaGetLastError());
     if (direct) {
       ls = s;

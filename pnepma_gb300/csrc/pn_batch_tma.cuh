@@ -105,11 +105,8 @@ struct TSolve {
   float* lam;
   long long slot_elems;
   double* wint;
-  const double* acs;
-  const double* noa;
-  const double* ibar;
+  const double* wsrc;
   double* wsum;
-  double* pad0_;
   double* rbar[8];
   long long dev_off[8];
   long long ms[8];
@@ -123,7 +120,6 @@ struct TSolve {
   int nr;
   int ne;
   double scale_g;
-  double pad_;
 };
 static_assert(sizeof(TSolve) % 16 == 0, "TSolve must be a 16-byte multiple");
 static_assert(sizeof(TTile) % 16 == 0, "TTile must be a 16-byte multiple");
@@ -458,6 +454,33 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
   }
 }
 
+constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
+
+// Sum values v[0 .. V-1] over the lanes of a warp.  Each halving step (lane bits 16, 8, ...) has
+// every lane keep half of its values and add its partner's copy of that half, so V values cost
+// V - 1 adds; the remaining lane bits then reduce the one value left.  Lane l ends with the sum of
+// value (l >> (5 - log2 V)); the first lane of each group writes it to red[w][value].
+template <int V>
+__device__ __forceinline__ void warp_partials(double* v, int lane, int w, int pr, double (&red)[TB / 32][MAXR]) {
+  constexpr int levels = ilog2c(V);
+  int base = 0;
+#pragma unroll
+  for (int lv = 0; lv < levels; ++lv) {
+    const int h = V >> (lv + 1), o = 16 >> lv;
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < h; ++k) {
+      const double give = upper ? v[k] : v[k + h];
+      const double keep = upper ? v[k + h] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, give, o);
+    }
+    if (upper) base += h;
+  }
+#pragma unroll
+  for (int o = 16 >> levels; o > 0; o >>= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+  if ((lane & ((32 >> levels) - 1)) == 0 && base < pr) red[w][base] = v[0];
+}
+
 // the advection sum of one point from the staged boxes: x, then y, then z (advection_sum's order)
 template <int N, int C, bool NEG, int DIMS>
 __device__ __forceinline__ void staged_advection(float* acc, const float* xn, const float* yn, const float* zn,
@@ -583,8 +606,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
       if constexpr (C == 0) ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
       if constexpr (ADJ && C == 0) {
         double q = 0.0;
-        for (int r = 0; r < I.nr; ++r)
-          q = q - ar.sig[r] * I.acs[ce * I.nr + r] * I.noa[ce * I.ne + I.xel[r]] * I.ibar[r];
+        for (int r = 0; r < I.nr; ++r) q = fma(-ar.sig[r], I.wsrc[ce * I.nr + r], q);
         q0 = float(q);
       }
 #pragma unroll
@@ -608,16 +630,12 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
   }
   if (want_part && tt.pslot >= 0) {   // block-uniform
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    // only the group's lines: FP64 adds are scarce on this GPU (2 per SM per clock)
-#pragma unroll
-    for (int r = 0; r < MAXR; ++r) {
-      if (r < L.pr) {
-        double v = part[r];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[w][r] = v;
-      }
-    }
+    // FP64 adds are scarce on this GPU (2 per SM per clock): reduce only the group's lines, V of
+    // them at once with V - 1 + log2(32 / V) adds per warp
+    if (L.pr <= 1) warp_partials<1>(part, lane, w, L.pr, red);
+    else if (L.pr <= 2) warp_partials<2>(part, lane, w, L.pr, red);
+    else if (L.pr <= 4) warp_partials<4>(part, lane, w, L.pr, red);
+    else warp_partials<8>(part, lane, w, L.pr, red);
     __syncthreads();
     if (threadIdx.x < L.pr) {
       double v = 0.0;

@@ -85,6 +85,7 @@ struct SubArgs {
   const double* ibar;         // [r] (device)
   int xel[MAXR];
   double sig_src[MAXR];
+  static constexpr bool line_src = false;   // Q from acs, noa and ibar per line
   // intensity partial sums of the new eee moment 0 (forward, even sub-step)
   const double* wint;         // [cell][r] = ACS * NOA
   double* partial;            // [block][r]
@@ -466,8 +467,13 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
       if (a.adjoint_source) {
         const long long ce = eee_cell(gt, i, j, k);
         double q = 0.0;
-        for (int r = 0; r < a.nr; ++r)
-          q = q - a.sig_src[r] * a.acs[ce * a.nr + r] * a.noa[ce * a.ne + a.xel[r]] * a.ibar[r];
+        if constexpr (A::line_src) {
+          // per-line source weights acs noa ibar, formed once per adjoint sweep
+          for (int r = 0; r < a.nr; ++r) q = fma(-a.sig_src[r], a.wsrc[ce * a.nr + r], q);
+        } else {
+          for (int r = 0; r < a.nr; ++r)
+            q = q - a.sig_src[r] * a.acs[ce * a.nr + r] * a.noa[ce * a.ne + a.xel[r]] * a.ibar[r];
+        }
         q0 = T(q);
       }
     }
