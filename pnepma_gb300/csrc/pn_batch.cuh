@@ -1008,7 +1008,7 @@ class BatchGroup : public BatchGroupBase {
           // (x, y, z, moment, slot); a 2D grid has z extent 1
           const long long st_dims[5] = {I.shape[c][0], I.shape[c][1], I.shape[c][2], nm, nslots};
           const long long st_str[5] = {1, I.px[c], (long long)I.px[c] * I.shape[c][1], I.g[c].ms, I.slot_elems};
-          const int boxt[5] = {TX, TY, 1, nm, 1}, boxx[5] = {BW, TY, 1, nm, 1}, boxy[5] = {BW, TY + 1, 1, nm, 1};
+          const int boxt[5] = {TX, TY, 1, nm, 1}, boxx[5] = {BW, TY, 1, nm, 1}, boxy[5] = {TX, TY + 1, 1, nm, 1};
           const int boxz[5] = {TX, TY, 2, nm, 1};
           bool ok = encode_f32(&m[TM_ST_T], I.slots + I.dev_off[c], 5, st_dims, st_str, boxt) &&
                     encode_f32(&m[TM_ST_X], I.slots + I.dev_off[c], 5, st_dims, st_str, boxx) &&

@@ -5,13 +5,14 @@
 //
 //   * persistent CTAs walk the tiles of a launch in grid-stride order, so the CTAs resident at
 //     any time work on neighbouring tiles;
-//   * a tile is 32 x 4 points of one plane of one target class, starting at x0 = 32 bx: lanes outside the
-//     class's target cells (its ghost points, or points past the grid) keep the values they
-//     were loaded with;
+//   * a tile is 32 x 4 points of one plane of one target class, starting at x0 = 32 bx: lanes
+//     outside the class's target cells (its ghost points, or points past the grid) keep the
+//     values they were loaded with;
 //   * one thread issues, on one mbarrier, cp.async.bulk.tensor loads of the target class's
-//     moments (32 x 4 box), the x- and y-neighbour classes with their one-cell halo (40 x 4 and
-//     40 x 5 boxes from x0 - 4, the first tile's negative start reading zeros), in 3D the
-//     z-neighbour class's two planes either side of the tile's plane (32 x 4 x 2), the densities,
+//     moments (32 x 4 box), the x-neighbour class with its one-point halo (40 x 4 from x0 - 4, the
+//     first tile's negative start reading zeros), the y-neighbour class with the halo row the
+//     stencil reads (32 x 5 at x0), in 3D the z-neighbour class's planes either side of the
+//     tile's plane (32 x 4 x 2), the densities,
 //     plus cp.async.bulk copies of the step's coefficient row, the tile record and the solve's
 //     arguments; every operand then sits at a compile-time shared-memory offset;
 //   * results overwrite the target box in shared memory and go back with one cp.async.bulk.tensor
@@ -44,7 +45,8 @@ constexpr int BW = TX + 8;          // neighbour box width: x0 - 4 .. x0 + 35 (a
 constexpr int XO = 4;               // the tile's first point in a neighbour box
 constexpr int PLO = TX * TY;        // floats per moment plane of a target / density box
 constexpr int PL4 = BW * TY;        // ... of a 4-row neighbour box
-constexpr int PL5 = BW * (TY + 1);  // ... of a 5-row neighbour box (y halo on the side the stencil reads)
+constexpr int PL5 = TX * (TY + 1);  // ... of a 5-row y-neighbour box (32 wide at x0; the y halo row on
+                                    // the side the stencil reads)
 
 // minimum resident CTAs per SM the sub-step kernel is compiled for: 5 keeps the adjoint
 // instances within 96 registers, so that shared memory, not registers, bounds their occupancy
@@ -345,12 +347,12 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
   if (ADJ) {
     tma_load_4d(st + LY::OWN, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
     if (n_x > 0) tma_load_4d(st + LY::XN, mp + cx * TM_KINDS + TM_LAM_X, xa, tt.y0, tt.z, 0, bar);
-    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM_Y, xa, ya, tt.z, 0, bar);
+    if (n_y > 0) tma_load_4d(st + LY::YN, mp + cy * TM_KINDS + TM_LAM_Y, tt.x0, ya, tt.z, 0, bar);
     if (n_z > 0) tma_load_4d(st + LY::ZN, mp + cz * TM_KINDS + TM_LAM_Z, tt.x0, tt.y0, za, 0, bar);
   } else {
     tma_load_5d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
     if (n_x > 0) tma_load_5d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, tt.z, 0, sl.from, bar);
-    if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, tt.z, 0, sl.from, bar);
+    if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, tt.x0, ya, tt.z, 0, sl.from, bar);
     if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, sl.from, bar);
   }
   tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
@@ -421,8 +423,8 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
           float bv = 0.0f;
 #pragma unroll
           for (int q = 0; q < nt; ++q) bv = fmaf(B[r * nt + q], own[q * PLO + crow * TX + tx], bv);
-          const float interior = yb[r * PL5 + irow * BW + tx + XO];
-          yb[r * PL5 + grow * BW + tx + XO] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
+          const float interior = yb[r * PL5 + irow * TX + tx];
+          yb[r * PL5 + grow * TX + tx] = left ? 2.0f * (0.0f - bv) - interior : 2.0f * (bv + 0.0f) - interior;
         }
       }
     }
@@ -572,7 +574,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
       const int i = tt.x0 + tx, j = tt.y0 + ty;
       const int lo = ty * TX + tx;                              // the point in the target / density / z boxes
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
-      const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;     // rows j, j - 1 (odd) or j + 1, j of the y box
+      const int yr = (ty + 1) * TX + tx, yl = yr - TX;          // rows j, j - 1 (odd) or j + 1, j of the y box
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
@@ -819,7 +821,7 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   tma_load_5d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, bar);
   tma_load_4d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
   if (n_x > 0) tma_load_5d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, tt.z, 0, slot, bar);
-  if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, xa, ya, tt.z, 0, slot, bar);
+  if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, tt.x0, ya, tt.z, 0, slot, bar);
   if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, slot, bar);
   tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
   tma_load_4d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, tt.x0, tt.y0, tt.z, 0, bar);
@@ -855,7 +857,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const int i = tt.x0 + tx, j = tt.y0 + ty;
       const int lo = ty * TX + tx;
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
-      const int yr = (ty + 1) * BW + tx + XO, yl = yr - BW;
+      const int yr = (ty + 1) * TX + tx, yl = yr - TX;
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
