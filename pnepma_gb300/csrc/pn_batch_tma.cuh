@@ -575,6 +575,16 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
       const int lo = ty * TX + tx;                              // the point in the target / density / z boxes
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;          // rows j, j - 1 (odd) or j + 1, j of the y box
+      // the eee cell's per-line weights (intensity or adjoint source), loaded before the stencil
+      // so that their latency overlaps it
+      long long ce = 0;
+      double wl[MAXR];
+      if constexpr (C == 0) {
+        ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
+        const double* wsrc = ADJ ? I.wsrc : I.wint;
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) wl[r] = (r < I.nr && (ADJ || want_part)) ? wsrc[ce * I.nr + r] : 0.0;
+      }
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
@@ -604,11 +614,11 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
         }
       }
       float q0 = 0.0f;
-      long long ce = 0;
-      if constexpr (C == 0) ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
       if constexpr (ADJ && C == 0) {
         double q = 0.0;
-        for (int r = 0; r < I.nr; ++r) q = fma(-ar.sig[r], I.wsrc[ce * I.nr + r], q);
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r)
+          if (r < I.nr) q = fma(-ar.sig[r], wl[r], q);
         q0 = float(q);
       }
 #pragma unroll
@@ -624,7 +634,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
           if (m == 0 && want_part) {
 #pragma unroll
             for (int r = 0; r < MAXR; ++r)
-              if (r < I.nr) part[r] += I.wint[ce * I.nr + r] * double(unew);
+              if (r < I.nr) part[r] += wl[r] * double(unew);
           }
         }
       }
@@ -858,6 +868,14 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const int lo = ty * TX + tx;
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;
+      // the eee cell's line sums, loaded before the stencil so that their latency overlaps it
+      long long ce = 0;
+      double wl[MAXR];
+      if constexpr (C == 0) {
+        ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r) wl[r] = r < I.nr ? I.wsum[ce * I.nr + r] : 0.0;
+      }
       float acc[n];
 #pragma unroll
       for (int m = 0; m < n; ++m) acc[m] = 0.0f;
@@ -907,9 +925,10 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
         }
       }
       if constexpr (C == 0) {
-        const long long ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
         const double u0 = double(own[lo]);
-        for (int r = 0; r < I.nr; ++r) I.wsum[ce * I.nr + r] += ar.coef[r] * u0;
+#pragma unroll
+        for (int r = 0; r < MAXR; ++r)
+          if (r < I.nr) I.wsum[ce * I.nr + r] = fma(ar.coef[r], u0, wl[r]);
       }
     }
   }

@@ -631,7 +631,7 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
       const double u0 = double(uu[0]);
       if constexpr (A::line_sums) {
         // W_r(cell) += coef_r u0; acs_bar and noa_bar are formed from W once, after the sweep
-        for (int r = 0; r < a.nr; ++r) a.wsum[ce * a.nr + r] += a.coef[r] * u0;
+        for (int r = 0; r < a.nr; ++r) a.wsum[ce * a.nr + r] = fma(a.coef[r], u0, a.wsum[ce * a.nr + r]);
       } else {
         for (int r = 0; r < a.nr; ++r) {
           const double cr = a.coef[r] * a.ibar[r];
