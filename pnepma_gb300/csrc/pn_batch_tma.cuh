@@ -597,9 +597,10 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
         S = fmaf(rr[e], ar.s[e], S);
       }
       const float invS = recip(S);
+      const float dts = dt * invS;
       constexpr unsigned mask = Ord<N>::deg_mask(C);
       float Cl[N + 1];
-      float ph[N + 1];
+      float gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
 #pragma unroll
       for (int l = 0; l <= N; ++l) {
         if ((mask >> l) & 1u) {
@@ -607,10 +608,10 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
 #pragma unroll
           for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
           Cl[l] = cc;
-          ph[l] = phi1(-cc * invS * dt);
+          gl[l] = dts * phi1(-cc * invS * dt);
         } else {
           Cl[l] = 0.0f;
-          ph[l] = 1.0f;
+          gl[l] = 0.0f;
         }
       }
       float q0 = 0.0f;
@@ -627,8 +628,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
         const float u = own[m * PLO + lo];
         const float q = (m == 0) ? q0 : 0.0f;
         const float num = (q - acc[m]) - Cl[l] * u;
-        const float du = num * invS * ph[l];
-        const float unew = u + dt * du;
+        const float unew = fmaf(num, gl[l], u);
         own[m * PLO + lo] = unew;
         if constexpr (C == 0 && !ADJ) {
           if (m == 0 && want_part) {
@@ -908,10 +908,10 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
         const int l = degree_of<N, C>(m);
         const float u = own[m * PLO + lo];
         const float lm = lam[m * PLO + lo];
-        const float du = (-acc[m] - Cl[l] * u) * invS;
-        P = fmaf(lm, du, P);
+        P = fmaf(lm, -acc[m] - Cl[l] * u, P);   // 1/S applied once, below (integrate_cell's order)
         R[l] = fmaf(lm, u, R[l]);
       }
+      P *= invS;
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
         if (e < tt.ne) {

@@ -414,18 +414,17 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
     advection_sum<T, N, C, ADJ, LIT, DIMS>(acc, a, rd, i, j, k);
 
     constexpr unsigned mask = Ord<N>::deg_mask(C);
-    T invS;
+    // per degree: C_l and g_l = dt phi1(-C_l dt / S) / S, so that u' = u + g_l (q - A u - C_l u)
     T Cl[N + 1];
-    T ph[N + 1];
+    T gl[N + 1];
     if (a.cache_mode == 2) {
       // the first half sub-step of this energy step left the factors of this cell
       const T* cp = a.cache[C] + p;
 #pragma unroll
       for (int l = 0; l <= N; ++l) {
-        Cl[l] = ((mask >> l) & 1u) ? cp[(1 + l) * gt.ms] : T(0);
-        ph[l] = ((mask >> l) & 1u) ? cp[(2 + N + l) * gt.ms] : T(1);
+        Cl[l] = ((mask >> l) & 1u) ? cp[l * gt.ms] : T(0);
+        gl[l] = ((mask >> l) & 1u) ? cp[(1 + N + l) * gt.ms] : T(0);
       }
-      invS = cp[0];
     } else {
       const T* rho = a.rho[C] + p;
       T rr[MAXE];
@@ -435,7 +434,8 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
         rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
         S = fma(rr[e], a.s[e], S);
       }
-      invS = recip(S);
+      const T invS = recip(S);
+      const T dts = a.dt * invS;
 #pragma unroll
       for (int l = 0; l <= N; ++l) {
         if ((mask >> l) & 1u) {
@@ -443,20 +443,19 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
 #pragma unroll
           for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
           Cl[l] = cc;
-          ph[l] = phi1(-cc * invS * a.dt);
+          gl[l] = dts * phi1(-cc * invS * a.dt);
         } else {
           Cl[l] = T(0);
-          ph[l] = T(1);
+          gl[l] = T(0);
         }
       }
       if (a.cache_mode == 1) {
         T* cp = a.cache[C] + p;
-        cp[0] = invS;
 #pragma unroll
         for (int l = 0; l <= N; ++l)
           if ((mask >> l) & 1u) {
-            cp[(1 + l) * gt.ms] = Cl[l];
-            cp[(2 + N + l) * gt.ms] = ph[l];
+            cp[l * gt.ms] = Cl[l];
+            cp[(1 + N + l) * gt.ms] = gl[l];
           }
       }
     }
@@ -485,8 +484,7 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
       else u = uo[m * gt.ms];
       const T q = (m == 0) ? q0 : T(0);
       const T num = (q - acc[m]) - Cl[l] * u;
-      const T du = num * invS * ph[l];
-      const T unew = u + a.dt * du;
+      const T unew = fma(num, gl[l], u);
       un[m * gt.ms] = unew;
       if constexpr (C == 0 && !ADJ) {
         if (m == 0 && part != nullptr) {
@@ -610,10 +608,11 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
         u = uu[m * gt.ms];
         lm = la[m * gt.ms];
       }
-      const T du = (-acc[m] - Cl[l] * u) * invS;
-      P = fma(lm, du, P);
+      // P = sum_m lambda_m du_m with du = (-A u - C_l u) / S: the 1/S applied once, below
+      P = fma(lm, -acc[m] - Cl[l] * u, P);
       R[l] = fma(lm, u, R[l]);
     }
+    P *= invS;
     double* rb = a.rbar[C] + p;
 #pragma unroll
     for (int e = 0; e < MAXE; ++e) {

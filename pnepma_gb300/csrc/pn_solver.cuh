@@ -374,17 +374,18 @@ class Solver : public SolverBase {
     if ((rc = alloc(ba_d, L.n_bnd))) return rc;
     if ((rc = alloc(beam_d, std::max<long long>(L.n_beam, 1)))) return rc;
     {
-      // factor cache of the odd classes: planes 1/S, C_0..C_N, phi1_0..phi1_N with each class's geometry
+      // factor cache of the odd classes: planes C_0..C_N, g_0..g_N (g_l = dt phi1_l / S) with each
+      // class's geometry
       long long n_cache = 0;
       for (int cl = 0; cl < 8; ++cl)
-        if (L.active[cl] && class_parity(cl) == 1) n_cache += (long long)(2 * N + 3) * L.ms[cl];
+        if (L.active[cl] && class_parity(cl) == 1) n_cache += (long long)(2 * N + 2) * L.ms[cl];
       if (n_cache > 0) {
         if ((rc = alloc(cache_d, n_cache))) return rc;
         long long o = 0;
         for (int cl = 0; cl < 8; ++cl)
           if (L.active[cl] && class_parity(cl) == 1) {
             cache_cls[cl] = cache_d + o;
-            o += (long long)(2 * N + 3) * L.ms[cl];
+            o += (long long)(2 * N + 2) * L.ms[cl];
           }
       }
     }
