@@ -601,19 +601,9 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
       constexpr unsigned mask = Ord<N>::deg_mask(C);
       float Cl[N + 1];
       float gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
+      cl_sums<float, N, mask>(rr, ar.c, tt.ne, Cl);
 #pragma unroll
-      for (int l = 0; l <= N; ++l) {
-        if ((mask >> l) & 1u) {
-          float cc = 0.0f;
-#pragma unroll
-          for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
-          Cl[l] = cc;
-          gl[l] = dts * phi1(-cc * invS * dt);
-        } else {
-          Cl[l] = 0.0f;
-          gl[l] = 0.0f;
-        }
-      }
+      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(-(Cl[l] * dts)) : 0.0f;
       float q0 = 0.0f;
       if constexpr (ADJ && C == 0) {
         double q = 0.0;
@@ -890,15 +880,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const float invS = recip(S);
       constexpr unsigned mask = Ord<N>::deg_mask(C);
       float Cl[N + 1];
-#pragma unroll
-      for (int l = 0; l <= N; ++l) {
-        float cc = 0.0f;
-        if ((mask >> l) & 1u) {
-#pragma unroll
-          for (int e = 0; e < MAXE; ++e) cc = fmaf(rr[e], ar.c[e][l], cc);
-        }
-        Cl[l] = cc;
-      }
+      cl_sums<float, N, mask>(rr, ar.c, tt.ne, Cl);
       float P = 0.0f;
       float R[N + 1];
 #pragma unroll

@@ -175,6 +175,36 @@ __device__ __forceinline__ float phi1_ref(float c) {
 template <class T>
 __device__ __forceinline__ T recip(T x) { return T(1) / x; }
 
+// minimum resident blocks per SM the plain sub-step kernel is compiled for: 5 keeps the FP64 P11
+// instances within 96 registers (5 x 4 warps per SM to feed the FP64 pipe, instead of 4 x 4)
+#ifndef PN_PLAIN_MINB
+#define PN_PLAIN_MINB 5
+#endif
+
+// C_l = sum_e rho_e c_{e,l} for the degrees of a class, over the solve's ne elements only
+template <class T, int N, unsigned MASK, int NE>
+__device__ __forceinline__ void cl_sums_n(const T* rr, const T (*c)[N + 1], T* Cl) {
+#pragma unroll
+  for (int l = 0; l <= N; ++l) {
+    T cc = T(0);
+    if ((MASK >> l) & 1u) {
+#pragma unroll
+      for (int e = 0; e < NE; ++e) cc = fma(rr[e], c[e][l], cc);
+    }
+    Cl[l] = cc;
+  }
+}
+
+template <class T, int N, unsigned MASK>
+__device__ __forceinline__ void cl_sums(const T* rr, const T (*c)[N + 1], int ne, T* Cl) {
+  switch (ne) {
+    case 1: cl_sums_n<T, N, MASK, 1>(rr, c, Cl); break;
+    case 2: cl_sums_n<T, N, MASK, 2>(rr, c, Cl); break;
+    case 3: cl_sums_n<T, N, MASK, 3>(rr, c, Cl); break;
+    default: cl_sums_n<T, N, MASK, MAXE>(rr, c, Cl); break;
+  }
+}
+
 __device__ __forceinline__ bool locate(const Seg* seg, int nseg, int b, int tid, int& s, int& i, int& j,
                                        int& k) {
   s = 0;
@@ -456,19 +486,9 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
       }
       const T invS = recip(S);
       const T dts = a.dt * invS;
+      cl_sums<T, N, mask>(rr, a.c, a.ne, Cl);
 #pragma unroll
-      for (int l = 0; l <= N; ++l) {
-        if ((mask >> l) & 1u) {
-          T cc = T(0);
-#pragma unroll
-          for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
-          Cl[l] = cc;
-          gl[l] = dts * phi1(-cc * invS * a.dt);
-        } else {
-          Cl[l] = T(0);
-          gl[l] = T(0);
-        }
-      }
+      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(-(Cl[l] * dts)) : T(0);
       if (a.cache_mode == 1) {
         T* cp = a.cache[C] + p;
 #pragma unroll
@@ -519,7 +539,7 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
 }
 
 template <class T, int N, bool ADJ>
-__global__ void __launch_bounds__(BLOCK) substep_kernel(const __grid_constant__ SubArgs<T, N> a) {
+__global__ void __launch_bounds__(BLOCK, PN_PLAIN_MINB) substep_kernel(const __grid_constant__ SubArgs<T, N> a) {
   int s, i, j, k;
   const bool ok = locate(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k);
   const int cls = a.seg[s].cls;
@@ -601,15 +621,7 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
     const T invS = recip(S);
     constexpr unsigned mask = Ord<N>::deg_mask(C);
     T Cl[N + 1];
-#pragma unroll
-    for (int l = 0; l <= N; ++l) {
-      T cc = T(0);
-      if ((mask >> l) & 1u) {
-#pragma unroll
-        for (int e = 0; e < MAXE; ++e) cc = fma(rr[e], a.c[e][l], cc);
-      }
-      Cl[l] = cc;
-    }
+    cl_sums<T, N, mask>(rr, a.c, a.ne, Cl);
     const T* uu = a.u[C] + p;
     const T* la = a.lam[C] + p;
     // P = sum_m lam_m du_m ; R_l = sum_{m: l(m) = l} lam_m u_m
