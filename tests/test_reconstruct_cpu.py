@@ -1,0 +1,107 @@
+"""Reconstruction driver (k-ratio standards cache, loss, gradient, Jacobian, fits) on the CPU,
+with the oracle as the solver backend (the driver's GPU backend is the batched library,
+tests/test_gpu_reconstruct.py)."""
+import numpy as np
+import pytest
+
+from pnepma_gb300 import reconstruct
+from pnepma_gb300.grid import GridSpec
+from pnepma_gb300.workloads import UM
+
+GSPEC = GridSpec.make((6, 1, 1), (-0.4 * UM, 0.0), 0.0, 0.0)
+
+
+class OracleBackend:
+    """The oracle behind the driver's backend interface (test infrastructure only)."""
+    calls = 0
+
+    def __init__(self, oracle, descs, keep):
+        self.o, self.descs, self.keep = oracle, descs, keep
+
+    def forward(self, inputs):
+        OracleBackend.calls += 1
+        self.inputs = inputs
+        return [self.o.forward(d, *x) for d, x in zip(self.descs, inputs)]
+
+    def adjoint(self, ibars):
+        out = [self.o.adjoint(d, *x, ib) for d, x, ib in zip(self.descs, self.inputs, ibars)]
+        return [o[1] for o in out], [o[2] for o in out], [o[3] for o in out]
+
+    def close(self):
+        pass
+
+
+def make(oracle, **kw):
+    return reconstruct.Reconstruction(3, GSPEC, ["Cu", "Ni"], (10.0, 13.0, 16.0), n_steps=30,
+                                      backend_factory=lambda d, k: OracleBackend(oracle, d, k), **kw)
+
+
+def truth(rec):
+    p = np.empty(rec.shape)
+    p[..., 0] = np.where(np.arange(6) < 3, 0.8, 0.25)
+    return p
+
+
+def test_standards_are_pure_element_intensities_computed_once(oracle):
+    reconstruct.clear_standards()
+    OracleBackend.calls = 0
+    rec = make(oracle)
+    assert OracleBackend.calls == 1          # one batch for every problem's standards
+    for s, sd in zip(rec.solves, rec.std):
+        for r, x in enumerate(s.x_rays):
+            e = [el.symbol for el in s.problem.elements].index(x.element)
+            m = reconstruct.pure_material(GSPEC, s.problem.elements, e, True)
+            d, k = s.problem.descriptor(s.x_rays)
+            I = oracle.forward(d, *reconstruct.Solve(s.problem, m, s.x_rays, s.detector).inputs())
+            assert sd[r] == I[r]
+    OracleBackend.calls = 0
+    make(oracle)
+    assert OracleBackend.calls == 0          # cached
+
+
+def test_k_ratios_of_a_standard_are_one(oracle):
+    rec = make(oracle)
+    k = rec.measure(np.ones(rec.shape))      # pure Cu: its own standard
+    assert np.allclose(k[0::2], 1.0, rtol=1e-13)
+    assert np.all(np.abs(k[1::2]) < 1e-12)   # no Ni
+
+
+def test_gradient_equals_jacobian_transpose_residual(oracle):
+    rec = make(oracle)
+    k_exp = rec.measure(truth(rec))
+    p = np.full(rec.shape, 0.5).ravel()
+    f, g = rec.loss_grad(p, k_exp)
+    k, J = rec.jacobian(p)
+    r = k - k_exp
+    assert abs(f - r @ r) <= 1e-12 * f
+    assert np.max(np.abs(g - 2.0 * J.T @ r)) <= 1e-10 * np.max(np.abs(g))
+
+
+def test_gradient_against_finite_differences(oracle):
+    """The reference's adjoint is continuous-style (not the transpose of the discrete march), so
+    adjoint and finite-difference gradients agree at discretisation level."""
+    rec = make(oracle)
+    k_exp = rec.measure(truth(rec))
+    p = np.full(rec.shape, 0.5).ravel()
+    _f, g = rec.loss_grad(p, k_exp)
+    h = 1e-6
+    fd = np.empty_like(g)
+    for i in range(p.size):
+        e = np.zeros_like(p)
+        e[i] = h
+        fd[i] = (rec.loss_grad(p + e, k_exp)[0] - rec.loss_grad(p - e, k_exp)[0]) / (2 * h)
+    assert np.linalg.norm(g - fd) <= 2e-2 * np.linalg.norm(fd)
+
+
+@pytest.mark.parametrize("method", ["lbfgs", "gauss_newton"])
+def test_fits_lower_the_loss(oracle, method):
+    rec = make(oracle)
+    k_exp = rec.measure(truth(rec))
+    p0 = np.full(rec.shape, 0.5)
+    f0 = rec.loss_grad(p0.ravel(), k_exp)[0]
+    if method == "lbfgs":
+        res = rec.fit_lbfgs(p0, k_exp, maxiter=40)
+    else:
+        res = rec.fit_gauss_newton(p0, k_exp, iterations=8)
+    assert res.loss <= 1e-3 * f0
+    assert np.all(res.params >= 0.0) and np.all(res.params <= 1.0)
