@@ -33,7 +33,14 @@ namespace pn {
 constexpr int MAXE = 4;     // elements per solve
 constexpr int MAXR = 8;     // x-ray lines per solve
 constexpr int MAXSEG = 16;  // work segments per launch
-constexpr int BLOCK = 128;  // threads per block
+constexpr int BLOCK = 128;  // threads per block of the batched generic kernels
+// threads per block of the plain (one solve per launch) kernels: one solve's sub-step launch has
+// only ~4 blocks of 128 per SM on a 2D P11 grid, so 64-thread blocks halve the imbalance between
+// SMs with one block more and one block fewer
+#ifndef PN_PLAIN_BLOCK
+#define PN_PLAIN_BLOCK 64
+#endif
+constexpr int PBLOCK = PN_PLAIN_BLOCK;
 
 struct Geom {
   int n[3];        // points per axis (ghosts included)
@@ -205,6 +212,7 @@ __device__ __forceinline__ void cl_sums(const T* rr, const T (*c)[N + 1], int ne
   }
 }
 
+template <int BS = BLOCK>
 __device__ __forceinline__ bool locate(const Seg* seg, int nseg, int b, int tid, int& s, int& i, int& j,
                                        int& k) {
   s = 0;
@@ -212,7 +220,7 @@ __device__ __forceinline__ bool locate(const Seg* seg, int nseg, int b, int tid,
   const Seg& g = seg[s];
   const int lb = b - g.block0;
   if (g.kind == 0) {
-    const int ty = BLOCK / g.tile_x;
+    const int ty = BS / g.tile_x;
     const int bx = lb % g.tiles_x;
     const int rest = lb / g.tiles_x;
     const int by = rest % g.tiles_y;
@@ -225,7 +233,7 @@ __device__ __forceinline__ bool locate(const Seg* seg, int nseg, int b, int tid,
     k = g.lo[2] + bz;
     return true;
   }
-  const int f = lb * BLOCK + tid;
+  const int f = lb * BS + tid;
   if (f >= g.n_face) return false;
   const int p = g.faces[f];
   i = p & 2047;
@@ -539,9 +547,9 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
 }
 
 template <class T, int N, bool ADJ>
-__global__ void __launch_bounds__(BLOCK, PN_PLAIN_MINB) substep_kernel(const __grid_constant__ SubArgs<T, N> a) {
+__global__ void __launch_bounds__(PBLOCK, PN_PLAIN_MINB * (BLOCK / PBLOCK)) substep_kernel(const __grid_constant__ SubArgs<T, N> a) {
   int s, i, j, k;
-  const bool ok = locate(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k);
+  const bool ok = locate<PBLOCK>(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k);
   const int cls = a.seg[s].cls;
   const bool face = a.seg[s].kind == 1;
   double part[MAXR];
@@ -562,7 +570,7 @@ __global__ void __launch_bounds__(BLOCK, PN_PLAIN_MINB) substep_kernel(const __g
   }
   if (a.partial != nullptr) {
     // block sum of the intensity partials, fixed order -> deterministic
-    __shared__ double red[BLOCK / 32][MAXR];
+    __shared__ double red[PBLOCK / 32][MAXR];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) {
@@ -577,7 +585,7 @@ __global__ void __launch_bounds__(BLOCK, PN_PLAIN_MINB) substep_kernel(const __g
     if (threadIdx.x < a.nr) {
       double v = 0.0;
 #pragma unroll
-      for (int q = 0; q < BLOCK / 32; ++q) v += red[q][threadIdx.x];
+      for (int q = 0; q < PBLOCK / 32; ++q) v += red[q][threadIdx.x];
       a.partial[(long long)blockIdx.x * a.nr + threadIdx.x] = v;
     }
   }
@@ -676,9 +684,9 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
 }
 
 template <class T, int N>
-__global__ void __launch_bounds__(BLOCK) integrate_kernel(const __grid_constant__ IntArgs<T, N> a) {
+__global__ void __launch_bounds__(PBLOCK) integrate_kernel(const __grid_constant__ IntArgs<T, N> a) {
   int s, i, j, k;
-  if (!locate(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k)) return;
+  if (!locate<PBLOCK>(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k)) return;
   const int cls = a.seg[s].cls;
   const bool face = a.seg[s].kind == 1;
   switch (cls) {

@@ -131,9 +131,9 @@ int noalloc_forward(const pn_desc* d, unsigned char* scratch, size_t cap, const 
       g.kind = 0;
       g.block0 = S.nblk[par];
       for (int k = 0; k < 3; ++k) { g.lo[k] = b.lo[k]; g.ext[k] = b.ext[k]; }
-      g.tile_x = (b.ext[1] > 1 || b.ext[2] > 1) ? 32 : BLOCK;
+      g.tile_x = (b.ext[1] > 1 || b.ext[2] > 1) ? 32 : PBLOCK;
       g.tiles_x = (b.ext[0] + g.tile_x - 1) / g.tile_x;
-      g.tiles_y = (b.ext[1] + BLOCK / g.tile_x - 1) / (BLOCK / g.tile_x);
+      g.tiles_y = (b.ext[1] + PBLOCK / g.tile_x - 1) / (PBLOCK / g.tile_x);
       g.nblocks = g.tiles_x * g.tiles_y * b.ext[2];
       S.nblk[par] += g.nblocks;
     }
@@ -142,11 +142,11 @@ int noalloc_forward(const pn_desc* d, unsigned char* scratch, size_t cap, const 
       g.cls = b.cls;
       g.kind = 1;
       g.block0 = S.nblk[par];
-      g.tile_x = BLOCK;
+      g.tile_x = PBLOCK;
       g.tiles_x = g.tiles_y = 1;
       g.n_face = b.nf;
       g.faces = faces_d + b.f0;
-      g.nblocks = (b.nf + BLOCK - 1) / BLOCK;
+      g.nblocks = (b.nf + PBLOCK - 1) / PBLOCK;
       S.nblk[par] += g.nblocks;
     }
   }
@@ -234,7 +234,7 @@ int noalloc_forward(const pn_desc* d, unsigned char* scratch, size_t cap, const 
       a.nseg = S.nseg[par];
       for (int q = 0; q < a.nseg; ++q) a.seg[q] = S.seg[par][q];
       a.partial = sub == 1 ? partial + (long long)i * S.nblk[0] * nr : nullptr;
-      substep_kernel<double, N, false><<<S.nblk[par], BLOCK, 0, s>>>(a);
+      substep_kernel<double, N, false><<<S.nblk[par], PBLOCK, 0, s>>>(a);
       PN_CUDA(cudaGetLastError());
     }
   }

@@ -467,9 +467,9 @@ class Solver : public SolverBase {
         s.kind = 0;
         s.block0 = nblk;
         for (int k = 0; k < 3; ++k) { s.lo[k] = t.lo[k]; s.ext[k] = t.ext[k]; }
-        s.tile_x = (t.ext[1] > 1 || t.ext[2] > 1) ? 32 : BLOCK;
+        s.tile_x = (t.ext[1] > 1 || t.ext[2] > 1) ? 32 : PBLOCK;
         s.tiles_x = (t.ext[0] + s.tile_x - 1) / s.tile_x;
-        const int ty = BLOCK / s.tile_x;
+        const int ty = PBLOCK / s.tile_x;
         s.tiles_y = (t.ext[1] + ty - 1) / ty;
         s.nblocks = s.tiles_x * s.tiles_y * t.ext[2];
         nblk += s.nblocks;
@@ -480,11 +480,11 @@ class Solver : public SolverBase {
         s.cls = t.cls;
         s.kind = 1;
         s.block0 = nblk;
-        s.tile_x = BLOCK;
+        s.tile_x = PBLOCK;
         s.tiles_x = s.tiles_y = 1;
         s.n_face = t.n_face;
         s.faces = faces_d + t.face_off;
-        s.nblocks = (t.n_face + BLOCK - 1) / BLOCK;
+        s.nblocks = (t.n_face + PBLOCK - 1) / PBLOCK;
         nblk += s.nblocks;
         segs.push_back(s);
       }
@@ -562,9 +562,9 @@ class Solver : public SolverBase {
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
     const int nb = nblk_par[par];
     if (adj)
-      substep_kernel<T, N, true><<<nb, BLOCK, 0, stream>>>(a);
+      substep_kernel<T, N, true><<<nb, PBLOCK, 0, stream>>>(a);
     else
-      substep_kernel<T, N, false><<<nb, BLOCK, 0, stream>>>(a);
+      substep_kernel<T, N, false><<<nb, PBLOCK, 0, stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
     return PN_OK;
@@ -606,7 +606,7 @@ class Solver : public SolverBase {
       a.coef[r] = dE * dvol * adj_sigma[(long long)j * L.nr + r] * adj_weight[j];
     }
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
-    integrate_kernel<T, N><<<nblk_all, BLOCK, 0, stream>>>(a);
+    integrate_kernel<T, N><<<nblk_all, PBLOCK, 0, stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
     return PN_OK;
