@@ -108,6 +108,10 @@ class Solver : public SolverBase {
   int nblk_all = 0;
 
   cudaStream_t stream = nullptr;
+  // the even classes' density integral of an adjoint iteration runs on `side`, beside the odd
+  // classes' integral and sub-step 1 (forked and joined by events inside the captured graph)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t g_fwd = nullptr, g_adj = nullptr;
   bool have_forward = false;
   bool have_state = false;
@@ -134,6 +138,9 @@ class Solver : public SolverBase {
         P.owner = 0;
       }
     }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
     for (void* p : allocs) cudaFree(p);
   }
@@ -340,8 +347,11 @@ class Solver : public SolverBase {
       if (m > 0.0 && std::isfinite(m)) scale_g = std::ldexp(1.0, -(int)std::lround(std::log2(m)));
     }
 
-    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) {
-      err = "cudaStreamCreate failed";
+    if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      err = "cudaStreamCreate / cudaEventCreate failed";
       return PN_ERR_CUDA;
     }
     // allocations (a pool user takes its tape from the shared buffer at its first forward)
@@ -570,7 +580,9 @@ class Solver : public SolverBase {
     return PN_OK;
   }
 
-  int launch_integrate(int j, T* u) {
+  // density integral of adjoint iteration j on tape state u: every class (par < 0) or the classes
+  // of one parity, on stream st (the handle's stream by default)
+  int launch_integrate(int j, T* u, int par = -1, cudaStream_t st = nullptr) {
     IntArgs<T, N> a;
     std::memset(&a, 0, sizeof(a));
     common_geom(a.g);
@@ -586,8 +598,9 @@ class Solver : public SolverBase {
     for (int k = 0; k < 3; ++k) a.act[k] = L.act[k];
     a.ne = L.ne;
     a.nr = L.nr;
-    a.nseg = (int)segs_all.size();
-    for (int q = 0; q < a.nseg; ++q) a.seg[q] = segs_all[q];
+    const std::vector<Seg>& sg = par < 0 ? segs_all : segs_par[par];
+    a.nseg = (int)sg.size();
+    for (int q = 0; q < a.nseg; ++q) a.seg[q] = sg[q];
     a.bc = adj_int_bc[j];
     a.scale_g = scale_g;
     a.wfac = dvol * dE * adj_weight[j];
@@ -606,7 +619,7 @@ class Solver : public SolverBase {
       a.coef[r] = dE * dvol * adj_sigma[(long long)j * L.nr + r] * adj_weight[j];
     }
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
-    integrate_kernel<T, N><<<nblk_all, PBLOCK, 0, stream>>>(a);
+    integrate_kernel<T, N><<<par < 0 ? nblk_all : nblk_par[par], PBLOCK, 0, st ? st : stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
     return PN_OK;
@@ -629,7 +642,8 @@ class Solver : public SolverBase {
     return PN_OK;
   }
 
-  int adjoint_step(int j) {
+  // adjoint step j; sub-step 2 first waits for `before_even` when given
+  int adjoint_step(int j, cudaEvent_t before_even = nullptr) {
     const int N1 = N + 1;
     const double* s = adj_s.data() + (long long)j * L.ne;
     const double* c = adj_c.data() + (long long)j * L.ne * N1;
@@ -637,6 +651,7 @@ class Solver : public SolverBase {
     const double dt2 = dE / 2;
     int rc;
     if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 1))) return rc;
+    if (before_even) PN_CUDA(cudaStreamWaitEvent(stream, before_even, 0));
     if ((rc = launch_substep(0, true, dE, s, c, 0.0, lam, lam, lam, nullptr, sg))) return rc;
     if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 2))) return rc;
     return PN_OK;
@@ -679,8 +694,17 @@ class Solver : public SolverBase {
       }
       for (; i > a; --i, ++j) {
         T* u = (i == b) ? slot(ck_index(b)) : slot(n_ck + (i - a - 1));
-        if ((rc = launch_integrate(j, u))) return rc;
-        if ((rc = adjoint_step(j))) return rc;
+        // The even classes' integral reads only the even adjoint classes (changed by sub-step 2)
+        // and writes their rho_bar, acs_bar and noa_bar (eee cells) and the odd classes' ghost
+        // points of the tape state; the odd classes' integral and sub-step 1 touch none of these.
+        // So it runs on the side stream, joined before sub-step 2 (and so before any
+        // recomputation reuses a slot).
+        PN_CUDA(cudaEventRecord(ev_fork, stream));
+        PN_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+        if ((rc = launch_integrate(j, u, 0, side))) return rc;
+        PN_CUDA(cudaEventRecord(ev_join, side));
+        if ((rc = launch_integrate(j, u, 1))) return rc;
+        if ((rc = adjoint_step(j, ev_join))) return rc;
       }
     }
     if ((rc = launch_integrate(L.ns, slot(ck_index(0))))) return rc;
