@@ -642,8 +642,9 @@ class Solver : public SolverBase {
     return PN_OK;
   }
 
-  // adjoint step j; sub-step 2 first waits for `before_even` when given
-  int adjoint_step(int j, cudaEvent_t before_even = nullptr) {
+  // adjoint step j; sub-step 2 first waits for `before_even` and is followed by a record of
+  // `after_even`, when given
+  int adjoint_step(int j, cudaEvent_t before_even = nullptr, cudaEvent_t after_even = nullptr) {
     const int N1 = N + 1;
     const double* s = adj_s.data() + (long long)j * L.ne;
     const double* c = adj_c.data() + (long long)j * L.ne * N1;
@@ -653,6 +654,7 @@ class Solver : public SolverBase {
     if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 1))) return rc;
     if (before_even) PN_CUDA(cudaStreamWaitEvent(stream, before_even, 0));
     if ((rc = launch_substep(0, true, dE, s, c, 0.0, lam, lam, lam, nullptr, sg))) return rc;
+    if (after_even) PN_CUDA(cudaEventRecord(after_even, stream));
     if ((rc = launch_substep(1, true, dt2, s, c, 0.0, lam, lam, lam, nullptr, sg, 2))) return rc;
     return PN_OK;
   }
@@ -682,6 +684,7 @@ class Solver : public SolverBase {
     PN_CUDA(cudaMemsetAsync(acs_bar_d, 0, sizeof(double) * (size_t)L.n_eee_cells * std::max(L.nr, 1), stream));
     PN_CUDA(cudaMemsetAsync(noa_bar_d, 0, sizeof(double) * (size_t)L.n_eee_cells * L.ne, stream));
     int j = 0;
+    const bool early = K == 1;   // every state kept: no recomputation between iterations
     for (int i = L.ns; i >= 1;) {
       // segment (a, b] holding step i
       const int a = ((i - 1) / K) * K;
@@ -698,13 +701,16 @@ class Solver : public SolverBase {
         // and writes their rho_bar, acs_bar and noa_bar (eee cells) and the odd classes' ghost
         // points of the tape state; the odd classes' integral and sub-step 1 touch none of these.
         // So it runs on the side stream, joined before sub-step 2 (and so before any
-        // recomputation reuses a slot).
-        PN_CUDA(cudaEventRecord(ev_fork, stream));
+        // recomputation reuses a slot).  With every state kept (no recomputation) it is forked
+        // right after the previous iteration's sub-step 2, the last change of the even classes,
+        // and so also overlaps that iteration's sub-step 3.
+        const bool forked = early && j > 0;
+        if (!forked) PN_CUDA(cudaEventRecord(ev_fork, stream));
         PN_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
         if ((rc = launch_integrate(j, u, 0, side))) return rc;
         PN_CUDA(cudaEventRecord(ev_join, side));
         if ((rc = launch_integrate(j, u, 1))) return rc;
-        if ((rc = adjoint_step(j, ev_join))) return rc;
+        if ((rc = adjoint_step(j, ev_join, early && j + 1 < L.ns ? ev_fork : nullptr))) return rc;
       }
     }
     if ((rc = launch_integrate(L.ns, slot(ck_index(0))))) return rc;
