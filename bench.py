@@ -66,6 +66,9 @@ def parse():
                     help="3D 96x96x64 P7 forward+adjoint (FP32 batch, checkpoint stride 16) with a central "
                          "finite-difference check of the mass-fraction gradient on 32 cells; prints its own line")
     ap.add_argument("--fd-cells", type=int, default=32)
+    ap.add_argument("--material", action="store_true",
+                    help="device material fields and pullbacks on the 3D 96x96x64 per-cell boxed material "
+                         "(3 elements, 3 lines, 100 samples per ray) against the host numpy path; prints its own line")
     ap.add_argument("--config1", action="store_true",
                     help="1D slab (config 1): FP64 plain latency, FP32 batch of 256 compositions, gradient vs "
                          "finite differences of the oracle on all 200 cells; prints its own line")
@@ -771,6 +774,74 @@ def material_gradient(s, rho_bar, noa_bar, acs_bar, acs):
     return g
 
 
+def run_material(args):
+    """pn_material_fields / pn_material_pullback on config 4's material, timed with CUDA events
+    (inputs resident), beside the host numpy material path on the same inputs."""
+    import torch
+    from pnepma_gb300 import capi, workloads
+    from pnepma_gb300.material_model import MaterialModel
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    s = workloads.config4()
+    m = s.material
+    beam = s.problem.beam_position.mean
+    mm, P = MaterialModel.per_cell_boxed(m, s.x_rays, s.detector, beam_x=beam[0])
+    dm = capi.DeviceMaterial(mm)
+    t0 = time.perf_counter()
+    rho_h, noa_h, acs_h = s.inputs()
+    host_fields_s = time.perf_counter() - t0
+    n_rho, n_noa, n_acs = rho_h.size, noa_h.size, acs_h.size
+    rng = np.random.default_rng(0)
+    n_eee_rho = noa_h.shape[0] * m.n_e
+    rb = np.zeros(n_rho)
+    rb[:n_eee_rho] = rng.normal(size=n_eee_rho)      # eee grid only: its points are box centres
+    nb, ab = rng.normal(size=noa_h.shape), rng.normal(size=acs_h.shape)
+    t0 = time.perf_counter()
+    g_h = material_gradient(s, rb, nb, ab, acs_h)
+    host_pullback_s = time.perf_counter() - t0
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+    dP, d_rb, d_nb, d_ab = dv(P), dv(rb), dv(nb), dv(ab)
+    z = lambda n: torch.zeros(int(n), dtype=torch.float64, device=dev)
+    d_rho, d_noa, d_acs, d_G = z(n_rho), z(n_noa), z(n_acs), z(mm.n_params)
+    st = torch.cuda.current_stream(dev).cuda_stream
+
+    def fields():
+        dm.fields(dP.data_ptr(), d_rho.data_ptr(), d_noa.data_ptr(), d_acs.data_ptr(), stream=st)
+
+    def pullback():
+        dm.pullback(dP.data_ptr(), d_G.data_ptr(), d_rb.data_ptr(), d_nb.data_ptr(), d_acs.data_ptr(),
+                    d_ab.data_ptr(), stream=st)
+
+    out = {}
+    for name, fn in (("fields", fields), ("pullback", pullback)):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(args.steps, 5)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[name] = e0.elapsed_time(e1) / reps
+    rho_d, noa_d, acs_d, G_d = (t.cpu().numpy() for t in (d_rho, d_noa, d_acs, d_G))
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    n_samples = noa_h.shape[0] * mm.n_int_points
+    line = {"metric": "material fields + pullback time (3D 96x96x64 per-cell boxes, Fe/Cr/Ni, 3 lines)",
+            "value": out["fields"] + out["pullback"], "unit": "ms", "higher_is_better": False,
+            "fields_ms": out["fields"], "pullback_ms": out["pullback"],
+            "host_numpy_fields_s": host_fields_s, "host_numpy_pullback_s": host_pullback_s,
+            "grid_points": int(n_rho // m.n_e), "ray_samples": int(n_samples),
+            "fields_write_gb_per_s": (n_rho + n_noa + n_acs) * 8 / (out["fields"] * 1e-3) / 1e9,
+            "rel_err_vs_host": {"rho_eee": rel(rho_d[:n_eee_rho], rho_h[:n_eee_rho]), "noa": rel(noa_d, noa_h.ravel()),
+                                "acs": rel(acs_d, acs_h.ravel()), "gradient": rel(G_d[:-m.n_par], g_h.ravel())},
+            "config": {"workload": "config 4 material: MassFraction over one box per eee cell, 100 samples per "
+                                   "absorption ray", "params": int(mm.n_params)}}
+    dm.close()
+    print(json.dumps(line), flush=True)
+
+
 def run_config4(args):
     import torch
     from pnepma_gb300 import capi, workloads
@@ -1112,6 +1183,8 @@ def main():
         run_serve(args)
     elif args.config4:
         run_config4(args)
+    elif args.material:
+        run_material(args)
     elif args.config1:
         run_config1(args)
     elif args.config3:

@@ -347,9 +347,105 @@ int pn_server_query(pn_server* s, pn_server_info* info);
 /* Requests not yet admitted fail with PN_ERR_STATE; running waves are completed first. */
 void pn_server_destroy(pn_server* s);
 
+/*
+ * Material on the device: the solve's inputs from the material parameters, and the material
+ * pullbacks of the gradient, so that neither the fields nor m_bar cross to the host.
+ *
+ *   pn_material_fields    <- component_densities(m, gspec)       pn_material_utils.jl:74-83
+ *                            compute_number_of_atoms             x_ray_intensities.jl:43-55
+ *                            compute_absorption_coefficients     x_ray_intensities.jl:100-128
+ *   pn_material_pullback  <- component_densities_pullback        pn_material_utils.jl:85-91
+ *                            compute_absorption_coefficient_pullback  x_ray_intensities.jl:131-153
+ *                            compute_number_of_atoms_pullback    x_ray_intensities.jl:84-96
+ *                            (the three calls at the end of calc_intensities_pullback,
+ *                            pn_intensities.jl:406-409)
+ *
+ * Material models (pn_parametrizations/pn_material.jl): with p the parametrisation's value at a
+ * point (n_e values, or n_e - 1 for an SC variant, whose last component is 1 - sum of the others):
+ *   MassConcentration  rho = p                              (:56-77; no SC variant)
+ *   VolumeFraction     rho = p .* rho_pure                  (:79-134)
+ *   LinearDensity      rho = p * dot(p, rho_pure)           (:137-197)
+ *   MassFraction       rho = p / sum(p ./ rho_pure)         (:199-264)
+ * Parametrisations: Const (pn_parametrization_const.jl), Boxed (pn_parametrization_boxed.jl:
+ * piecewise constant on the boxes between slices, `embedding` outside) and Bilinear
+ * (pn_parametrization_bilinear.jl with biliner_interp.jl:63-111: trilinear between knots, the
+ * embedding value at knots outside the grid).
+ * Parameter vector (the reference's param_vec order): Const: [n_par]; Boxed and Bilinear:
+ * [z][y][x][n_par] over boxes or knots, then the embedding [n_par] (always present; its entries of
+ * params_bar are the embedding's gradient, which a non-optimisable embedding ignores).
+ */
+typedef enum pn_material_model {
+  PN_MAT_MASS_CONCENTRATION = 0,
+  PN_MAT_VOLUME_FRACTION = 1,
+  PN_MAT_LINEAR_DENSITY = 2,
+  PN_MAT_MASS_FRACTION = 3
+} pn_material_model;
+
+typedef enum pn_parametrization_kind {
+  PN_PAR_CONST = 0,
+  PN_PAR_BOXED = 1,
+  PN_PAR_BILINEAR = 2
+} pn_parametrization_kind;
+
+/* Slices (box boundaries) or knots along one axis.  Range form (`values` NULL): a StepRangeLen
+   with Float64(ref), Float64(step), its offset (1-based index of ref) and length n; located by
+   floor((x - ref) / step) (biliner_interp.jl:5-15).  Vector form (Boxed only): n increasing values
+   located by the reference's linear search (biliner_interp.jl:18-36), under which a point on an
+   interior slice belongs to the box below it. */
+typedef struct pn_slices {
+  int32_t n;
+  int32_t offset;
+  double ref;
+  double step;
+  const double* values;
+} pn_slices;
+
+typedef struct pn_material_desc {
+  int32_t model;             /* pn_material_model */
+  int32_t sc;                /* 1: the SC variant (not for MassConcentration) */
+  int32_t parametrization;   /* pn_parametrization_kind */
+  int32_t n_elements;        /* n_e */
+  int32_t n_points[3];       /* the solve's pn_desc.n_points */
+  int32_t n_xrays;           /* lines of the absorption factors (0: none) */
+  int32_t n_int_points;      /* samples per absorption ray (the reference uses 100) */
+  int32_t reserved;
+  /* grid coordinates per axis x, y, z: the even points (n_points[d]) then the odd points
+     (n_points[d] + 1; 1 on a singleton axis), as points(eo, gspec) yields them */
+  const double* coords;
+  pn_slices slices[3];       /* unused for Const */
+  const double* rho_pure;    /* [n_e] VolumeFraction / MassFraction rho_pure, LinearDensity rho */
+  const double* atom_mass;   /* [n_e] mass of one atom (g), the divisor of the number of atoms */
+  const double* mac;         /* [n_r][n_e] mass absorption coefficients */
+  double detector[3];        /* detector position x_d */
+  double beam_x;             /* x coordinate of the beam position x_b */
+} pn_material_desc;
+
+typedef struct pn_material pn_material;
+
+/* Validate the descriptor and copy its tables to the device; *n_params receives the length of
+   the parameter vector (NULL allowed). */
+int pn_material_create(const pn_material_desc* desc, pn_material** out, int64_t* n_params);
+
+/* Device pointers, ordered on `stream` (a cudaStream_t, NULL = legacy default stream).  params:
+   [n_params].  Outputs in pn_forward's layouts, each optional (NULL skips it): rho [n_rho] on all
+   eight class grids, noa [n_eee_cells][n_e], acs [n_eee_cells][n_r]. */
+int pn_material_fields(pn_material* m, const double* params, double* rho, double* noa, double* acs,
+                       void* stream);
+
+/* params_bar [n_params] (overwritten) = the parameter gradient of sum(rho_bar . rho) +
+   sum(noa_bar . noa) + sum(acs_bar . acs), from pn_adjoint's outputs; acs is the forward's
+   absorption factors.  Any of rho_bar, noa_bar and acs_bar may be NULL (acs then too).
+   Accumulated with FP64 atomics: the summation order, hence the last bits, may vary between
+   runs. */
+int pn_material_pullback(pn_material* m, const double* params, const double* rho_bar,
+                         const double* noa_bar, const double* acs, const double* acs_bar,
+                         double* params_bar, void* stream);
+
+void pn_material_destroy(pn_material* m);
+
 /* Human-readable description of the last error on this handle (or, when h is NULL, of the last
    failed call in this thread that has no handle: pn_create, pn_query_sizes, pn_batch_*,
-   pn_forward_noalloc, pn_server_*, pn_submit, pn_poll, pn_wait).  Never NULL. */
+   pn_forward_noalloc, pn_server_*, pn_submit, pn_poll, pn_wait, pn_material_*).  Never NULL. */
 const char* pn_last_error(const pn_handle* h);
 
 /* Self-test of the FP32 exponential factor phi1(c) = (e^c - 1) / c used by the FP32 kernels

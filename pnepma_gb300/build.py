@@ -67,12 +67,14 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
     objs.append(o)
     if force or _stale(o, deps + [capi]):
         jobs.append((capi, o, [], extra))
-    for unit in ("pn_batch", "pn_noalloc", "pn_server", "pn_selftest"):
+    # the material unit rounds every product and sum separately, as the reference's Julia code does
+    unit_flags = {"pn_material": ["-fmad=false"]}
+    for unit in ("pn_batch", "pn_noalloc", "pn_server", "pn_selftest", "pn_material"):
         src = os.path.join(CSRC, unit + ".cu")
         o = os.path.join(out_dir, unit + ".o")
         objs.append(o)
         if force or _stale(o, deps + [src]):
-            jobs.append((src, o, [], extra))
+            jobs.append((src, o, [], extra + unit_flags.get(unit, [])))
     for unit in ("pn_order", "pn_order_batch"):
         src = os.path.join(CSRC, unit + ".cu")
         for N in codegen.ORDERS:

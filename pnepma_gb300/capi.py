@@ -73,7 +73,8 @@ SERVER_EXPORTS = ("pn_server_create", "pn_submit", "pn_poll", "pn_wait", "pn_ser
 EXPORTS = SERVER_EXPORTS + ("pn_batch_create", "pn_batch_forward", "pn_batch_adjoint", "pn_batch_query", "pn_batch_destroy",
            "pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
-           "pn_abi_version", "pn_compiled_orders")
+           "pn_abi_version", "pn_compiled_orders", "pn_material_create", "pn_material_fields",
+           "pn_material_pullback", "pn_material_destroy")
 
 
 class PnError(RuntimeError):
@@ -133,6 +134,14 @@ def lib():
         L.pn_server_destroy.restype = None
         L.pn_selftest_phi1.argtypes = [ctypes.c_int32, P, P, P]
         L.pn_selftest_phi1.restype = ctypes.c_int
+        L.pn_material_create.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int64)]
+        L.pn_material_create.restype = ctypes.c_int
+        L.pn_material_fields.argtypes = [P, P, P, P, P, P]
+        L.pn_material_fields.restype = ctypes.c_int
+        L.pn_material_pullback.argtypes = [P, P, P, P, P, P, P, P]
+        L.pn_material_pullback.restype = ctypes.c_int
+        L.pn_material_destroy.argtypes = [P]
+        L.pn_material_destroy.restype = None
         L.pn_abi_version.restype = ctypes.c_int32
         L.pn_compiled_orders.restype = ctypes.c_int64
         for name in ("pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device",
@@ -407,6 +416,46 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DeviceMaterial:
+    """Owns one ``pn_material``: a material model whose fields and pullbacks run on the GPU.
+
+    `model` is a ``material_model.MaterialModel``.  The calls take device pointers (ints) and are
+    ordered on `stream` (a cudaStream_t as int, 0 = legacy default stream)."""
+
+    def __init__(self, model):
+        self.model = model
+        self.desc, self._keep = model.descriptor()
+        m = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        rc = lib().pn_material_create(ctypes.byref(self.desc), ctypes.byref(m), ctypes.byref(n))
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+        self._m = m
+        self.n_params = int(n.value)
+
+    def _check(self, rc):
+        if rc:
+            raise PnError(rc, lib().pn_last_error(None).decode())
+
+    def fields(self, params, rho=None, noa=None, acs=None, stream=0):
+        self._check(lib().pn_material_fields(self._m, _ptr(params), _ptr(rho), _ptr(noa), _ptr(acs), _ptr(stream)))
+
+    def pullback(self, params, params_bar, rho_bar=None, noa_bar=None, acs=None, acs_bar=None, stream=0):
+        self._check(lib().pn_material_pullback(self._m, _ptr(params), _ptr(rho_bar), _ptr(noa_bar), _ptr(acs),
+                                               _ptr(acs_bar), _ptr(params_bar), _ptr(stream)))
+
+    def close(self):
+        if getattr(self, "_m", None):
+            lib().pn_material_destroy(self._m)
+            self._m = None
 
     def __del__(self):
         try:

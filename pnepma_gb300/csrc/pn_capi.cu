@@ -167,16 +167,21 @@ int pn_adjoint(pn_handle* h, const double* intensities_bar, double* rho_bar, dou
   PN_GUARD(h->s->adjoint(intensities_bar, rho_bar, noa_bar, acs_bar, nullptr, false))
 }
 
+// The stream argument of the device-pointer calls: NULL names the legacy default stream (the
+// solver's own non-blocking stream, which does not synchronise with it, serves the host-pointer
+// calls only).
+static cudaStream_t caller_stream(void* stream) { return stream ? (cudaStream_t)stream : cudaStreamLegacy; }
+
 int pn_forward_device(pn_handle* h, const double* rho, const double* noa, const double* acs, double* intensities,
                       void* stream) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
-  PN_GUARD(h->s->forward(rho, noa, acs, intensities, (cudaStream_t)stream, true))
+  PN_GUARD(h->s->forward(rho, noa, acs, intensities, caller_stream(stream), true))
 }
 
 int pn_adjoint_device(pn_handle* h, const double* intensities_bar, double* rho_bar, double* noa_bar,
                       double* acs_bar, void* stream) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
-  PN_GUARD(h->s->adjoint(intensities_bar, rho_bar, noa_bar, acs_bar, (cudaStream_t)stream, true))
+  PN_GUARD(h->s->adjoint(intensities_bar, rho_bar, noa_bar, acs_bar, caller_stream(stream), true))
 }
 
 int pn_generation_field(pn_handle* h, const double* rho, double* field) {
