@@ -7,6 +7,7 @@ import subprocess
 import pytest
 
 from pnepma_gb300 import capi
+from pnepma_gb300.material_model import PnMaterialDesc, PnSlices
 from pnepma_gb300.problem import PnDesc, PnSizes
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -33,6 +34,7 @@ STRUCTS = {
     "pn_batch_info": capi.PnBatchInfo, "pn_handle_info": capi.PnHandleInfo,
     "pn_server_options": capi.PnServerOptions, "pn_request": capi.PnRequest,
     "pn_ticket_info": capi.PnTicketInfo, "pn_server_info": capi.PnServerInfo,
+    "pn_slices": PnSlices, "pn_material_desc": PnMaterialDesc,
 }
 
 
