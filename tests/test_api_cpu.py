@@ -1,0 +1,92 @@
+"""The reference-shaped Python API (pnepma_gb300/api.py) on the CPU: a pullback reads the tape of
+its own forward even when other calls used the shared handle in between, and a GPUMaterial reaches
+the device library (which reports that there is no device here)."""
+import numpy as np
+import pytest
+
+from pnepma_gb300 import api, capi, workloads
+from pnepma_gb300.material_model import MaterialModel
+
+
+class FakeHandle:
+    """Records which densities the tape was marched with; the adjoint returns them as rho_bar."""
+
+    def __init__(self, n_noa, n_acs, nr):
+        self.tape = None
+        self.n_noa, self.n_acs, self.nr = n_noa, n_acs, nr
+        self.forwards = 0
+
+    def forward(self, rho, noa, acs):
+        self.tape = np.array(rho, copy=True)
+        self.forwards += 1
+        return np.ones(self.nr)
+
+    def adjoint(self, ibar):
+        return self.tape.copy(), np.zeros(self.n_noa), np.zeros(self.n_acs)
+
+    def generation_field(self, rho):
+        self.tape = None
+        return np.zeros(1)
+
+
+def test_pullback_marches_its_own_forward_again_after_another_call(monkeypatch):
+    s = workloads.small_case(dims=1, N=3, shape=(12,), n_steps=4)
+    rho, noa, acs = s.inputs()
+    fake = FakeHandle(noa.size, acs.size, len(s.x_rays))
+    monkeypatch.setattr(api, "get_handle", lambda problem, x_rays: fake)
+    seen = []
+
+    class Mat:
+        """The host material protocol; each instance has its own densities."""
+
+        def __init__(self, scale):
+            self.scale = scale
+            self.n_e = s.material.n_e
+            self.values = s.material.values
+
+        def rho_flat(self):
+            return rho * self.scale
+
+        def number_of_atoms(self):
+            return noa
+
+        def absorption(self, *a):
+            return acs
+
+        def grid_pullback(self, rho_bar):
+            seen.append(float(rho_bar[np.argmax(np.abs(rho))] / rho[np.argmax(np.abs(rho))]))
+            return np.zeros(1)
+
+        def absorption_pullback(self, *a):
+            return np.zeros(1), np.zeros(1)
+
+        def noa_pullback(self, nb):
+            return np.zeros(1)
+
+    A, B = Mat(1.0), Mat(2.0)
+    _, pb_a = api.calc_intensities_pullback(s.problem, A, s.x_rays, s.detector)
+    _, pb_b = api.calc_intensities_pullback(s.problem, B, s.x_rays, s.detector)
+    assert fake.forwards == 2
+    pb_b(np.ones(len(s.x_rays)))          # B still owns the tape: no new forward
+    assert fake.forwards == 2 and seen[-1] == pytest.approx(2.0)
+    pb_a(np.ones(len(s.x_rays)))          # A's tape was overwritten by B: marched again
+    assert fake.forwards == 3 and seen[-1] == pytest.approx(1.0)
+    pb_a(np.ones(len(s.x_rays)))
+    assert fake.forwards == 3
+    api.calc_x_ray_generation_field(s.problem, B, s.x_rays)
+    pb_a(np.ones(len(s.x_rays)))          # the generation field replaced the densities
+    assert fake.forwards == 4 and seen[-1] == pytest.approx(1.0)
+
+
+def test_gpu_material_reaches_the_device_library():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    s = workloads.small_case(dims=1, N=3, shape=(12,), n_steps=4)
+    mm, P = MaterialModel.per_cell_boxed(s.material, s.x_rays, s.detector)
+    m = api.GPUMaterial(mm, P)
+    with pytest.raises(capi.PnError) as e:
+        m.device(s.x_rays, s.detector, 0.0)
+    assert e.value.code == -9
+    with pytest.raises(ValueError):
+        api.GPUMaterial(mm, P[:-1])
