@@ -117,7 +117,9 @@ def calc_intensities(problem: ForwardPNProblem, m, x_rays, detector_position) ->
         return _device_forward(problem, m, x_rays, detector_position)[3]
     h = get_handle(problem, x_rays)
     rho, noa, acs = _inputs(problem, m, x_rays, detector_position)
-    return h.forward(rho, noa, acs)
+    I = h.forward(rho, noa, acs)
+    _mark(h)                 # this forward replaced the tape of any pending pullback
+    return I
 
 
 def calc_intensities_pullback(problem: ForwardPNProblem, m, x_rays, detector_position):

@@ -76,6 +76,10 @@ def test_pullback_marches_its_own_forward_again_after_another_call(monkeypatch):
     api.calc_x_ray_generation_field(s.problem, B, s.x_rays)
     pb_a(np.ones(len(s.x_rays)))          # the generation field replaced the densities
     assert fake.forwards == 4 and seen[-1] == pytest.approx(1.0)
+    api.calc_intensities(s.problem, B, s.x_rays, s.detector)     # a plain forward of another material
+    assert fake.forwards == 5
+    pb_a(np.ones(len(s.x_rays)))
+    assert fake.forwards == 6 and seen[-1] == pytest.approx(1.0)
 
 
 def test_gpu_material_reaches_the_device_library():
