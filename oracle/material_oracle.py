@@ -14,6 +14,12 @@ Follows, point by point and in the reference's loop and summation order:
   (``x_ray_intensities.jl:43-96``), the 100-sample absorption factors and their pullback
   (``x_ray_intensities.jl:100-153``).
 
+Parity status: "parity unpinned" against the reference itself (Julia is not available here, and
+the reference's own pn_material_test.jl checks its pullbacks only against finite differences).  This
+restatement is pinned the same way: by central finite differences of its own fields for every
+model and parametrisation, by the reference's point-location rules as known answers, and by the
+host boxed mass-fraction path, which it reproduces to 1e-14 (tests/test_material_cpu.py).
+
 Sums run left to right as Julia's ``sum`` and the broadcast expressions do for short vectors;
 ``dot`` and ``mul!`` (BLAS in Julia) are written as left-to-right sums, which can differ from the
 BLAS result in the last bits.  Inputs come from a ``MaterialModel`` (``pnepma_gb300``), the same
