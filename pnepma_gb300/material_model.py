@@ -154,6 +154,12 @@ class MaterialModel:
         d.beam_x = self.beam_x
         return d, keep
 
+    def with_geometry(self, x_rays, detector, beam_x: float) -> "MaterialModel":
+        """The same material seen from another measurement geometry (lines, detector, beam)."""
+        return MaterialModel(self.gspec, self.elements, self.model, sc=self.sc, parametrization=self.parametrization,
+                             slices=self.slices, x_rays=list(x_rays), detector=detector, beam_x=beam_x,
+                             n_int_points=self.n_int_points)
+
     @staticmethod
     def per_cell_boxed(mat, x_rays, detector, beam_x: float = 0.0, n_int_points: int = 100):
         """(MaterialModel, params) of a ``material.BoxedMassFraction``: a MassFraction(SC) model

@@ -20,6 +20,12 @@ the host as in the reference, where they follow the adjoint.
 
 The Jacobian of the k-ratios (for Gauss-Newton) takes one adjoint per k-ratio: the problems are
 repeated once per line in a second batch, each copy with the unit cotangent of its line.
+
+The fitted material is either the per-cell boxed mass fractions (host material and pullbacks) or
+any ``MaterialModel`` -- the reference's reconstructions fit a VolumeFractionSC material over a
+Boxed or Bilinear field of ten parameters with a fixed embedding (``reconstructions_1d.jl:115-130``)
+-- whose fields and pullbacks run on the device through one ``pn_material`` per measurement
+geometry (:class:`DeviceMaterialSet`).
 """
 from __future__ import annotations
 
@@ -30,6 +36,7 @@ import numpy as np
 from . import physics
 from .grid import GridSpec
 from .material import BoxedMassFraction
+from .material_model import MaterialModel
 from .problem import PN_FP64
 from .workloads import NM, Solve, make_solve, stable_steps
 
@@ -77,6 +84,119 @@ class BatchBackend:
 
     def close(self):
         self.batch.close()
+
+
+class DeviceMaterialSet:
+    """The fields and pullbacks of a ``MaterialModel`` for every problem of a reconstruction, on the
+    device: one ``pn_material`` per measurement geometry (lines, detector, beam position), shared by
+    the problems that have the same one.  Host arrays in and out, as the batch backend takes them."""
+
+    def __init__(self, model: MaterialModel, solves, device: int = 0):
+        import torch
+        from . import capi
+        self.torch = torch
+        self.dev = torch.device("cuda", device)
+        cache, self.mats, self.sizes = {}, [], []
+        for s in solves:
+            key = (tuple(s.x_rays), tuple(float(v) for v in s.detector), float(s.problem.beam_position.mean[0]))
+            if key not in cache:
+                cache[key] = capi.DeviceMaterial(model.with_geometry(s.x_rays, s.detector, key[2]))
+            self.mats.append(cache[key])
+            d, k = s.problem.descriptor(s.x_rays)
+            self.sizes.append(capi.query_sizes(d))
+        self._owned = list(cache.values())
+        self.ne, self.nr = model.n_e, [len(s.x_rays) for s in solves]
+
+    def _dv(self, a):
+        return self.torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(self.dev)
+
+    def _z(self, n):
+        return self.torch.zeros(max(int(n), 1), dtype=self.torch.float64, device=self.dev)
+
+    def fields(self, P):
+        """[(rho, noa [cells][n_e], acs [cells][n_r])] per problem."""
+        dP = self._dv(P)
+        out = []
+        for dm, sz in zip(self.mats, self.sizes):
+            rho, noa, acs = self._z(sz.n_rho), self._z(sz.n_noa), self._z(sz.n_acs)
+            dm.fields(dP.data_ptr(), rho.data_ptr(), noa.data_ptr(), acs.data_ptr())
+            out.append((rho, noa, acs))
+        self.torch.cuda.synchronize(self.dev)
+        res = []
+        for (rho, noa, acs), sz, nr in zip(out, self.sizes, self.nr):
+            res.append((rho.cpu().numpy()[:sz.n_rho], noa.cpu().numpy()[:sz.n_noa].reshape(-1, self.ne),
+                        acs.cpu().numpy()[:sz.n_acs].reshape(-1, max(nr, 1))))
+        return res
+
+    def pullback(self, i, P, rho_bar, noa_bar, acs, acs_bar):
+        """Parameter gradient of problem i from its adjoint outputs."""
+        dm = self.mats[i]
+        G = self._z(dm.n_params)
+        dP, rb, nb, a, ab = (self._dv(x) for x in (P, rho_bar, noa_bar, acs, acs_bar))
+        dm.pullback(dP.data_ptr(), G.data_ptr(), rb.data_ptr(), nb.data_ptr(), a.data_ptr(), ab.data_ptr())
+        self.torch.cuda.synchronize(self.dev)
+        return G.cpu().numpy()[:dm.n_params]
+
+    def close(self):
+        for dm in self._owned:
+            dm.close()
+        self._owned = []
+
+
+class _BoxedMaterials:
+    """Per-cell boxed mass fractions: host material, host pullbacks (the parameters are the
+    ``values`` of a ``BoxedMassFraction``)."""
+
+    def __init__(self, rec):
+        self.rec = rec
+        self.shape = rec.gspec.class_shape(0)[::-1] + (rec.n_par,)
+
+    def inputs(self, p):
+        r = self.rec
+        m = BoxedMassFraction(r.elements, r.gspec, np.asarray(p, float).reshape(self.shape), sc=r.sc)
+        return m, [Solve(s.problem, m, s.x_rays, s.detector).inputs() for s in r.solves]
+
+    def pullback(self, m, i, inputs_i, rb, nb, ab):
+        s = self.rec.solves[i]
+        g = m.grid_pullback(rb) + m.noa_pullback(nb.reshape(self.shape[:-1] + (self.rec.n_e,)))
+        g = g + m.absorption_pullback(s.x_rays, s.detector, s.problem.beam_position.mean, inputs_i[2], ab)[0]
+        return g.ravel()
+
+    def close(self):
+        pass
+
+
+class _ModelMaterials:
+    """A ``MaterialModel`` through a material set (fields and per-problem pullbacks); the free
+    parameters are its parameter vector, without the embedding when that is fixed."""
+
+    def __init__(self, rec, model: MaterialModel, embedding, material_set_factory):
+        if model.gspec != rec.gspec or [e.symbol for e in model.elements] != [e.symbol for e in rec.elements]:
+            raise ValueError("the material model must live on the reconstruction's grid and elements")
+        if model.sc != rec.sc:
+            raise ValueError("the material model's SC flag must match the reconstruction's")
+        self.model = model
+        self.embedding = None if embedding is None else np.asarray(embedding, dtype=float).ravel()
+        if self.embedding is not None and self.embedding.size != model.n_par:
+            raise ValueError(f"the embedding has {model.n_par} values")
+        self.n_free = model.n_params - (model.n_par if self.embedding is not None else 0)
+        self.shape = (self.n_free,)
+        factory = material_set_factory or (lambda mm, solves: DeviceMaterialSet(mm, solves))
+        self.set = factory(model, rec.solves)
+
+    def full(self, p):
+        p = np.asarray(p, dtype=float).ravel()
+        return np.concatenate([p, self.embedding]) if self.embedding is not None else p
+
+    def inputs(self, p):
+        P = self.full(p)
+        return P, self.set.fields(P)
+
+    def pullback(self, P, i, inputs_i, rb, nb, ab):
+        return self.set.pullback(i, P, rb, nb, inputs_i[2], ab)[:self.n_free]
+
+    def close(self):
+        self.set.close()
 
 
 # --------------------------------------------------------------------------- standards cache
@@ -156,17 +276,24 @@ class Reconstruction:
     stable count for the lowest stopping power of the pure elements, so that every mixture the
     fit visits (and every standard) marches stably.  ``backend_factory(descs, keep)`` returns an
     object with ``forward(inputs)``, ``adjoint(ibars)`` and ``close()``; by default the GPU batch.
+
+    With ``model`` (a ``MaterialModel`` on the same grid and elements) the fitted parameters are the
+    model's parameter vector, without the embedding when ``embedding`` fixes it (the reference's
+    ``BoxedPNParametrization{false}`` / ``BilinearPNParametrization{false}``).
+    ``material_set_factory(model, solves)`` returns an object with ``fields(P)``,
+    ``pullback(i, P, rho_bar, noa_bar, acs, acs_bar)`` and ``close()``; by default
+    :class:`DeviceMaterialSet`.
     """
 
     def __init__(self, N: int, gspec: GridSpec, elements, energies_kev, beam_ys=(0.0,), detector=(50 * NM, 0.0, 0.0),
                  n_steps: int = 100, precision: int = PN_FP64, sc: bool = True, beam_sigma: float = 30 * NM,
-                 E_cut=None, backend_factory=None, memory_budget: int = 0):
+                 E_cut=None, backend_factory=None, memory_budget: int = 0, model: MaterialModel | None = None,
+                 embedding=None, material_set_factory=None):
         self.gspec = gspec
         self.elements = [physics.ELEMENTS[e] if isinstance(e, str) else e for e in elements]
         self.sc = sc
         self.n_e = len(self.elements)
         self.n_par = self.n_e - 1 if sc else self.n_e
-        self.shape = gspec.class_shape(0)[::-1] + (self.n_par,)
         self.backend_factory = backend_factory or (lambda d, k: BatchBackend(d, k, memory_budget=memory_budget))
         names = [e.symbol for e in self.elements]
         mix = np.full(gspec.class_shape(0)[::-1] + (self.n_e,), 1.0 / self.n_e)
@@ -186,13 +313,15 @@ class Reconstruction:
         self.std = standard_intensities(self.solves, self.backend_factory, sc)
         self._be = None
         self._jac_be = None
+        self.mat = (_ModelMaterials(self, model, embedding, material_set_factory) if model is not None
+                    else _BoxedMaterials(self))
+        self.shape = self.mat.shape
 
     # ------------------------------------------------------------------ material and inputs
-    def material(self, p) -> BoxedMassFraction:
-        return BoxedMassFraction(self.elements, self.gspec, np.asarray(p, float).reshape(self.shape), sc=self.sc)
-
-    def _inputs(self, m):
-        return [Solve(s.problem, m, s.x_rays, s.detector).inputs() for s in self.solves]
+    def material(self, p):
+        """The material of parameters p: a ``BoxedMassFraction``, or the model's full parameter
+        vector (embedding included)."""
+        return self.mat.inputs(p)[0] if isinstance(self.mat, _BoxedMaterials) else self.mat.full(p)
 
     def _backend(self):
         if self._be is None:
@@ -205,26 +334,24 @@ class Reconstruction:
             if be is not None:
                 be.close()
         self._be = self._jac_be = None
+        self.mat.close()
 
     # ---------------------------------------------------------------------------- evaluations
     def measure(self, p) -> np.ndarray:
         """k-ratios of every problem and line (problem-major), one batched forward."""
-        I = self._backend().forward(self._inputs(self.material(p)))
+        I = self._backend().forward(self.mat.inputs(p)[1])
         return np.concatenate([v / sd for v, sd in zip(I, self.std)])
 
     def _pullback(self, m, inputs, rb, nb, ab):
-        g = np.zeros(self.shape)
-        for s, (rho, noa, acs), r_, n_, a_ in zip(self.solves, inputs, rb, nb, ab):
-            g += m.grid_pullback(r_)
-            g += m.noa_pullback(n_.reshape(self.shape[:-1] + (self.n_e,)))
-            g += m.absorption_pullback(s.x_rays, s.detector, s.problem.beam_position.mean, acs, a_)[0]
-        return g
+        g = np.zeros(int(np.prod(self.shape)))
+        for i in range(len(self.solves)):
+            g += self.mat.pullback(m, i, inputs[i], rb[i], nb[i], ab[i])
+        return g.reshape(self.shape)
 
     def loss_grad(self, p, k_exp):
         """sum (k - k_exp)^2 and its gradient with respect to the parameters: one batched forward,
         one batched adjoint with I_bar = 2 (k - k_exp) / I_std, the material pullbacks."""
-        m = self.material(p)
-        inputs = self._inputs(m)
+        m, inputs = self.mat.inputs(p)
         be = self._backend()
         I = be.forward(inputs)
         k = np.concatenate([v / sd for v, sd in zip(I, self.std)])
@@ -238,8 +365,7 @@ class Reconstruction:
     def jacobian(self, p):
         """(k, J) with J[i, :] = d k_i / d params: the problems repeated once per line in one batch,
         each copy's adjoint with the unit cotangent of its line (divided by the standard)."""
-        m = self.material(p)
-        inputs = self._inputs(m)
+        m, inputs = self.mat.inputs(p)
         rows = [(i, r) for i, sd in enumerate(self.std) for r in range(len(sd))]
         if self._jac_be is None:
             descs, keep = [], []
@@ -259,11 +385,7 @@ class Reconstruction:
         rb, nb, ab = be.adjoint(ibars)
         J = np.empty((len(rows), int(np.prod(self.shape))))
         for q, (i, r) in enumerate(rows):
-            s = self.solves[i]
-            acs = inputs[i][2]
-            g = m.grid_pullback(rb[q]) + m.noa_pullback(nb[q].reshape(self.shape[:-1] + (self.n_e,)))
-            g = g + m.absorption_pullback(s.x_rays, s.detector, s.problem.beam_position.mean, acs, ab[q])[0]
-            J[q] = g.ravel()
+            J[q] = self.mat.pullback(m, i, inputs[i], rb[q], nb[q], ab[q])
         return k, J
 
     # ----------------------------------------------------------------------------------- fits

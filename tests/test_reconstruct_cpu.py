@@ -4,8 +4,10 @@ tests/test_gpu_reconstruct.py)."""
 import numpy as np
 import pytest
 
+import material_oracle as mo
 from pnepma_gb300 import reconstruct
 from pnepma_gb300.grid import GridSpec
+from pnepma_gb300.material_model import MaterialModel, Slices
 from pnepma_gb300.workloads import UM
 
 GSPEC = GridSpec.make((6, 1, 1), (-0.4 * UM, 0.0), 0.0, 0.0)
@@ -103,5 +105,80 @@ def test_fits_lower_the_loss(oracle, method):
         res = rec.fit_lbfgs(p0, k_exp, maxiter=40)
     else:
         res = rec.fit_gauss_newton(p0, k_exp, iterations=8)
+    assert res.loss <= 1e-3 * f0
+    assert np.all(res.params >= 0.0) and np.all(res.params <= 1.0)
+
+
+# ------------------------------------------------------- a MaterialModel (the reference's fits)
+class OracleMaterialSet:
+    """The material restatement behind the driver's material-set interface (test infrastructure)."""
+
+    def __init__(self, model, solves):
+        self.mms = [model.with_geometry(s.x_rays, s.detector, s.problem.beam_position.mean[0]) for s in solves]
+
+    def fields(self, P):
+        return [mo.fields(mm, P) for mm in self.mms]
+
+    def pullback(self, i, P, rho_bar, noa_bar, acs, acs_bar):
+        return mo.pullback(self.mms[i], P, rho_bar, noa_bar, acs, acs_bar)
+
+    def close(self):
+        pass
+
+
+def bilinear_model(par="bilinear"):
+    """VolumeFractionSC over five knots (Bilinear) or five boxes (Boxed) down to -300 nm, the
+    embedding (pure Cu) below: reconstructions_1d.jl:115-130 on the test grid."""
+    if par == "bilinear":
+        sl = [Slices.range(-0.3 * UM, 0.0, 5), Slices.range(0.0, 0.0, 1), Slices.range(0.0, 0.0, 1)]
+    else:
+        sl = [Slices.range(-0.3 * UM, 0.0, 6), Slices.range(-0.5, 0.5, 2), Slices.range(-0.5, 0.5, 2)]
+    return MaterialModel(GSPEC, ["Cu", "Ni"], "volume_fraction", sc=True, parametrization=par, slices=sl)
+
+
+def make_model(oracle, par="bilinear", **kw):
+    return reconstruct.Reconstruction(3, GSPEC, ["Cu", "Ni"], (10.0, 13.0, 16.0), n_steps=30,
+                                      backend_factory=lambda d, k: OracleBackend(oracle, d, k),
+                                      model=bilinear_model(par), embedding=[1.0],
+                                      material_set_factory=OracleMaterialSet, **kw)
+
+
+def test_model_parameters_exclude_a_fixed_embedding(oracle):
+    rec = make_model(oracle)
+    assert rec.shape == (5,)
+    assert np.array_equal(rec.material(np.zeros(5)), np.r_[np.zeros(5), 1.0])
+
+
+def test_model_k_ratios_of_a_standard_are_one(oracle):
+    rec = make_model(oracle)
+    k = rec.measure(np.ones(rec.shape))      # Cu everywhere (the embedding is Cu too)
+    assert np.allclose(k[0::2], 1.0, rtol=1e-12)
+    assert np.all(np.abs(k[1::2]) < 1e-12)
+
+
+@pytest.mark.parametrize("par", ["bilinear", "boxed"])
+def test_model_gradient_is_consistent_and_matches_finite_differences(oracle, par):
+    rec = make_model(oracle, par)
+    truth_p = np.linspace(0.9, 0.2, rec.shape[0])
+    k_exp = rec.measure(truth_p)
+    p = np.full(rec.shape, 0.5)
+    f, g = rec.loss_grad(p, k_exp)
+    k, J = rec.jacobian(p)
+    r = k - k_exp
+    assert abs(f - r @ r) <= 1e-12 * f
+    assert np.max(np.abs(g - 2.0 * J.T @ r)) <= 1e-10 * np.max(np.abs(g))
+    h = 1e-6
+    fd = np.array([(rec.loss_grad(p + h * e, k_exp)[0] - rec.loss_grad(p - h * e, k_exp)[0]) / (2 * h)
+                   for e in np.eye(p.size)])
+    assert np.linalg.norm(g - fd) <= 2e-2 * np.linalg.norm(fd)
+
+
+def test_model_fit_recovers_the_profile(oracle):
+    rec = make_model(oracle)
+    truth_p = np.array([0.9, 0.8, 0.4, 0.3, 0.2])
+    k_exp = rec.measure(truth_p)
+    p0 = np.full(rec.shape, 0.5)
+    f0 = rec.loss_grad(p0, k_exp)[0]
+    res = rec.fit_gauss_newton(p0, k_exp, iterations=8)
     assert res.loss <= 1e-3 * f0
     assert np.all(res.params >= 0.0) and np.all(res.params <= 1.0)
