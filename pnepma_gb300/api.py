@@ -30,6 +30,7 @@ from .problem import ForwardPNProblem
 
 _CACHE: dict = {}
 _CACHE_MAX = 8
+_DEVICE = "cuda"          # where the GPUMaterial path keeps its buffers
 
 
 def get_handle(problem: ForwardPNProblem, x_rays) -> Handle:
@@ -87,20 +88,25 @@ def _owns_tape(h, token) -> bool:
     return getattr(h, "_api_forward", None) is token
 
 
+def _sync(torch):
+    if _DEVICE != "cpu":
+        torch.cuda.synchronize()
+
+
 def _device_forward(problem, m: GPUMaterial, x_rays, detector_position):
     """Device fields -> pn_forward_device; every call on the legacy default stream, in order."""
     import torch
     h = get_handle(problem, x_rays)
     dm = m.device(x_rays, detector_position, problem.beam_position.mean[0])
     sz = h.sizes
-    f64 = dict(dtype=torch.float64, device="cuda")
-    d = {"P": torch.from_numpy(m.params).to("cuda"), "rho": torch.empty(sz.n_rho, **f64),
+    f64 = dict(dtype=torch.float64, device=_DEVICE)
+    d = {"P": torch.from_numpy(m.params).to(_DEVICE), "rho": torch.empty(sz.n_rho, **f64),
          "noa": torch.empty(sz.n_noa, **f64), "acs": torch.empty(max(sz.n_acs, 1), **f64),
          "I": torch.empty(max(len(x_rays), 1), **f64)}
     dm.fields(d["P"].data_ptr(), d["rho"].data_ptr(), d["noa"].data_ptr(), d["acs"].data_ptr())
     h.forward_device(d["rho"].data_ptr(), d["noa"].data_ptr(), d["acs"].data_ptr(), d["I"].data_ptr())
     d["token"] = _mark(h)
-    torch.cuda.synchronize()
+    _sync(torch)
     I = d["I"].cpu().numpy()[:len(x_rays)].copy()
     return h, dm, d, I
 
@@ -151,10 +157,10 @@ def _device_pullback(problem, m: GPUMaterial, x_rays, detector_position):
     import torch
     h, dm, d, I = _device_forward(problem, m, x_rays, detector_position)
     sz = h.sizes
-    f64 = dict(dtype=torch.float64, device="cuda")
+    f64 = dict(dtype=torch.float64, device=_DEVICE)
 
     def pullback(I_bar):
-        ib = torch.from_numpy(np.ascontiguousarray(I_bar, dtype=np.float64)).to("cuda")
+        ib = torch.from_numpy(np.ascontiguousarray(I_bar, dtype=np.float64)).to(_DEVICE)
         rb, nb = torch.empty(sz.n_rho, **f64), torch.empty(sz.n_noa, **f64)
         ab, G = torch.empty(max(sz.n_acs, 1), **f64), torch.empty(dm.n_params, **f64)
         # the adjoint reads the tape of this call's forward; march it again if another call used
@@ -165,7 +171,7 @@ def _device_pullback(problem, m: GPUMaterial, x_rays, detector_position):
         h.adjoint_device(ib.data_ptr(), rb.data_ptr(), nb.data_ptr(), ab.data_ptr())
         dm.pullback(d["P"].data_ptr(), G.data_ptr(), rb.data_ptr(), nb.data_ptr(),
                     d["acs"].data_ptr() if len(x_rays) else None, ab.data_ptr() if len(x_rays) else None)
-        torch.cuda.synchronize()
+        _sync(torch)
         return G.cpu().numpy()
 
     return I, pullback

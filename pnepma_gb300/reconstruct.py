@@ -91,11 +91,11 @@ class DeviceMaterialSet:
     device: one ``pn_material`` per measurement geometry (lines, detector, beam position), shared by
     the problems that have the same one.  Host arrays in and out, as the batch backend takes them."""
 
-    def __init__(self, model: MaterialModel, solves, device: int = 0):
+    def __init__(self, model: MaterialModel, solves, device=0):
         import torch
         from . import capi
         self.torch = torch
-        self.dev = torch.device("cuda", device)
+        self.dev = torch.device(device) if isinstance(device, str) else torch.device("cuda", device)
         cache, self.mats, self.sizes = {}, [], []
         for s in solves:
             key = (tuple(s.x_rays), tuple(float(v) for v in s.detector), float(s.problem.beam_position.mean[0]))
@@ -113,6 +113,10 @@ class DeviceMaterialSet:
     def _z(self, n):
         return self.torch.zeros(max(int(n), 1), dtype=self.torch.float64, device=self.dev)
 
+    def _sync(self):
+        if self.dev.type == "cuda":
+            self.torch.cuda.synchronize(self.dev)
+
     def fields(self, P):
         """[(rho, noa [cells][n_e], acs [cells][n_r])] per problem."""
         dP = self._dv(P)
@@ -121,7 +125,7 @@ class DeviceMaterialSet:
             rho, noa, acs = self._z(sz.n_rho), self._z(sz.n_noa), self._z(sz.n_acs)
             dm.fields(dP.data_ptr(), rho.data_ptr(), noa.data_ptr(), acs.data_ptr())
             out.append((rho, noa, acs))
-        self.torch.cuda.synchronize(self.dev)
+        self._sync()
         res = []
         for (rho, noa, acs), sz, nr in zip(out, self.sizes, self.nr):
             res.append((rho.cpu().numpy()[:sz.n_rho], noa.cpu().numpy()[:sz.n_noa].reshape(-1, self.ne),
@@ -134,7 +138,7 @@ class DeviceMaterialSet:
         G = self._z(dm.n_params)
         dP, rb, nb, a, ab = (self._dv(x) for x in (P, rho_bar, noa_bar, acs, acs_bar))
         dm.pullback(dP.data_ptr(), G.data_ptr(), rb.data_ptr(), nb.data_ptr(), a.data_ptr(), ab.data_ptr())
-        self.torch.cuda.synchronize(self.dev)
+        self._sync()
         return G.cpu().numpy()[:dm.n_params]
 
     def close(self):

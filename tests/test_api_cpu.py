@@ -94,3 +94,57 @@ def test_gpu_material_reaches_the_device_library():
     assert e.value.code == -9
     with pytest.raises(ValueError):
         api.GPUMaterial(mm, P[:-1])
+
+
+class FakeDeviceHandle:
+    """pn_forward_device / pn_adjoint_device on host memory, the oracle doing the march."""
+
+    def __init__(self, oracle, desc):
+        self.o, self.desc = oracle, desc
+        self.sizes = capi.query_sizes(desc)
+        self.forwards = 0
+
+    @staticmethod
+    def _arr(ptr, n):
+        import ctypes
+        return np.ctypeslib.as_array((ctypes.c_double * n).from_address(ptr))
+
+    def forward_device(self, rho, noa, acs, out, stream=0):
+        z = self.sizes
+        self.inputs = (self._arr(rho, z.n_rho).copy(), self._arr(noa, z.n_noa).copy(), self._arr(acs, z.n_acs).copy())
+        I = self.o.forward(self.desc, *self.inputs)
+        self._arr(out, I.size)[:] = I
+        self.forwards += 1
+
+    def adjoint_device(self, ibar, rho_bar, noa_bar, acs_bar, stream=0):
+        z = self.sizes
+        ib = self._arr(ibar, self.desc.n_xrays).copy()
+        _, rb, nb, ab = self.o.adjoint(self.desc, *self.inputs, ib)
+        for ptr, v in ((rho_bar, rb), (noa_bar, nb), (acs_bar, ab)):
+            self._arr(ptr, v.size)[:] = np.ravel(v)
+
+
+def test_gpu_material_path_on_host_buffers(oracle, monkeypatch):
+    """The GPUMaterial path's buffers, call order and tape ownership, run on host tensors with a
+    fake handle and a fake device material (the oracle and the material restatement doing the
+    arithmetic): the intensities and the gradient equal the restatements used directly."""
+    pytest.importorskip("torch")
+    import material_oracle as mo
+    from test_reconstruct_cpu import FakeDeviceMaterial
+    s = workloads.small_case(dims=1, N=3, shape=(12,), n_steps=4)
+    desc, keep = s.problem.descriptor(s.x_rays)
+    fake = FakeDeviceHandle(oracle, desc)
+    monkeypatch.setattr(api, "_DEVICE", "cpu")
+    monkeypatch.setattr(api, "get_handle", lambda problem, x_rays: fake)
+    monkeypatch.setattr(api, "DeviceMaterial", FakeDeviceMaterial)
+    mm, P = MaterialModel.per_cell_boxed(s.material, s.x_rays, s.detector, beam_x=s.problem.beam_position.mean[0])
+    I, pb = api.calc_intensities_pullback(s.problem, api.GPUMaterial(mm, P), s.x_rays, s.detector)
+    rho, noa, acs = mo.fields(mm, P)
+    assert np.array_equal(I, oracle.forward(desc, rho, noa, acs))
+    api.calc_intensities(s.problem, api.GPUMaterial(mm, 0.9 * P + 0.05), s.x_rays, s.detector)
+    assert fake.forwards == 2
+    ib = np.array([1.0, 0.5]) / np.abs(I)
+    G = pb(ib)
+    assert fake.forwards == 3                 # the pullback marched its own forward again
+    _, rb, nb, ab = oracle.adjoint(desc, rho, noa, acs, ib)
+    assert np.array_equal(G, mo.pullback(mm, P, rb, nb, acs, ab))

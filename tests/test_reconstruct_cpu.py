@@ -182,3 +182,57 @@ def test_model_fit_recovers_the_profile(oracle):
     res = rec.fit_gauss_newton(p0, k_exp, iterations=8)
     assert res.loss <= 1e-3 * f0
     assert np.all(res.params >= 0.0) and np.all(res.params <= 1.0)
+
+
+class FakeDeviceMaterial:
+    """Stands in for capi.DeviceMaterial on host memory: reads and writes the buffers behind the
+    pointers it is given, with the material restatement doing the arithmetic."""
+
+    def __init__(self, mm):
+        self.mm, self.n_params = mm, mm.n_params
+        g = mm.gspec
+        self.n = dict(rho=sum(g.n_cells(c) for c in range(8)) * mm.n_e,
+                      noa=int(np.prod([a.M for a in g.axes])) * mm.n_e,
+                      acs=int(np.prod([a.M for a in g.axes])) * len(mm.x_rays))
+
+    @staticmethod
+    def _arr(ptr, n):
+        import ctypes
+        return np.ctypeslib.as_array((ctypes.c_double * n).from_address(ptr))
+
+    def fields(self, params, rho=None, noa=None, acs=None, stream=0):
+        P = self._arr(params, self.n_params).copy()
+        r, n, a = mo.fields(self.mm, P)
+        for ptr, v in ((rho, r), (noa, n), (acs, a)):
+            if ptr:
+                self._arr(ptr, v.size)[:] = v.ravel()
+
+    def pullback(self, params, params_bar, rho_bar=None, noa_bar=None, acs=None, acs_bar=None, stream=0):
+        P = self._arr(params, self.n_params).copy()
+        G = mo.pullback(self.mm, P, self._arr(rho_bar, self.n["rho"]).copy(), self._arr(noa_bar, self.n["noa"]).copy(),
+                        self._arr(acs, self.n["acs"]).copy(), self._arr(acs_bar, self.n["acs"]).copy())
+        self._arr(params_bar, self.n_params)[:] = G
+
+    def close(self):
+        pass
+
+
+def test_device_material_set_passes_buffers_in_order(oracle, monkeypatch):
+    """DeviceMaterialSet's buffers, sizes, argument order and reshapes, on host tensors with a fake
+    device material: the same fields and gradients as the restatement used directly."""
+    pytest.importorskip("torch")
+    from pnepma_gb300 import capi
+    monkeypatch.setattr(capi, "DeviceMaterial", FakeDeviceMaterial)
+    rec = make_model(oracle)
+    dset = reconstruct.DeviceMaterialSet(bilinear_model(), rec.solves, device="cpu")
+    ref = OracleMaterialSet(bilinear_model(), rec.solves)
+    P = rec.material(np.linspace(0.2, 0.8, 5))
+    got, want = dset.fields(P), ref.fields(P)
+    rng = np.random.default_rng(2)
+    for i, (g, w) in enumerate(zip(got, want)):
+        for a, b in zip(g, w):
+            assert a.shape == np.asarray(b).reshape(a.shape).shape
+            assert np.array_equal(a.ravel(), np.asarray(b).ravel())
+        rb, nb, ab = (rng.normal(size=np.asarray(x).shape) for x in w)
+        assert np.array_equal(dset.pullback(i, P, rb, nb, g[2], ab), ref.pullback(i, P, rb, nb, w[2], ab))
+    dset.close()
