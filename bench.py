@@ -224,6 +224,23 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------------------
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of the ranks' values (the slowest rank sets the step time); x itself when the
+    run is not distributed.  Every rank calls it and gets the same result."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world: int, units_per_rank: int, step_ms: float) -> float:
+    """Units per second of the whole job: every rank processes its own units in the same step
+    (weak scaling), timed by the slowest rank."""
+    return world * units_per_rank / (step_ms / 1e3)
+
+
 def run_ours(args):
     import torch
     from pnepma_gb300 import capi
@@ -313,11 +330,8 @@ def run_ours(args):
             lat.append(prev.elapsed_time(e))
             prev = e
     step_ms = float(np.mean(steps_ms))
-    if dist:
-        t = torch.tensor([step_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * nsol / (step_ms / 1e3)
+    step_ms = max_over_ranks(step_ms, dist, dev)
+    value = whole_job_rate(world, nsol, step_ms)
 
     # ---------------- FP32 batched: all 60 solves in one batch (one launch per sub-step)
     descs32, keep32 = [], []
