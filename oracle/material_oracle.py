@@ -238,7 +238,7 @@ def fields(mm, P):
     noa = np.array([densities(mm, param_value(mm, P, x)) / mm.atom_mass for x in eee])
     nr = len(mm.x_rays)
     acs = np.zeros((len(eee), nr))
-    for ci, o in enumerate(eee):
+    for ci, o in enumerate(eee if nr else []):      # no lines: no absorption factors to form
         d, lam, dx = _ray(mm, o)
         ac = [0.0] * nr
         for k in range(mm.n_int_points):

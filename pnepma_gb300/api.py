@@ -18,7 +18,7 @@ Two kinds of material ``m`` are accepted:
 * a :class:`GPUMaterial` (any model and Const / Boxed / Bilinear parametrisation of
   ``pn_material.jl``): fields, march, adjoint and material pullbacks all run on the device, and
   only the intensities and the parameter gradient (the reference's ``param_vec`` order, embedding
-  last) come back to the host.
+  last) come back to the host; the generation field takes its densities from the device too.
 """
 from __future__ import annotations
 
@@ -180,6 +180,15 @@ def _device_pullback(problem, m: GPUMaterial, x_rays, detector_position):
 def calc_x_ray_generation_field(problem: ForwardPNProblem, m, x_rays) -> np.ndarray:
     h = get_handle(problem, x_rays)
     _mark(h)                 # the handle's densities and state change: pending pullbacks re-march
+    if isinstance(m, GPUMaterial):
+        import torch
+        # the densities only: a material without lines (no absorption factors)
+        dm = m.device((), (0.0, 0.0, 0.0), problem.beam_position.mean[0])
+        P = torch.from_numpy(m.params).to(_DEVICE)
+        rho = torch.empty(h.sizes.n_rho, dtype=torch.float64, device=_DEVICE)
+        dm.fields(P.data_ptr(), rho.data_ptr())
+        _sync(torch)
+        return h.generation_field(rho.cpu().numpy())
     return h.generation_field(m.rho_flat())
 
 

@@ -116,6 +116,9 @@ class FakeDeviceHandle:
         self._arr(out, I.size)[:] = I
         self.forwards += 1
 
+    def generation_field(self, rho):
+        return self.o.generation_field(self.desc, rho)
+
     def adjoint_device(self, ibar, rho_bar, noa_bar, acs_bar, stream=0):
         z = self.sizes
         ib = self._arr(ibar, self.desc.n_xrays).copy()
@@ -148,3 +151,18 @@ def test_gpu_material_path_on_host_buffers(oracle, monkeypatch):
     assert fake.forwards == 3                 # the pullback marched its own forward again
     _, rb, nb, ab = oracle.adjoint(desc, rho, noa, acs, ib)
     assert np.array_equal(G, mo.pullback(mm, P, rb, nb, acs, ab))
+
+
+def test_gpu_material_generation_field_on_host_buffers(oracle, monkeypatch):
+    pytest.importorskip("torch")
+    import material_oracle as mo
+    from test_reconstruct_cpu import FakeDeviceMaterial
+    s = workloads.small_case(dims=1, N=3, shape=(12,), n_steps=4)
+    desc, keep = s.problem.descriptor(s.x_rays)
+    fake = FakeDeviceHandle(oracle, desc)
+    monkeypatch.setattr(api, "_DEVICE", "cpu")
+    monkeypatch.setattr(api, "get_handle", lambda problem, x_rays: fake)
+    monkeypatch.setattr(api, "DeviceMaterial", FakeDeviceMaterial)
+    mm, P = MaterialModel.per_cell_boxed(s.material, s.x_rays, s.detector, beam_x=s.problem.beam_position.mean[0])
+    f = api.calc_x_ray_generation_field(s.problem, api.GPUMaterial(mm, P), s.x_rays)
+    assert np.array_equal(f, oracle.generation_field(desc, mo.fields(mm, P)[0]))
