@@ -7,7 +7,7 @@ absent), so these vectors come from the CPU restatement (oracle/): forward inten
 adjoint outputs of seeded small solves in 1D, 2D and 3D, and the device-material fields and
 pullback of a seeded Bilinear MassFractionSC material.  They pin the oracle against drift
 (tests/test_golden_cpu.py) and give the GPU tests committed vectors to compare with
-(tests/test_gpu_golden.py).  Every input is regenerated from its seed by the case functions below.
+(tests/test_gpu_vs_golden.py).  Every input is regenerated from its seed by the case functions below.
 """
 from __future__ import annotations
 
