@@ -170,3 +170,18 @@ def test_invalid_material_descriptors_are_errors_not_crashes():
     out = ctypes.c_void_p()
     assert L.pn_material_create(ctypes.byref(d), ctypes.byref(out), None) == -1
     assert "increasing" in L.pn_last_error(None).decode()
+
+
+@pytest.mark.parametrize("case", [dict(dims=1, shape=(9,)), dict(dims=2, shape=(7, 5)), dict(dims=3, shape=(5, 4, 3))],
+                         ids=["1d", "2d", "3d"])
+def test_material_fields_have_the_solver_input_sizes(case):
+    """The material's points (all eight class grids, ghosts included) and the solver's buffers
+    (pn_query_sizes) agree for every dimension, so device fields feed pn_forward_device as they are."""
+    from pnepma_gb300 import capi
+    s = workloads.small_case(N=3, n_steps=3, **case)
+    desc, keep = s.problem.descriptor(s.x_rays)
+    sz = capi.query_sizes(desc)
+    mm, P = MaterialModel.per_cell_boxed(s.material, s.x_rays, s.detector, n_int_points=4)
+    rho, noa, acs = mo.fields(mm, P)
+    assert (rho.size, noa.size, acs.size) == (sz.n_rho, sz.n_noa, sz.n_acs)
+    assert mm.coords().size == sum(a.M + (1 if a.M == 1 else a.M + 1) for a in mm.gspec.axes)
