@@ -789,8 +789,9 @@ def material_gradient(s, rho_bar, noa_bar, acs_bar, acs):
 
 
 def run_material(args):
-    """pn_material_fields / pn_material_pullback on config 4's material, timed with CUDA events
-    (inputs resident), beside the host numpy material path on the same inputs."""
+    """pn_material_fields / pn_material_pullback on the material of the 3D 96x96x64 workload (one
+    box per eee cell), timed with CUDA events (inputs resident), beside the host numpy material
+    path on the same inputs."""
     import torch
     from pnepma_gb300 import capi, workloads
     from pnepma_gb300.material_model import MaterialModel
@@ -858,8 +859,8 @@ def run_material(args):
             "rel_err_vs_host": {"rho_eee": rel(rho_d[:n_eee_rho], rho_h[:n_eee_rho]), "noa": rel(noa_d, noa_h.ravel()),
                                 "acs": rel(acs_d, acs_h.ravel()), "gradient": rel(G_d[:-m.n_par], g_h.ravel())}
             if host else None,
-            "config": {"workload": "config 4 material: MassFraction over one box per eee cell, 100 samples per "
-                                   "absorption ray", "params": int(mm.n_params)}}
+            "config": {"workload": "3D 96x96x64 material: MassFraction over one box per eee cell, 100 samples "
+                                   "per absorption ray", "params": int(mm.n_params)}}
     dm.close()
     print(json.dumps(line), flush=True)
 
