@@ -70,10 +70,10 @@ def parse():
                     help="device material fields and pullbacks on the 3D 96x96x64 per-cell boxed material "
                          "(3 elements, 3 lines, 100 samples per ray) against the host numpy path; prints its own line")
     ap.add_argument("--config1", action="store_true",
-                    help="1D slab (config 1): FP64 plain latency, FP32 batch of 256 compositions, gradient vs "
+                    help="1D slab (200 cells, P7): FP64 plain latency, FP32 batch of 256 compositions, gradient vs "
                          "finite differences of the oracle on all 200 cells; prints its own line")
     ap.add_argument("--config3", action="store_true",
-                    help="256 mixed 2D instances (config 3) in one FP32 batch, errors against FP64; prints its own line")
+                    help="256 mixed 2D instances (64x32 to 256x128, P5-P11) in one FP32 batch, errors against FP64; prints its own line")
     return ap.parse_args()
 
 
@@ -965,7 +965,7 @@ def run_config4(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     fwd_ms = float(np.mean(fw))
     line = {
-        "metric": "3D forward+adjoint solve (config 4) with a finite-difference gradient check",
+        "metric": "3D 96x96x64 P7 forward+adjoint solve with a finite-difference gradient check",
         "value": 1e3 / (fwd_ms + float(np.mean(ad))), "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
         "dtype": "f32 state and stencil, f64 accumulators", "data": "synthetic (seeded)",
         "config": {"workload": "3D 96x96 (lateral) x 64 (depth) over 1.5 x 1.5 x 1 um, P7, Fe/Cr/Ni smooth field "
@@ -1114,7 +1114,7 @@ def run_config1(args):
         e_g = max(e_g, _rel(out[1][i], rq))
         hq.close()
     line = {
-        "metric": "1D slab forward+adjoint (config 1)", "value": 1e3 / float(np.median(lat)), "unit": "solves/s",
+        "metric": "1D slab forward+adjoint (200 cells, P7)", "value": 1e3 / float(np.median(lat)), "unit": "solves/s",
         "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "1D 200 cells over 1 um, P7, Cu/Ni in 4 layers (SC mass fractions), 15 keV",
                    "energy_steps": s.problem.N_steps, "configured_energy_steps": 100},
@@ -1176,7 +1176,7 @@ def run_config3(args):
         _b, ma = algorithmic_bytes_per_step(q, 4)
         mcu += 2 * q.problem.N_steps * ma
     line = {
-        "metric": "batched FP32 forward+adjoint solves/s (config 3: 256 mixed 2D instances in one batch)",
+        "metric": "batched FP32 forward+adjoint solves/s (256 mixed 2D instances in one batch)",
         "value": len(solves) / ((fw + ad) / 1e3), "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
         "dtype": "f32 state and stencil, f64 accumulators", "data": "synthetic (seeded)",
         "config": {"workload": "256 instances: grids {64x32, 128x64, 256x128}, N in {5, 7, 11}, 2-4 of Fe/Cr/Ni/Cu, "

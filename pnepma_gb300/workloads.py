@@ -130,7 +130,7 @@ def config1(seed: int = 1, precision=PN_FP64, stabilise=True) -> Solve:
     w[0, 0, :, 0] = cu[layer]
     w[0, 0, :, 1] = 1.0 - cu[layer]
     return make_solve(7, gspec, ["Cu", "Ni"], w, 15.0, beam_sigma=30 * NM, E_init=15.5e3, E_cut=1.0e3,
-                      n_steps=100, sc=True, precision=precision, stabilise=stabilise, label="cfg1")
+                      n_steps=100, sc=True, precision=precision, stabilise=stabilise, label="slab1d")
 
 
 def config2(seed: int = 2, precision=PN_FP64, stabilise=True, n_positions=20, energies=(10.0, 15.0, 20.0),
@@ -147,7 +147,7 @@ def config2(seed: int = 2, precision=PN_FP64, stabilise=True, n_positions=20, en
         for y in ys:
             s = make_solve(11, gspec, ["Fe", "Cr", "Ni"], frac, E, beam_y=float(y), beam_sigma=50 * NM,
                            n_steps=n_steps, detector=(100 * NM, 0.0, 0.0), precision=precision,
-                           stabilise=stabilise, label=f"cfg2 E={E} y={y:.3e}")
+                           stabilise=stabilise, label=f"2d256x128 E={E} y={y:.3e}")
             if mat is None:
                 mat = s.material
             s.material = mat
@@ -175,7 +175,7 @@ def config3(seed: int = 3, n_instances: int = 256, stabilise=True):
         y = float(rng.uniform(-0.5, 0.5) * UM)
         out.append(make_solve(N, gspec, els, frac, E, beam_y=y, beam_sigma=50 * NM, n_steps=n_steps,
                               detector=(100 * NM, 0.0, 0.0), precision=PN_FP32, stabilise=stabilise,
-                              label=f"cfg3[{i}] N={N} {mx}x{my} ne={ne} E={E:.2f}"))
+                              label=f"mixed2d[{i}] N={N} {mx}x{my} ne={ne} E={E:.2f}"))
     return out
 
 
@@ -192,7 +192,7 @@ def config4(seed: int = 4, precision=PN_FP32, stabilise=True, shape=(64, 96, 96)
     frac = smooth_fractions(rng, gspec, 3, inclusion=(centre, 0.2 * UM, amp))
     return make_solve(7, gspec, ["Fe", "Cr", "Ni"], frac, 20.0, beam_sigma=50 * NM, n_steps=n_steps,
                       detector=(100 * NM, 0.0, 0.0), precision=precision, stabilise=stabilise,
-                      checkpoint_stride=checkpoint_stride, label="cfg4")
+                      checkpoint_stride=checkpoint_stride, label="3d96x96x64")
 
 
 def small_case(dims: int = 2, N: int = 3, shape=None, n_steps: int = 12, seed: int = 7, precision=PN_FP64,
@@ -249,7 +249,7 @@ def config5_kind(kind: str, seed: int, precision=PN_FP32, positions: int = 16, e
         for y in ys:
             s = make_solve(N, gspec, els, frac, E, beam_y=float(y), beam_sigma=50 * NM, n_steps=100,
                            detector=(100 * NM, 0.0, 0.0), precision=precision, stabilise=stabilise,
-                           label=f"cfg5 {kind} E={E} y={y:.3e}")
+                           label=f"served {kind} E={E} y={y:.3e}")
             if mat is None:
                 mat = s.material
             s.material = mat          # one material per request: the inputs are shared
