@@ -13,6 +13,7 @@
 
 #include "pn_batch_base.h"
 #include "pn_batch_impl.h"
+#include "pn_trace.h"
 
 namespace pn {
 #define PN_DECL(N) BatchGroupBase* make_batch_group_##N(int precision, int dims);
@@ -203,6 +204,7 @@ int pn_batch_forward(pn_batch* b, const double* const* rho, const double* const*
       b->io[i].acs = acs[i];
       b->io[i].I = intensities[i];
     }
+    pn::TraceRange trace("pn_batch_forward");
     return run_groups(b, (cudaStream_t)stream,
                       [&](pn::BatchGroupBase* g, cudaStream_t s) { return g->forward(b->io.data(), s); });
   } catch (...) {
@@ -221,6 +223,7 @@ int pn_batch_adjoint(pn_batch* b, const double* const* intensities_bar, double* 
       b->io[i].noa_bar = noa_bar[i];
       b->io[i].acs_bar = acs_bar[i];
     }
+    pn::TraceRange trace("pn_batch_adjoint");
     return run_groups(b, (cudaStream_t)stream,
                       [&](pn::BatchGroupBase* g, cudaStream_t s) { return g->adjoint(b->io.data(), s); });
   } catch (...) {

@@ -14,6 +14,7 @@
 #include "pn_layout.h"
 #include "pn_solver_base.h"
 #include "pn_tape_pool.h"
+#include "pn_trace.h"
 
 namespace pn {
 
@@ -159,11 +160,13 @@ int pn_create(const pn_desc* desc, pn_handle** out) {
 
 int pn_forward(pn_handle* h, const double* rho, const double* noa, const double* acs, double* intensities) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
+  pn::TraceRange trace("pn_forward");
   PN_GUARD(h->s->forward(rho, noa, acs, intensities, nullptr, false))
 }
 
 int pn_adjoint(pn_handle* h, const double* intensities_bar, double* rho_bar, double* noa_bar, double* acs_bar) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
+  pn::TraceRange trace("pn_adjoint");
   PN_GUARD(h->s->adjoint(intensities_bar, rho_bar, noa_bar, acs_bar, nullptr, false))
 }
 
@@ -175,17 +178,20 @@ static cudaStream_t caller_stream(void* stream) { return stream ? (cudaStream_t)
 int pn_forward_device(pn_handle* h, const double* rho, const double* noa, const double* acs, double* intensities,
                       void* stream) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
+  pn::TraceRange trace("pn_forward_device");
   PN_GUARD(h->s->forward(rho, noa, acs, intensities, caller_stream(stream), true))
 }
 
 int pn_adjoint_device(pn_handle* h, const double* intensities_bar, double* rho_bar, double* noa_bar,
                       double* acs_bar, void* stream) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
+  pn::TraceRange trace("pn_adjoint_device");
   PN_GUARD(h->s->adjoint(intensities_bar, rho_bar, noa_bar, acs_bar, caller_stream(stream), true))
 }
 
 int pn_generation_field(pn_handle* h, const double* rho, double* field) {
   if (!h || !h->s) return fail("handle is NULL", PN_ERR_INVALID);
+  pn::TraceRange trace("pn_generation_field");
   PN_GUARD(h->s->generation_field(rho, field))
 }
 

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "../../include/pnepma.h"
+#include "pn_trace.h"
 
 namespace pn {
 void set_last_error(const std::string& msg);  // pn_capi.cu
@@ -630,6 +631,7 @@ int pn_material_create(const pn_material_desc* d, pn_material** out, int64_t* n_
 
 int pn_material_fields(pn_material* m, const double* params, double* rho, double* noa, double* acs, void* stream) {
   if (!m || !params) return fail(m, PN_ERR_INVALID, "material handle or params is NULL");
+  pn::TraceRange trace("pn_material_fields");
   const MatDev& g = m->dev;
   cudaStream_t s = (cudaStream_t)stream;
   if (rho || noa) mat_fields_kernel<<<grid_for(g.off[8], MAT_BLOCK), MAT_BLOCK, 0, s>>>(g, params, rho, noa);
@@ -644,6 +646,7 @@ int pn_material_pullback(pn_material* m, const double* params, const double* rho
                          const double* acs, const double* acs_bar, double* params_bar, void* stream) {
   if (!m || !params || !params_bar) return fail(m, PN_ERR_INVALID, "material handle, params or params_bar is NULL");
   if (acs_bar && !acs) return fail(m, PN_ERR_INVALID, "acs_bar needs the forward's acs");
+  pn::TraceRange trace("pn_material_pullback");
   const MatDev& g = m->dev;
   cudaStream_t s = (cudaStream_t)stream;
   if (cudaMemsetAsync(params_bar, 0, sizeof(double) * (size_t)m->n_params, s) != cudaSuccess) {
