@@ -104,9 +104,14 @@ def test_beam_moments_converged():
 # ------------------------------------------------------------------ the two restatements
 CASES = [dict(dims=1, N=5, shape=(16,), n_steps=6), dict(dims=2, N=3, shape=(8, 7), n_steps=5),
          dict(dims=3, N=3, shape=(5, 5, 4), n_steps=3)]
+# the edges of the domain: the highest orders, one element, four elements, 3D at P5
+EDGE_CASES = [dict(dims=2, N=9, shape=(7, 6), n_steps=3), dict(dims=1, N=11, shape=(10,), n_steps=3),
+              dict(dims=2, N=3, shape=(7, 6), n_steps=3, elements=("Fe", "Cr", "Ni", "Cu")),
+              dict(dims=1, N=3, shape=(10,), n_steps=4, elements=("Cu",)),
+              dict(dims=3, N=5, shape=(4, 4, 3), n_steps=2)]
 
 
-@pytest.mark.parametrize("case", CASES, ids=["1d", "2d", "3d"])
+@pytest.mark.parametrize("case", CASES + EDGE_CASES, ids=["1d", "2d", "3d", "2d-N9", "1d-N11", "2d-4el", "1d-1el", "3d-N5"])
 def test_numpy_restatement_matches_c_oracle(oracle, case):
     s = workloads.small_case(**case)
     rho, noa, acs = s.inputs()
