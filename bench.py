@@ -66,6 +66,10 @@ def parse():
                     help="3D 96x96x64 P7 forward+adjoint (FP32 batch, checkpoint stride 16) with a central "
                          "finite-difference check of the mass-fraction gradient on 32 cells; prints its own line")
     ap.add_argument("--fd-cells", type=int, default=32)
+    ap.add_argument("--autotune", action="store_true",
+                    help="measure the batch configurations (kernel family, launch mode, tape schedule) on the FP32 "
+                         "batch of the 60-solve 2D workload, keep the fastest in the autotuner table and print it")
+    ap.add_argument("--autotune-table", default=os.path.join(HERE, "pnepma_gb300", "_build", "autotune.json"))
     ap.add_argument("--material", action="store_true",
                     help="device material fields and pullbacks on the 3D 96x96x64 per-cell boxed material "
                          "(3 elements, 3 lines, 100 samples per ray) against the host numpy path; prints its own line")
@@ -788,6 +792,38 @@ def material_gradient(s, rho_bar, noa_bar, acs_bar, acs):
     return g
 
 
+def run_autotune(args):
+    """The autotuner on the FP32 batch of the 2D workload: every applicable configuration timed
+    (forward + adjoint of the 60 solves, inputs resident), the fastest kept in the table."""
+    import torch
+    from pnepma_gb300 import autotune
+    from pnepma_gb300.problem import PN_FP32, PN_FP64
+    torch.cuda.set_device(0)
+    solves = workload(args.positions)
+    inputs = [solves[0].inputs()] * len(solves)        # one material: the solves share the inputs
+    descs, keep = [], []
+    for s in solves:
+        s.problem.precision = PN_FP32
+        d, k = s.problem.descriptor(s.x_rays)
+        descs.append(d)
+        keep.append(k)
+        s.problem.precision = PN_FP64
+    ibars = [np.ones(len(s.x_rays)) for s in solves]
+    torch.cuda.empty_cache()
+    free_b, _tot = torch.cuda.mem_get_info()
+    os.makedirs(os.path.dirname(args.autotune_table), exist_ok=True)
+    tuner = autotune.Autotuner(args.autotune_table)
+    key = autotune.batch_key(descs)
+    tuner.table.pop(key, None)                          # measure afresh
+    best = tuner.tune(descs, autotune.batch_timer(descs, keep, inputs, ibars, memory_budget=int(0.8 * free_b)))
+    entry = tuner.table[key]
+    line = {"metric": "autotuned FP32 batch: forward+adjoint seconds per configuration (60-solve 2D workload)",
+            "value": entry["seconds"], "unit": "s", "higher_is_better": False, "best": best.label(),
+            "measured": {m["label"]: m["seconds"] for m in entry["measured"]}, "key": key,
+            "table": args.autotune_table}
+    print(json.dumps(line), flush=True)
+
+
 def run_material(args):
     """pn_material_fields / pn_material_pullback on the material of the 3D 96x96x64 workload (one
     box per eee cell), timed with CUDA events (inputs resident), beside the host numpy material
@@ -1208,6 +1244,8 @@ def main():
         run_config4(args)
     elif args.material:
         run_material(args)
+    elif args.autotune:
+        run_autotune(args)
     elif args.config1:
         run_config1(args)
     elif args.config3:
