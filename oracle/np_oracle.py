@@ -1,10 +1,12 @@
-"""Second CPU restatement of the reference march, in vectorised numpy (test infrastructure only).
+"""Second CPU restatement of the reference march and its adjoint, in vectorised numpy (test
+infrastructure only).
 
 Written independently of ``pn_oracle.c``: whole classes are advanced with array slicing and
 ``einsum`` instead of per-cell loops, so a mistake in one restatement does not repeat in the other.
 It follows the same reference code -- ``starmap/src/solver.jl:107-196`` (boundary, sub-steps),
 ``solver_core.jl:7-137`` (stencil, right-hand side, expm1div), ``boundary_conditions.jl:67-102``,
-``pn_problem.jl:205-249`` (coefficients, source), ``pn_intensities.jl:325-351`` (intensities) --
+``pn_problem.jl:205-249`` (coefficients, source), ``pn_intensities.jl:325-351`` (intensities),
+``pn_intensities.jl:129-164,353-413`` and ``x_ray_intensities.jl:155-223`` (the adjoint) --
 and the state layout of the C ABI (per class [z][y][x][moment], classes concatenated).  The
 tests compare the two restatements, including ghost and corner points, on small grids.
 """
@@ -200,7 +202,9 @@ def step(g, u, rho, s, cdeg, bc, dt, adjoint=False, Q=None):
     half(1, dt / 2)
 
 
-def forward(desc, rho_flat, noa, acs, return_state=False):
+def forward(desc, rho_flat, noa, acs, return_state=False, tape=None):
+    """Intensities of the forward march (pn_intensities.jl:325-351); with a list as ``tape``, every
+    state of the march (initial state first) is appended to it."""
     g = Geometry(desc)
     N1 = g.N + 1
     rho = g.split(np.asarray(rho_flat, float), lambda c: g.ne)
@@ -216,6 +220,8 @@ def forward(desc, rho_flat, noa, acs, return_state=False):
     for i in range(g.ns + 1):
         if i > 0:
             step(g, u, rho, fs[i - 1], fc[i - 1], fbc[i - 1], desc.delta_e)
+        if tape is not None:
+            tape.append([x.copy() for x in u])
         integral = W.T @ u[0][..., 0].ravel()
         I = I + desc.delta_e * desc.dvol * sig[i] * integral * w[i]
     if return_state:
@@ -233,3 +239,67 @@ def one_step(desc, rho_flat, state_flat, i):
     fbc = np.ctypeslib.as_array(desc.fwd_bc, shape=(g.ns,))
     step(g, u, rho, fs[i], fc[i], fbc[i], desc.delta_e)
     return np.concatenate([x.ravel() for x in u])
+
+
+def adjoint(desc, rho_flat, noa, acs, Ibar):
+    """(I, rho_bar, noa_bar, acs_bar) of the reference's adjoint (pn_intensities.jl:353-413),
+    written independently of pn_oracle.c.  Iteration j = 0..n_steps takes tape state n_steps - j
+    (the initial state last) and, as the reference's pullback loop does:
+
+    * integrate_adjoint_densities! (pn_intensities.jl:129-164): the forward problem at the tape
+      energy sets the tape state's ghost points (both parities, beam source included), du of every
+      class without the exponential factor, and rho_bar += lambda . (s_e du + c_{e,l} u) dvol dE w;
+    * integrate_step_and_add_pullback! (x_ray_intensities.jl:196-223): the cotangents of the
+      absorption factors and numbers of atoms from the eee cells' first moment;
+    * for j < n_steps, compute_adjoint_source! at E + dE/2 (x_ray_intensities.jl:155-170) and one
+      step of the adjoint problem (its coefficients at E + dE/2, zero boundary source).
+    """
+    from pnepma_gb300.moments import degree_table
+    g = Geometry(desc)
+    N1, ne, nr, ns = g.N + 1, g.ne, g.nr, g.ns
+    dE = desc.delta_e
+    rho = g.split(np.asarray(rho_flat, float), lambda c: ne)
+    tape = []
+    I = forward(desc, rho_flat, noa, acs, tape=tape)
+    arr = lambda p, n: np.ctypeslib.as_array(p, shape=(n,))
+    ais = arr(desc.adj_int_s, (ns + 1) * ne).reshape(ns + 1, ne)
+    aic = arr(desc.adj_int_c, (ns + 1) * ne * N1).reshape(ns + 1, ne, N1)
+    aibc = arr(desc.adj_int_bc, ns + 1)
+    asig = arr(desc.adj_sigma, (ns + 1) * nr).reshape(ns + 1, nr)
+    aw = arr(desc.adj_weight, ns + 1)
+    asrc = arr(desc.adj_src_sigma, max(ns * nr, 1))[:ns * nr].reshape(ns, nr)
+    as_ = arr(desc.adj_s, ns * ne).reshape(ns, ne)
+    ac = arr(desc.adj_c, ns * ne * N1).reshape(ns, ne, N1)
+    xel = arr(desc.xray_element, nr)
+    noa2 = np.asarray(noa, float).reshape(-1, ne)
+    acs2 = np.asarray(acs, float).reshape(-1, nr)
+    Ib = np.asarray(Ibar, float)
+    degs = degree_table(g.N)
+    lam = [np.zeros_like(x) for x in tape[0]]
+    rho_bar = [np.zeros(x.shape[:3] + (ne,)) for x in tape[0]]
+    noa_bar = np.zeros_like(noa2)
+    acs_bar = np.zeros_like(acs2)
+    for j in range(ns + 1):
+        u = [x.copy() for x in tape[ns - j]]
+        apply_boundary(g, u, 0, False, aibc[j])
+        apply_boundary(g, u, 1, False, aibc[j])
+        du = calc_du(g, u, rho, ais[j], aic[j], None, 0, dE, False, False)
+        du.update(calc_du(g, u, rho, ais[j], aic[j], None, 1, dE, False, False))
+        fac = desc.dvol * dE * aw[j]
+        for c, d in du.items():
+            inner = _interior(g, c)
+            lc, uc = lam[c][inner], u[c][inner]
+            P = np.einsum("...m,...m->...", lc, d)                        # sum_m lambda_m du_m
+            R = np.einsum("...m,em->...e", lc * uc, aic[j][:, degs[c]])   # sum_m lambda_m c_{e,l(m)} u_m
+            rho_bar[c][inner] += (P[..., None] * ais[j][None, :] + R) * fac
+        u0 = u[0][..., 0].ravel()
+        w = dE * desc.dvol * asig[j] * aw[j] * Ib                               # [r]
+        acs_bar += noa2[:, xel] * u0[:, None] * w[None, :]
+        for r in range(nr):
+            noa_bar[:, xel[r]] += acs2[:, r] * u0 * w[r]
+        if j == ns:
+            break
+        Q = [np.zeros_like(x) for x in lam]
+        Q[0][..., 0] = -(acs2 * noa2[:, xel] * asrc[j][None, :] * Ib[None, :]).sum(axis=1).reshape(Q[0].shape[:3])
+        step(g, lam, rho, as_[j], ac[j], 0.0, dE, adjoint=True, Q=Q)
+    return I, np.concatenate([x.ravel() for x in rho_bar]), noa_bar, acs_bar

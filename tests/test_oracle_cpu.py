@@ -123,6 +123,21 @@ def test_numpy_restatement_matches_c_oracle(oracle, case):
     assert rel(state_n, tape[-1]) < 1e-12
 
 
+@pytest.mark.parametrize("case", CASES + EDGE_CASES[2:3], ids=["1d", "2d", "3d", "2d-4el"])
+def test_numpy_adjoint_matches_c_oracle(oracle, case):
+    """The adjoint (density integral, intensity pullback, adjoint source and march) restated twice,
+    independently: intensities and all three cotangents agree to rounding."""
+    s = workloads.small_case(**case)
+    rho, noa, acs = s.inputs()
+    desc, keep = s.problem.descriptor(s.x_rays)
+    I = oracle.forward(desc, rho, noa, acs)
+    ib = np.linspace(1.0, 2.0, len(I)) / np.abs(I)
+    c = oracle.adjoint(desc, rho, noa, acs, ib)
+    n = np_oracle.adjoint(desc, rho, noa, acs, ib)
+    for a, b in zip(n, c):
+        assert rel(a, b) < 1e-12
+
+
 @pytest.mark.parametrize("case", CASES, ids=["1d", "2d", "3d"])
 def test_single_step_matches(oracle, case):
     s = workloads.small_case(**case)
