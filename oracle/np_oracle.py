@@ -303,3 +303,20 @@ def adjoint(desc, rho_flat, noa, acs, Ibar):
         Q[0][..., 0] = -(acs2 * noa2[:, xel] * asrc[j][None, :] * Ib[None, :]).sum(axis=1).reshape(Q[0].shape[:3])
         step(g, lam, rho, as_[j], ac[j], 0.0, dE, adjoint=True, Q=Q)
     return I, np.concatenate([x.ravel() for x in rho_bar]), noa_bar, acs_bar
+
+
+def generation_field(desc, rho_flat):
+    """calc_x_ray_generation_field (pn_intensities.jl:189-212 with
+    integrate_step_and_add_x_ray_generation!, x_ray_intensities.jl:226-234): per eee cell and line,
+    the sum over the states of the forward march of u_eee[cell, 0] dE sigma_r(E) w."""
+    g = Geometry(desc)
+    nr, ns = g.nr, g.ns
+    tape = []
+    ncell = g.shape[0][0] * g.shape[0][1] * g.shape[0][2]
+    forward(desc, rho_flat, np.zeros(ncell * g.ne), np.zeros(ncell * max(nr, 1)), tape=tape)
+    sig = np.ctypeslib.as_array(desc.fwd_sigma, shape=((ns + 1) * nr,)).reshape(ns + 1, nr)
+    w = np.ctypeslib.as_array(desc.fwd_weight, shape=(ns + 1,))
+    field = np.zeros((ncell, nr))
+    for i, u in enumerate(tape):
+        field += u[0][..., 0].ravel()[:, None] * (desc.delta_e * sig[i] * w[i])[None, :]
+    return field

@@ -123,7 +123,11 @@ def test_numpy_restatement_matches_c_oracle(oracle, case):
     assert rel(state_n, tape[-1]) < 1e-12
 
 
-@pytest.mark.parametrize("case", CASES + EDGE_CASES[2:3], ids=["1d", "2d", "3d", "2d-4el"])
+ADJOINT_CASES = CASES + EDGE_CASES[2:3] + [dict(dims=2, N=7, shape=(6, 5), n_steps=3),
+                                             dict(dims=1, N=9, shape=(12,), n_steps=3)]
+
+
+@pytest.mark.parametrize("case", ADJOINT_CASES, ids=["1d", "2d", "3d", "2d-4el", "2d-N7", "1d-N9"])
 def test_numpy_adjoint_matches_c_oracle(oracle, case):
     """The adjoint (density integral, intensity pullback, adjoint source and march) restated twice,
     independently: intensities and all three cotangents agree to rounding."""
@@ -136,6 +140,14 @@ def test_numpy_adjoint_matches_c_oracle(oracle, case):
     n = np_oracle.adjoint(desc, rho, noa, acs, ib)
     for a, b in zip(n, c):
         assert rel(a, b) < 1e-12
+
+
+@pytest.mark.parametrize("case", CASES, ids=["1d", "2d", "3d"])
+def test_numpy_generation_field_matches_c_oracle(oracle, case):
+    s = workloads.small_case(**case)
+    rho, noa, acs = s.inputs()
+    desc, keep = s.problem.descriptor(s.x_rays)
+    assert rel(np_oracle.generation_field(desc, rho), oracle.generation_field(desc, rho)) < 1e-12
 
 
 @pytest.mark.parametrize("case", CASES, ids=["1d", "2d", "3d"])
