@@ -185,3 +185,40 @@ def test_material_fields_have_the_solver_input_sizes(case):
     rho, noa, acs = mo.fields(mm, P)
     assert (rho.size, noa.size, acs.size) == (sz.n_rho, sz.n_noa, sz.n_acs)
     assert mm.coords().size == sum(a.M + (1 if a.M == 1 else a.M + 1) for a in mm.gspec.axes)
+
+
+def _device_vector_locate(values, x):
+    """The vector-slice location of pn_material.cu (locate_axis), step for step: a binary search
+    for the first k in [1, n-1] with x <= v[k], then the reference's partition and corrections."""
+    n = len(values)
+    if n == 1:
+        return 1, 0.0
+    lo, hi = 1, n - 1
+    while lo < hi:
+        mid = (lo + hi) >> 1
+        if x <= values[mid]:
+            hi = mid
+        else:
+            lo = mid + 1
+    i = lo
+    d = (x - values[i - 1]) / (values[i] - values[i - 1])
+    if d < 0.0:
+        i -= 1
+    elif d > 1.0:
+        i += 1
+    return i, d
+
+
+def test_binary_search_returns_the_linear_search_index():
+    """The device's binary search and the reference's linear search agree on every point: random
+    points, points exactly on slices, and points outside on either side."""
+    rng = np.random.default_rng(8)
+    for n in (2, 3, 5, 17):
+        for _ in range(20):
+            v = np.sort(rng.uniform(-1.0, 1.0, n))
+            if np.any(np.diff(v) <= 0):
+                continue
+            sl = Slices.vector(v)
+            xs = np.concatenate([rng.uniform(-1.5, 1.5, 30), v, [v[0] - 1.0, v[-1] + 1.0]])
+            for x in xs:
+                assert _device_vector_locate(v, float(x)) == mo.locate(sl, float(x)), (v, x)
