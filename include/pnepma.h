@@ -3,8 +3,9 @@
  * its adjoint gradient).
  *
  * The reference exposes this path as Julia methods with no foreign-function layer; the entry
- * points below are what a Julia shim binds with ccall to replace them (the binding is shown in
- * INTEGRATION.md):
+ * points below are what a Julia shim binds with ccall to replace the methods at these places in
+ * the reference (the callers, scripts/reconstructions_1d.jl:154, scripts/sensitivities_1d.jl:126-127
+ * and scripts/2d_full_reconstruction_test.jl:138-147, reach them through Zygote):
  *
  *   pn_create            <- ForwardPNProblem{N,T}(...) / AdjointPNProblem(frwd)
  *                           pn_solver/pn_problem.jl:72-136 (matrices, boundary source, tables)
@@ -198,8 +199,11 @@ int pn_get_state(pn_handle* h, double* state);
    not fit are rejected with PN_ERR_NO_MEMORY (message from pn_last_error(NULL)).  The first call
    on a device looks up the array's device address (cudaGetSymbolAddress) and should come before
    any stream capture.  All calls share the array: calls whose work overlaps on the GPU race and
-   must be serialised by the caller.  The descriptor's host tables may be reused once the call
-   returns. */
+   must be serialised by the caller.  The descriptor is checked as pn_create checks it (same
+   errors, PN_FLAG_CHECK_CFL and PN_FLAG_CHECK_FINITE honoured; the latter synchronises `stream`).
+   The descriptor's host tables are read by asynchronous host-to-device copies on `stream`:
+   pageable tables may be reused once the call returns, page-locked (pinned or registered) tables
+   must stay unchanged until `stream` has reached this call's work. */
 #define PN_NOALLOC_SCRATCH_BYTES (64u << 20)
 int pn_forward_noalloc(const pn_desc* desc, const double* rho, const double* noa, const double* acs,
                        double* intensities, void* stream);

@@ -30,8 +30,21 @@ def lib():
         L.ora_generation_field.argtypes = [P, P, P]
         L.ora_step.argtypes = [P, P, P, ctypes.c_int]
         L.ora_solve_many.argtypes = [P] * 9 + [ctypes.c_int, ctypes.c_int]
+        L.ora_set_threads.argtypes = [ctypes.c_int]
+        L.ora_set_threads.restype = ctypes.c_int
+        L.ora_openmp.restype = ctypes.c_int
         _lib = L
     return _lib
+
+
+def set_threads(n: int) -> int:
+    """Host threads of each following solve; returns the count in effect (1 without OpenMP)."""
+    return int(lib().ora_set_threads(int(n)))
+
+
+def threads_available() -> int:
+    """Threads a solve can use: the host's cores when the oracle was built with OpenMP, else 1."""
+    return (os.cpu_count() or 1) if lib().ora_openmp() else 1
 
 
 def _p(a):

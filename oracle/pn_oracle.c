@@ -29,6 +29,35 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Host threads per solve.  The loops over the points of a class are split across threads when
+   the file is built with OpenMP; each point's arithmetic, and every sum over points (intensities),
+   keeps the serial evaluation order, so the results do not depend on the thread count.  The
+   workers of ora_solve_many run one solve each and force one thread. */
+static int g_threads = 1;
+static __thread int tl_serial = 0;
+
+int ora_openmp(void) {
+#ifdef _OPENMP
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+int ora_set_threads(int n) {
+#ifdef _OPENMP
+  if (n < 1) n = 1;
+  g_threads = n;
+#else
+  (void)n;
+  g_threads = 1;
+#endif
+  return g_threads;
+}
 
 /* ------------------------------------------------------------------------------------------ */
 /* problem geometry and moments                                                               */
@@ -62,6 +91,7 @@ typedef struct {
 
 typedef struct {
   const pn_desc* d;
+  int threads;            /* host threads for the loops over points */
   int N, ne, nr, ns;
   int nm[8];              /* moments per class */
   int deg[8][ORA_MAXM];   /* degree of each moment */
@@ -105,6 +135,7 @@ static int csc_from_dense(csc_t* a, const double* D, int nrow, int ncol, double 
 static int ora_init(ora_t* o, const pn_desc* d) {
   memset(o, 0, sizeof(*o));
   o->d = d;
+  o->threads = tl_serial ? 1 : g_threads;
   o->N = d->order;
   o->ne = d->n_elements;
   o->nr = d->n_xrays;
@@ -215,6 +246,7 @@ static void update_problem(const ora_t* o, prob_t* p, const double* rho, const d
   /* weighted_sum!: S[i] .= 0; for e: S[i] .+= rho[i][e] .* s[e] */
   for (int cl = 0; cl < 8; ++cl) {
     int nm = o->nm[cl];
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
     for (int64_t q = 0; q < o->npts[cl]; ++q) {
       const double* r = rho + o->off_rho[cl] + q * o->ne;
       double* S = p->S + o->off_state[cl] + q * nm;
@@ -248,47 +280,55 @@ static void apply_bc_class(const ora_t* o, const prob_t* p, double* st, int cl, 
   double* U = st + o->off_state[cl];
   const double* V = st + o->off_state[vc];
   const int nx = o->shape[cl][0], ny = o->shape[cl][1], nz = o->shape[cl][2];
-  double tmp[ORA_MAXM];
+  const int sh[3] = {nx, ny, nz};
+  /* the two axes across the face, in x, y, z order; a face point f is (f % sh[a], f / sh[a]) */
+  const int a = dim == 0 ? 1 : 0, b = dim == 2 ? 1 : 2;
+  const int64_t nf = (int64_t)sh[a] * sh[b];
   /* left face: index 0 along dim, every point across */
-  int lo[3] = {0, 0, 0}, hi[3] = {nx, ny, nz};
-  hi[dim] = 1;
-  for (int k = lo[2]; k < hi[2]; ++k)
-    for (int j = lo[1]; j < hi[1]; ++j)
-      for (int i = lo[0]; i < hi[0]; ++i) {
-        int64_t q = pidx(o, cl, i, j, k);
-        int64_t qv = pidx(o, vc, i, j, k);
-        int rr[3] = {i, j, k};
-        rr[dim] += 1;
-        int64_t qr = pidx(o, cl, rr[0], rr[1], rr[2]);
-        matvec(B, nu, nv, V + qv * nv, tmp);
-        for (int m = 0; m < nu; ++m) {
-          double g = 0.0; /* left source g[1,:,:] is zero (only gx_temp[2,...] is set) */
-          if (source) U[q * nu + m] = 2.0 * (-tmp[m] + g) - U[qr * nu + m];
-          else U[q * nu + m] = -2.0 * tmp[m] - U[qr * nu + m];
-        }
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
+  for (int64_t f = 0; f < nf; ++f) {
+    double tmp[ORA_MAXM];
+    int ii[3];
+    ii[dim] = 0;
+    ii[a] = (int)(f % sh[a]);
+    ii[b] = (int)(f / sh[a]);
+    int64_t q = pidx(o, cl, ii[0], ii[1], ii[2]);
+    int64_t qv = pidx(o, vc, ii[0], ii[1], ii[2]);
+    int rr[3] = {ii[0], ii[1], ii[2]};
+    rr[dim] += 1;
+    int64_t qr = pidx(o, cl, rr[0], rr[1], rr[2]);
+    matvec(B, nu, nv, V + qv * nv, tmp);
+    for (int m = 0; m < nu; ++m) {
+      double g = 0.0; /* left source g[1,:,:] is zero (only gx_temp[2,...] is set) */
+      if (source) U[q * nu + m] = 2.0 * (-tmp[m] + g) - U[qr * nu + m];
+      else U[q * nu + m] = -2.0 * tmp[m] - U[qr * nu + m];
+    }
+  }
+  /* right face: last index along dim */
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
+  for (int64_t f = 0; f < nf; ++f) {
+    double tmp[ORA_MAXM];
+    int ii[3];
+    ii[dim] = sh[dim] - 1;
+    ii[a] = (int)(f % sh[a]);
+    ii[b] = (int)(f / sh[a]);
+    const int i = ii[0], j = ii[1], k = ii[2];
+    int64_t q = pidx(o, cl, i, j, k);
+    int ll[3] = {i, j, k};
+    ll[dim] -= 1;
+    int64_t qv = pidx(o, vc, ll[0], ll[1], ll[2]);
+    int64_t ql = pidx(o, cl, ll[0], ll[1], ll[2]);
+    matvec(B, nu, nv, V + qv * nv, tmp);
+    for (int m = 0; m < nu; ++m) {
+      if (source) {
+        /* g[2, j, k] = gx_temp[2, j, k] * bc ; dim == 0 so (j, k) index the face */
+        double g = o->gx[cl][((int64_t)k * ny + j) * nu + m] * p->bc;
+        U[q * nu + m] = 2.0 * (tmp[m] + g) - U[ql * nu + m];
+      } else {
+        U[q * nu + m] = 2.0 * tmp[m] - U[ql * nu + m];
       }
-  /* right face */
-  lo[dim] = (dim == 0 ? nx : dim == 1 ? ny : nz) - 1;
-  hi[0] = nx; hi[1] = ny; hi[2] = nz;
-  for (int k = lo[2]; k < hi[2]; ++k)
-    for (int j = lo[1]; j < hi[1]; ++j)
-      for (int i = lo[0]; i < hi[0]; ++i) {
-        int64_t q = pidx(o, cl, i, j, k);
-        int ll[3] = {i, j, k};
-        ll[dim] -= 1;
-        int64_t qv = pidx(o, vc, ll[0], ll[1], ll[2]);
-        int64_t ql = pidx(o, cl, ll[0], ll[1], ll[2]);
-        matvec(B, nu, nv, V + qv * nv, tmp);
-        for (int m = 0; m < nu; ++m) {
-          if (source) {
-            /* g[2, j, k] = gx_temp[2, j, k] * bc ; dim == 0 so (j, k) index the face */
-            double g = o->gx[cl][((int64_t)k * ny + j) * nu + m] * p->bc;
-            U[q * nu + m] = 2.0 * (tmp[m] + g) - U[ql * nu + m];
-          } else {
-            U[q * nu + m] = 2.0 * tmp[m] - U[ql * nu + m];
-          }
-        }
-      }
+    }
+  }
 }
 
 static void apply_boundary(const ora_t* o, const prob_t* p, double* st, int parity) {
@@ -322,6 +362,7 @@ static void kernel_class(const ora_t* o, const prob_t* p, double* du, const doub
     else { lo[dd] = 0; hi[dd] = n[dd]; }                   /* 1:n   */
   }
   const double adv_sign = p->adjoint ? -1.0 : 1.0;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(o->threads) if (o->threads > 1)
   for (int k = lo[2]; k < hi[2]; ++k)
     for (int j = lo[1]; j < hi[1]; ++j)
       for (int i = lo[0]; i < hi[0]; ++i) {
@@ -376,6 +417,7 @@ static void update(const ora_t* o, double* st, const double* du, int parity, dou
     int64_t n = o->npts[cl] * o->nm[cl];
     double* U = st + o->off_state[cl];
     const double* D = du + o->off_state[cl];
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
     for (int64_t q = 0; q < n; ++q) U[q] = U[q] + dt * D[q];
   }
 }
@@ -411,6 +453,17 @@ static void integrate_step_and_add(const ora_t* o, double* I, const double* st, 
   for (int r = 0; r < o->nr; ++r) I[r] = I[r] + dE * dvol * sigma[r] * integral[r] * weight;
 }
 
+/* dst = src over n doubles, split across the solve's threads */
+static void copy_state(const ora_t* o, double* dst, const double* src, int64_t n) {
+  const int64_t chunk = 1 << 16;
+  const int64_t nchunk = (n + chunk - 1) / chunk;
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
+  for (int64_t c = 0; c < nchunk; ++c) {
+    int64_t a = c * chunk, len = n - a < chunk ? n - a : chunk;
+    memcpy(dst + a, src + a, sizeof(double) * (size_t)len);
+  }
+}
+
 static int alloc_prob(const ora_t* o, prob_t* p, int adjoint, int with_Q) {
   memset(p, 0, sizeof(*p));
   p->adjoint = adjoint;
@@ -432,12 +485,12 @@ int ora_forward(const pn_desc* d, const double* rho, const double* noa, const do
   if (alloc_prob(&o, &p, 0, 0) || !st || !du) { free(st); free(du); free_prob(&p); ora_free(&o); return -3; }
   const int N1 = o.N + 1;
   for (int r = 0; r < o.nr; ++r) intensities[r] = 0.0;
-  if (tape) memcpy(tape, st, sizeof(double) * (size_t)o.n_state);
+  if (tape) copy_state(&o, tape, st, o.n_state);
   integrate_step_and_add(&o, intensities, st, noa, acs, d->fwd_sigma, d->fwd_weight[0]);
   for (int i = 0; i < o.ns; ++i) {
     update_problem(&o, &p, rho, d->fwd_s + (int64_t)i * o.ne, d->fwd_c + (int64_t)i * o.ne * N1, d->fwd_bc[i]);
     step_pde(&o, &p, st, du, d->delta_e);
-    if (tape) memcpy(tape + (int64_t)(i + 1) * o.n_state, st, sizeof(double) * (size_t)o.n_state);
+    if (tape) copy_state(&o, tape + (int64_t)(i + 1) * o.n_state, st, o.n_state);
     integrate_step_and_add(&o, intensities, st, noa, acs, d->fwd_sigma + (int64_t)(i + 1) * o.nr,
                            d->fwd_weight[i + 1]);
   }
@@ -463,6 +516,7 @@ int ora_generation_field(const pn_desc* d, const double* rho, double* field) {
       step_pde(&o, &p, st, du, d->delta_e);
     }
     const double* sg = d->fwd_sigma + (int64_t)i * o.nr;
+#pragma omp parallel for schedule(static) num_threads(o.threads) if (o.threads > 1)
     for (int64_t c = 0; c < ncell; ++c)
       for (int r = 0; r < o.nr; ++r)
         field[c * o.nr + r] = field[c * o.nr + r] + st[o.off_state[0] + c * nm] * d->delta_e * sg[r] * d->fwd_weight[i];
@@ -503,6 +557,7 @@ static void integrate_adjoint_densities(const ora_t* o, prob_t* pf, const double
       if (bit(cl, dd)) { lo[dd] = 1; hi[dd] = n[dd] - 1; }
       else { lo[dd] = 0; hi[dd] = n[dd]; }
     }
+#pragma omp parallel for collapse(3) schedule(static) num_threads(o->threads) if (o->threads > 1)
     for (int i = lo[0]; i < hi[0]; ++i)
       for (int j = lo[1]; j < hi[1]; ++j)
         for (int k = lo[2]; k < hi[2]; ++k) {
@@ -526,6 +581,7 @@ static void integrate_step_and_add_pullback(const ora_t* o, const double* u, con
   for (int r = 0; r < o->nr; ++r) integral_[r] = 0.0 + dE * dvol * sigma[r] * weight * Ibar[r];
   const int64_t ncell = o->npts[0];
   const int nm = o->nm[0];
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
   for (int64_t i = 0; i < ncell; ++i)
     for (int r = 0; r < o->nr; ++r) {
       int el = o->d->xray_element[r];
@@ -539,6 +595,7 @@ static void compute_adjoint_source(const ora_t* o, double* Q, const double* Ibar
                                    const double* acs, const double* sigma) {
   const int64_t ncell = o->npts[0];
   const int nm = o->nm[0];
+#pragma omp parallel for schedule(static) num_threads(o->threads) if (o->threads > 1)
   for (int64_t i = 0; i < ncell; ++i) {
     double* Qi = Q + o->off_state[0] + i * nm;
     Qi[0] = 0.0;
@@ -620,6 +677,7 @@ typedef struct {
 
 static void* many_worker(void* arg) {
   many_t* w = (many_t*)arg;
+  tl_serial = 1;
   for (;;) {
     pthread_mutex_lock(&w->mu);
     int i = w->next++;

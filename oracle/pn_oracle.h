@@ -18,6 +18,10 @@
 extern "C" {
 #endif
 
+/* 1 when built with OpenMP; ora_set_threads sets the host threads of one solve (returns the
+   count in effect: 1 without OpenMP) */
+int ora_openmp(void);
+int ora_set_threads(int n);
 int64_t ora_state_size(const pn_desc* d);
 int64_t ora_rho_size(const pn_desc* d);
 /* calc_intensities; tape (optional) receives the n_steps + 1 states */

@@ -41,34 +41,13 @@ int noalloc_forward(const pn_desc* d, unsigned char* scratch, size_t cap, const 
   int rc = L.init(d, err);
   if (rc) return rc;
   if (d->precision != PN_FP64) { err = "the no-allocation entry point runs the FP64 path only"; return PN_ERR_UNSUPPORTED; }
-  if (L.ne > MAXE || L.nr > MAXR || L.nr < 1) { err = "1..8 x-ray lines and at most 4 elements are supported"; return PN_ERR_UNSUPPORTED; }
+  if (L.nr < 1) { err = "the no-allocation entry point needs at least one x-ray line"; return PN_ERR_UNSUPPORTED; }
   if (!rho || !noa || !acs || !intensities) { err = "NULL buffer"; return PN_ERR_INVALID; }
-  if (!d->advection || !d->boundary_fwd || !d->beam_face || !d->fwd_s || !d->fwd_c || !d->fwd_bc ||
-      !d->fwd_sigma || !d->fwd_weight || !d->xray_element) {
-    err = "descriptor has a NULL forward table";
-    return PN_ERR_INVALID;
-  }
+  if ((rc = validate_desc(d, L, false, err))) return rc;
   const int ns = L.ns, ne = L.ne, nr = L.nr, N1 = N + 1;
-  for (int r = 0; r < nr; ++r)
-    if (d->xray_element[r] < 0 || d->xray_element[r] >= ne) { err = "xray_element out of range"; return PN_ERR_INVALID; }
-
-  // advection table (compiled sparsity, values / h)
+  // advection table (compiled sparsity, values / h), checked as the handle path checks it
   double tab[Ord<N>::n_tab > 0 ? Ord<N>::n_tab : 1];
-  {
-    const double* pa = d->advection;
-    for (int k = 0; k < 3; ++k)
-      for (int c = 0; c < 8; ++c) {
-        const int ncol = L.nm[class_switch(c, k)];
-        const int off = Ord<N>::off(c, k);
-        const int endk = (c == 7 && k == 2) ? Ord<N>::n_tab : (k < 2 ? Ord<N>::off(c, k + 1) : Ord<N>::off(c + 1, 0));
-        for (int kk = off; kk < endk; ++kk) {
-          const double v = pa[(long long)Ord<N>::rc[kk][0] * ncol + Ord<N>::rc[kk][1]];
-          if (v == 0.0) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
-          tab[kk] = v / d->h[k];
-        }
-        pa += (long long)L.nm[c] * ncol;
-      }
-  }
+  if ((rc = advection_table<N>(d, L, tab, err))) return rc;
 
   std::lock_guard<std::mutex> lock(noalloc_face_mutex());
   int* faces_h = noalloc_face_buffer();
@@ -242,6 +221,13 @@ int noalloc_forward(const pn_desc* d, unsigned char* scratch, size_t cap, const 
   PN_CUDA(cudaGetLastError());
   final_intensity_kernel<<<1, 32, 0, s>>>(integral, sigma, weight, intensities, ns + 1, nr, d->delta_e, d->dvol, 1.0);
   PN_CUDA(cudaGetLastError());
+  if (d->flags & PN_FLAG_CHECK_FINITE) {
+    double hI[MAXR];
+    PN_CUDA(cudaStreamSynchronize(s));
+    PN_CUDA(cudaMemcpy(hI, intensities, sizeof(double) * (size_t)nr, cudaMemcpyDeviceToHost));
+    for (int r = 0; r < nr; ++r)
+      if (!std::isfinite(hI[r])) { err = "intensities are not finite: the march diverged"; return PN_ERR_DIVERGED; }
+  }
   // the face staging buffer was copied by a pageable-memory copy, which has completed on return
   return PN_OK;
 }

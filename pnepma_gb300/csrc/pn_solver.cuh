@@ -53,6 +53,77 @@ inline int grid_for(long long n) {
   return (int)b;
 }
 
+// Descriptor checks shared by the handle path (pn_create) and the no-allocation forward
+// (pn_forward_noalloc), so that both accept and reject the same descriptors: table limits, the
+// grid limits of the cell packing (pack_cell keeps 11 bits of x and y and 10 of z), presence of
+// the forward tables (and of the adjoint tables when `adjoint`), a positive energy step and cell
+// volume, PN_FLAG_CHECK_CFL, the line-to-element map and positive, finite stopping powers.
+inline int validate_desc(const pn_desc* d, const Layout& L, bool adjoint, std::string& err) {
+  if (L.ne > MAXE) { err = "at most " + std::to_string(MAXE) + " elements per solve are supported"; return PN_ERR_UNSUPPORTED; }
+  if (L.nr > MAXR) { err = "at most " + std::to_string(MAXR) + " x-ray lines per solve are supported"; return PN_ERR_UNSUPPORTED; }
+  for (int k = 0; k < 3; ++k)
+    if (L.M[k] > 2000 || (k == 2 && L.M[k] > 1000)) { err = "grid too large for the cell packing"; return PN_ERR_UNSUPPORTED; }
+  if (!d->advection || !d->boundary_fwd || !d->beam_face || !d->fwd_s || !d->fwd_c || !d->fwd_bc || !d->fwd_sigma ||
+      !d->fwd_weight || (L.nr > 0 && !d->xray_element)) {
+    err = "descriptor has a NULL table";
+    return PN_ERR_INVALID;
+  }
+  if (adjoint && (!d->boundary_adj || !d->adj_int_s || !d->adj_int_c || !d->adj_int_bc || !d->adj_sigma ||
+                  !d->adj_weight || !d->adj_src_sigma || !d->adj_s || !d->adj_c)) {
+    err = "descriptor has a NULL table";
+    return PN_ERR_INVALID;
+  }
+  if (!(d->delta_e > 0.0) || !(d->dvol > 0.0)) { err = "delta_e and dvol must be positive"; return PN_ERR_INVALID; }
+  if ((d->flags & PN_FLAG_CHECK_CFL) && d->delta_e > d->cfl_limit) {
+    err = "energy step " + std::to_string(d->delta_e) + " exceeds cfl_limit " + std::to_string(d->cfl_limit);
+    return PN_ERR_CFL;
+  }
+  for (int r = 0; r < L.nr; ++r)
+    if (d->xray_element[r] < 0 || d->xray_element[r] >= L.ne) { err = "xray_element out of range"; return PN_ERR_INVALID; }
+  const long long ns = L.ns, ne = L.ne;
+  auto positive = [](double v) { return v > 0.0 && std::isfinite(v); };
+  for (long long q = 0; q < ns * ne; ++q)
+    if (!positive(d->fwd_s[q])) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
+  if (adjoint) {
+    for (long long q = 0; q < (ns + 1) * ne; ++q)
+      if (!positive(d->adj_int_s[q])) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
+    for (long long q = 0; q < ns * ne; ++q)
+      if (!(d->adj_s[q] > 0.0)) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
+  }
+  return PN_OK;
+}
+
+// Advection values at the compiled stencil positions, divided by the grid step (tab[Ord<N>::n_tab]).
+// Rejects blocks whose nonzero pattern differs from the compiled one: a zero at a stencil position
+// or a nonzero outside it.
+template <int N>
+int advection_table(const pn_desc* d, const Layout& L, double* tab, std::string& err) {
+  const double* pa = d->advection;
+  int t = 0;
+  std::vector<char> used;
+  for (int k = 0; k < 3; ++k)
+    for (int c = 0; c < 8; ++c) {
+      const int nrow = L.nm[c], ncol = L.nm[class_switch(c, k)];
+      const int off = Ord<N>::off(c, k);
+      // blocks are laid out class-major, axis-minor; this block ends where the next one starts
+      const int endk = (c == 7 && k == 2) ? Ord<N>::n_tab : (k < 2 ? Ord<N>::off(c, k + 1) : Ord<N>::off(c + 1, 0));
+      used.assign((size_t)nrow * ncol + 1, 0);
+      for (int kk = off; kk < endk; ++kk) {
+        const int row = Ord<N>::rc[kk][0], col = Ord<N>::rc[kk][1];
+        const double v = pa[(long long)row * ncol + col];
+        if (v == 0.0) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
+        tab[kk] = v / d->h[k];
+        used[(size_t)row * ncol + col] = 1;
+        ++t;
+      }
+      for (int q = 0; q < nrow * ncol; ++q)
+        if (!used[q] && pa[q] != 0.0) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
+      pa += (long long)nrow * ncol;
+    }
+  if (t != Ord<N>::n_tab) { err = "internal: advection table size"; return PN_ERR_INVALID; }
+  return PN_OK;
+}
+
 template <class T, int N>
 class Solver : public SolverBase {
  public:
@@ -249,23 +320,8 @@ class Solver : public SolverBase {
     int rc = L.init(d, err);
     if (rc) return rc;
     if (L.N != N) { err = "internal: order mismatch"; return PN_ERR_INVALID; }
-    if (L.ne > MAXE) { err = "at most " + std::to_string(MAXE) + " elements per solve are supported"; return PN_ERR_UNSUPPORTED; }
-    if (L.nr > MAXR) { err = "at most " + std::to_string(MAXR) + " x-ray lines per solve are supported"; return PN_ERR_UNSUPPORTED; }
-    for (int k = 0; k < 3; ++k)
-      if (L.M[k] > 2000 || (k == 2 && L.M[k] > 1000)) { err = "grid too large for the cell packing"; return PN_ERR_UNSUPPORTED; }
-    if (!d->advection || !d->boundary_fwd || !d->boundary_adj || !d->beam_face || !d->fwd_s || !d->fwd_c ||
-        !d->fwd_bc || !d->fwd_sigma || !d->fwd_weight || !d->adj_int_s || !d->adj_int_c || !d->adj_int_bc ||
-        !d->adj_sigma || !d->adj_weight || !d->adj_src_sigma || !d->adj_s || !d->adj_c ||
-        (L.nr > 0 && !d->xray_element)) {
-      err = "descriptor has a NULL table";
-      return PN_ERR_INVALID;
-    }
-    if (!(d->delta_e > 0.0) || !(d->dvol > 0.0)) { err = "delta_e and dvol must be positive"; return PN_ERR_INVALID; }
+    if ((rc = validate_desc(d, L, true, err))) return rc;
     flags = d->flags;
-    if ((flags & PN_FLAG_CHECK_CFL) && d->delta_e > d->cfl_limit) {
-      err = "energy step " + std::to_string(d->delta_e) + " exceeds cfl_limit " + std::to_string(d->cfl_limit);
-      return PN_ERR_CFL;
-    }
     dE = d->delta_e;
     dvol = d->dvol;
     for (int k = 0; k < 3; ++k) h[k] = d->h[k];
@@ -285,43 +341,8 @@ class Solver : public SolverBase {
     adj_s = cp(d->adj_s, (long long)(ns + 1) * ne);
     adj_c = cp(d->adj_c, (long long)(ns + 1) * ne * N1);
     xel.assign(d->xray_element, d->xray_element + nr);
-    for (int r = 0; r < nr; ++r)
-      if (xel[r] < 0 || xel[r] >= ne) { err = "xray_element out of range"; return PN_ERR_INVALID; }
-    for (double v : fwd_s)
-      if (!(v > 0.0) || !std::isfinite(v)) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
-    for (double v : adj_int_s)
-      if (!(v > 0.0) || !std::isfinite(v)) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
-    for (int j = 0; j < ns; ++j)
-      for (int e = 0; e < ne; ++e)
-        if (!(adj_s[(long long)j * ne + e] > 0.0)) { err = "stopping power must be positive and finite"; return PN_ERR_INVALID; }
     beam_face_h = cp(d->beam_face, L.n_beam);
-
-    // advection table: compiled sparsity, values divided by the grid step
-    {
-      const double* pa = d->advection;
-      int t = 0;
-      for (int k = 0; k < 3; ++k)
-        for (int c = 0; c < 8; ++c) {
-          const int nrow = L.nm[c], ncol = L.nm[class_switch(c, k)];
-          const int off = Ord<N>::off(c, k);
-          // blocks are laid out class-major, axis-minor; this block ends where the next one starts
-          const int endk = (c == 7 && k == 2) ? Ord<N>::n_tab : (k < 2 ? Ord<N>::off(c, k + 1) : Ord<N>::off(c + 1, 0));
-          std::vector<char> used((size_t)nrow * ncol + 1, 0);
-          int kk = off;
-          for (; kk < endk; ++kk) {
-            const int row = Ord<N>::rc[kk][0], col = Ord<N>::rc[kk][1];
-            const double v = pa[(long long)row * ncol + col];
-            if (v == 0.0) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
-            tab_h[kk] = v / h[k];
-            used[(size_t)row * ncol + col] = 1;
-            ++t;
-          }
-          for (int q = 0; q < nrow * ncol; ++q)
-            if (!used[q] && pa[q] != 0.0) { err = "advection block sparsity differs from the compiled stencil"; return PN_ERR_INVALID; }
-          pa += (long long)nrow * ncol;
-        }
-      if (t != Ord<N>::n_tab) { err = "internal: advection table size"; return PN_ERR_INVALID; }
-    }
+    if ((rc = advection_table<N>(d, L, tab_h, err))) return rc;
 
     // checkpoint stride
     const long long slot_bytes = L.slot_elems * (long long)sizeof(T);

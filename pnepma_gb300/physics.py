@@ -4,7 +4,7 @@ The reference takes these quantities from third-party packages or from a file th
 its tree:
 
 * mass stopping power s_e(E) and its slope -- ICRU-77 tables, linearly interpolated
-  (``pn_solver/stopping_power.jl:37-44``);
+  (``pn_solver/stopping_power.jl:37-154``);
 * elastic transport coefficients tc_{e,l}(E) -- ``transport_coefficient_funcs`` from
   ``pn_solver/transport_coefficient.jl``, absent from the reference tree;
 * ionisation cross-sections sigma_r(E) -- NeXLCore 0.3.7 ``ionizationcrosssection`` (Bote-Salvat
@@ -12,21 +12,24 @@ its tree:
 * mass absorption coefficients -- NeXLCore ``mac`` (FFAST) (``x_ray_intensities.jl:117``);
 * element densities and atomic masses -- PeriodicTable 1.1.3.
 
-None of those data sets is available here.  This module supplies documented stand-ins with the
-same roles and units (cm, g, eV); every solve consumes them as tables, so the GPU path and the
-oracle see identical numbers.  A caller with the real data passes its own tables instead.
+The stopping power is the reference's own in-tree data: ``icru77.py`` restates its ICRU-77
+table for the elements modelled here, and ``stopping_power_table`` converts and interpolates it
+as ``stopping_power_func`` does.  The other data sets are not available here, so this module
+supplies documented stand-ins with the same roles and units (cm, g, eV); every solve consumes
+them as tables, so the GPU path and the oracle see identical numbers.  A caller with the real
+data passes its own tables instead.
 
-Stand-ins, each a published closed form:
+Stand-ins (labelled as such), each a published closed form:
 
-* stopping power: Bethe formula with the Joy-Luo (1989) low-energy correction, tabulated on a
-  log-spaced knot grid and then linearly interpolated with a piecewise-constant slope, which is
-  the evaluation scheme of the reference (interpolation + forward-mode derivative);
 * transport coefficients: Legendre moments of the screened-Rutherford cross-section with a
   Wentzel screening parameter eta = 3.4e-3 Z^(2/3) / E[keV]; the moments use Neumann's integral
   int P_l(mu)/(a-mu) dmu = 2 Q_l(a) (Legendre functions of the second kind);
 * ionisation cross-section: Worthington-Tomlin (1956) form
   6.51e-14 n b / (U E_c^2) ln(4U / (1.65 + 2.35 e^(1-U))) cm^2 (E_c in eV), zero below the edge;
 * mass absorption coefficient: Kramers-type c Z^4 / (A E^3) with a K-edge jump of 8.
+
+Element densities are PeriodicTable's (the divisor of the stopping-power table); the line and
+edge energies are tabulated values.
 """
 from __future__ import annotations
 
@@ -85,7 +88,10 @@ class XRay:
 # stopping power
 # ------------------------------------------------------------------------------------------------
 def joy_luo_mass_stopping_power(el: Element, E_ev):
-    """Mass stopping power in eV cm^2/g (Bethe with the Joy-Luo correction)."""
+    """Mass stopping power in eV cm^2/g from the Bethe formula with the Joy-Luo (1989) correction.
+
+    Not used by the solve (which takes the ICRU-77 table); kept as an independent closed form that
+    the tests compare the table against."""
     E_kev = np.asarray(E_ev, dtype=float) * 1e-3
     J = (9.76 * el.Z + 58.5 * el.Z ** -0.19) * 1e-3
     k = 0.734 * el.Z ** 0.037
@@ -93,16 +99,16 @@ def joy_luo_mass_stopping_power(el: Element, E_ev):
     return s_kev * 1e3
 
 
-STOPPING_KNOTS_EV = np.geomspace(50.0, 1.0e9, 111)
-
-
 class LinearTable:
-    """Piecewise-linear interpolation on knots with the slope of the containing interval.
+    """Piecewise-linear interpolation on knots, with the slope of the interval holding E.
 
-    Mirrors ``stopping_power_func`` (stopping_power.jl:41-44): a linear interpolant evaluated at E
-    and differentiated by forward-mode AD, which yields the slope of the interval holding E.
-    Intervals are taken right-open, [x_i, x_{i+1}); outside the knots the call raises, as the
-    reference's interpolant does.
+    Mirrors ``stopping_power_func`` (stopping_power.jl:41-44): Interpolations' gridded linear
+    interpolant, value ``y_i (1 - t) + y_{i+1} t`` with ``t = (E - x_i) / (x_{i+1} - x_i)``, and its
+    derivative by forward-mode AD, ``y_i (-r) + y_{i+1} r`` with ``r = 1 / (x_{i+1} - x_i)``.  The
+    interval holding E is the last one whose left knot is <= E (right-open intervals), the last
+    interval at the last knot: at an interior knot the slope is the one of the interval to its
+    right.  Outside the knots the call raises, as the reference's interpolant does (its default
+    extrapolation throws).
     """
 
     def __init__(self, knots, values):
@@ -119,15 +125,25 @@ class LinearTable:
         i = self._interval(E)
         x0, x1, y0, y1 = self.x[i], self.x[i + 1], self.y[i], self.y[i + 1]
         t = (E - x0) / (x1 - x0)
-        return float(y0 + t * (y1 - y0))
+        return float(y0 * (1.0 - t) + y1 * t)
 
     def slope(self, E: float) -> float:
         i = self._interval(E)
-        return float((self.y[i + 1] - self.y[i]) / (self.x[i + 1] - self.x[i]))
+        r = 1.0 / (self.x[i + 1] - self.x[i])
+        return float(self.y[i] * -r + self.y[i + 1] * r)
 
 
 def stopping_power_table(el: Element) -> LinearTable:
-    return LinearTable(STOPPING_KNOTS_EV, joy_luo_mass_stopping_power(el, STOPPING_KNOTS_EV))
+    """ICRU-77 total mass stopping power of `el` in eV cm^2/g on knots in eV.
+
+    As ``stopping_power_func`` builds it (stopping_power.jl:40-41): the energies converted MeV -> eV,
+    the stopping powers MeV/cm -> eV/cm and divided by the element's density in g/cm^3."""
+    from . import icru77
+    if el.Z not in icru77.TOTAL_MEV_PER_CM:
+        raise ValueError(f"no ICRU-77 stopping-power row for Z = {el.Z}; pass the element's table")
+    knots = np.array(icru77.ENERGIES_MEV) * 1000000.0
+    values = np.array(icru77.TOTAL_MEV_PER_CM[el.Z]) * 1000000.0 / el.density
+    return LinearTable(knots, values)
 
 
 # ------------------------------------------------------------------------------------------------

@@ -154,6 +154,8 @@ def test_tma_tiles_against_the_oracle(gpu_lib, oracle):
         I_o, rb_o, nb_o, ab_o = oracle.adjoint(d, rho, noa, acs, ib[q])
         assert rel(I[q], I_o) < 1e-4
         assert rel(rb[q], rb_o) < 1e-3
+        assert rel(nb[q], nb_o) < 1e-3
+        assert rel(ab[q], ab_o) < 1e-3
 
 
 def test_tma_tiles_3d_against_the_oracle(gpu_lib, oracle):

