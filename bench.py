@@ -3,18 +3,27 @@
 Workload: 256 (lateral) x 128 (depth) grid over 2 x 1 um, P_11 (78 active moments), Fe/Cr/Ni with
 a seeded smooth mass-fraction field, 20 beam positions x {10, 15, 20} keV, forward + adjoint for
 each of the 60 beam/energy combinations.  Synthetic data (seeded); the step counts follow the
-stability estimate of the march (200, 372 and 702 steps for the three energies).
+stability estimate of the march (200, 356 and 663 steps for the three energies).
 
 One bench step = all 60 forward + adjoint solves.
   value          FP64 "plain" solves/s: one solve at a time through the device-pointer C ABI
                  (inputs resident in HBM), per-solve latencies from CUDA events
-  fp32_batched   the same 60 solves in FP32 (FP64 accumulators), all in flight at once
-  e2e            FP64 plain through the host-pointer C ABI (pinned host buffers, copies timed)
-  roofline       the sub-step kernel (dominant kernel): algorithmic bytes per launch / launch time
-  cpu_baseline   the CPU oracle on the host cores, bounded sample, extrapolated to solves/s
+  e2e            the same through the host-pointer C ABI (pinned host buffers, copies timed),
+                 over every timed step
+  fp32_batched   the same 60 solves in FP32 (FP64 accumulators), all in flight at once, with the
+                 forward and adjoint sweeps' HBM rooflines and an e2e through the server's
+                 host-buffer C ABI
+  served         the served stream (Poisson requests of 1D/2D/3D solves, 50/40/10) through
+                 pn_server at the offered rate and at 90 % of the measured capacity
+  roofline       the FP64 sub-step kernel (dominant kernel of `value`): algorithmic FP64 flops
+                 per launch / launch time against the FP64 FMA rate measured in this run; its
+                 HBM view beside it
+  cpu_baseline   the CPU oracle on all host cores: one complete forward + adjoint solve per beam
+                 energy, timed, weighted as the workload mixes them
 
-`--impl reference` times the CPU oracle (the restatement of the reference's Julia path; Julia is
-not available) on all host cores with the same metric and prints its own line.
+`--impl reference` times complete solves of the CPU oracle (the restatement of the reference's
+Julia path; Julia is not available) on all host cores with the same metric and prints its own
+line.
 """
 from __future__ import annotations
 
@@ -44,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--positions", type=int, default=20, help="beam positions per energy (20 = full workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-steps", type=int, default=3)
+    ap.add_argument("--no-serve", action="store_true", help="leave the served stream out of the default line")
     ap.add_argument("--profile", action="store_true",
                     help="run one 10 keV solve (FP64 twice, FP32 once) for a profiler, print nothing else")
     ap.add_argument("--profile-batch", action="store_true",
@@ -162,66 +171,210 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def algorithmic_bytes_adjoint_step(solve, elem):
+    """Bytes one adjoint energy step of the batched TMA path must move: the fused sub-steps of
+    the adjoint state (as the forward, `algorithmic_bytes_per_step(fused=True)`) plus the density
+    integral, which reads the tape state and the adjoint state of every class once
+    (s * 2 M_active), the densities (s n_e C_all) and reads and writes rho_bar (2 * 8 n_e C_all)."""
+    g = solve.problem.gspec
+    from pnepma_gb300.moments import class_sizes
+    nm = class_sizes(solve.problem.N)
+    sub, m_active = algorithmic_bytes_per_step(solve, elem, fused=True)
+    cells = 0
+    for c in g.active_classes():
+        if nm[c] == 0:
+            continue
+        rx, ry, rz = g.interior_ranges(c)
+        cells += len(rx) * len(ry) * len(rz)
+    ne = len(solve.problem.elements)
+    return sub + elem * 2 * m_active + elem * ne * cells + 16 * ne * cells
+
+
+def fp64_flops_per_launch(solve):
+    """Algorithmic FP64 flops of one average sub-step launch of the plain path (three launches per
+    energy step), counted from the compiled stencil: per target cell, per active axis one
+    difference per neighbour moment and one FMA (2 flops) per coupling coefficient; per moment the
+    update u + g_l ((q - A u) - C_l u) (5 flops); per cell and degree present in the class the
+    factors, S = sum_e rho_e s_e (2 n_e), C_l (2 n_e), g_l = dt/S phi1(-C_l dt/S) with the degree-10
+    series (22) -- computed in sub-steps 1 and 2 and reused by sub-step 3; per ghost point of a face
+    the boundary product B v (2 n_odd n_even)."""
+    from pnepma_gb300 import codegen
+    from pnepma_gb300.moments import class_moments, parity, switch, class_bits
+    N = solve.problem.N
+    g = solve.problem.gspec
+    ne = len(solve.problem.elements)
+    ms = class_moments(N)
+    nm = [len(v) for v in ms]
+    act = [not g.axes[d].singleton for d in range(3)]
+    per_launch = {0: 0.0, 1: 0.0}         # by parity: computing factors
+    cached = 0.0                          # odd parity with cached factors
+    for c in g.active_classes():
+        if nm[c] == 0:
+            continue
+        rx, ry, rz = g.interior_ranges(c)
+        cells = len(rx) * len(ry) * len(rz)
+        sten = 0
+        for d in range(3):
+            if not act[d]:
+                continue
+            cols = codegen.block_structure(N, c, d)
+            sten += len(cols) + 2 * sum(len(r) for _j, r in cols)
+        degs = len(set(l for (l, _k) in ms[c]))
+        upd = 5 * nm[c]
+        fac = 2 * ne + 2 + degs * (2 * ne + 22)
+        ghosts = 0
+        shape = g.class_shape(c)
+        for d in range(3):
+            # the ghost faces of the neighbour class switch(c, d) that this class's stencil reads
+            f = switch(c, d)
+            if act[d] and class_bits(f)[d] and nm[f] > 0:
+                across = 1
+                for e in range(3):
+                    if e != d:
+                        across *= shape[e]
+                ghosts += 2 * across * (2 * nm[f] * nm[c])
+        par = parity(c)
+        per_launch[par] += cells * (sten + upd + fac) + ghosts
+        if par == 1:
+            cached += cells * (sten + upd) + ghosts
+    return (per_launch[1] + per_launch[0] + cached) / 3.0
+
+
+def fp64_peak_tflops(dev, stream):
+    """FP64 FMA throughput of this GPU, measured now: the library's probe kernel (8 independent FMA
+    chains per thread, 16 flops per iteration) on 8 blocks per SM, timed with CUDA events."""
+    import torch
+    from pnepma_gb300 import capi
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = 8 * sms, 4096
+    out = torch.zeros(blocks, dtype=torch.float64, device=dev)
+    L = capi.lib()
+    best = None
+    for rep in range(6):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        rc = L.pn_probe_fp64_fma(blocks, iters, capi._ptr(out.data_ptr()), capi._ptr(stream.cuda_stream))
+        if rc:
+            raise capi.PnError(rc, L.pn_last_error(None).decode())
+        b.record(stream)
+        stream.synchronize()
+        if rep:
+            t = a.elapsed_time(b) / 1e3
+            best = t if best is None else min(best, t)
+    return blocks * 256 * iters * 16 / best / 1e12
+
+
 # ------------------------------------------------------------------------------------------------
-def cpu_sample(solves, threads, sample_steps):
-    """Oracle time of `threads` solves truncated to `sample_steps` steps, run concurrently; returns
-    (seconds per energy step per core, description)."""
+def oracle_solve_seconds(solve, threads):
+    """Wall time of one complete forward + adjoint solve of the CPU oracle on `threads` host
+    threads (the loops over points split across them; results independent of the count)."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import oracle
-    from pnepma_gb300.problem import ForwardPNProblem
-    picks = [solves[(i * 7) % len(solves)] for i in range(threads)]
-    descs, keeps, rhos, noas, acss, ibars = [], [], [], [], [], []
-    for s in picks:
-        p = s.problem
-        q = ForwardPNProblem(p.N, p.gspec, p.elements, p.beam_energy, p.beam_position, p.beam_direction,
-                             p.E_initial, p.E_initial - sample_steps * p.delta_e, sample_steps)
-        d, k = q.descriptor(s.x_rays)
-        rho, noa, acs = s.inputs()
-        descs.append(d)
-        keeps.append((k, q))
-        rhos.append(rho)
-        noas.append(noa)
-        acss.append(acs)
-        ibars.append(np.ones(len(s.x_rays)))
+    from pnepma_gb300.problem import PN_FP64
+    prec = solve.problem.precision
+    solve.problem.precision = PN_FP64
+    d, k = solve.problem.descriptor(solve.x_rays)
+    solve.problem.precision = prec
+    rho, noa, acs = solve.inputs()
+    oracle.set_threads(threads)
     t0 = time.perf_counter()
-    oracle.solve_many(descs, rhos, noas, acss, ibars, threads)
-    wall = time.perf_counter() - t0
-    per_step_core = wall / sample_steps
-    desc = (f"{threads} of the 60 solves truncated to {sample_steps} energy steps each, forward+adjoint, "
-            f"one solve per host thread; scaled by the full step counts")
-    return per_step_core, desc, wall
+    oracle.adjoint(d, rho, noa, acs, np.ones(len(solve.x_rays)))
+    return time.perf_counter() - t0
 
 
-def cpu_solves_per_s(solves, per_step_core, threads):
-    total_steps = sum(s.problem.N_steps for s in solves)
-    return len(solves) / (per_step_core * total_steps / threads)
+def by_energy(solves):
+    out = {}
+    for s in solves:
+        out.setdefault(float(s.problem.beam_energy.mean), []).append(s)
+    return out
+
+
+def cpu_threads():
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import oracle
+    return oracle.threads_available()
+
+
+def mix_rate(times, groups):
+    """Solves/s of the workload's mix from the mean complete-solve time per beam energy: the
+    workload holds the same number of solves at each energy.  An energy without a timed solve
+    takes the per-energy-step time of the timed ones times its step count (marked estimated)."""
+    per_step = [t / s for E, ts in times.items() for (t, s) in ts]
+    est = []
+    total = 0.0
+    for E, group in sorted(groups.items()):
+        if times.get(E):
+            total += float(np.mean([t for t, _s in times[E]]))
+        else:
+            total += float(np.mean(per_step)) * group[0].problem.N_steps
+            est.append(E)
+    return len(groups) / total, est
+
+
+def cpu_baseline_measure(solves):
+    """The CPU baseline of the GPU line: one complete oracle solve per beam energy (position 7 of
+    20, as the parity fixtures), all host cores, weighted as the workload mixes the energies."""
+    threads = cpu_threads()
+    groups = by_energy(solves)
+    times = {}
+    for E, group in sorted(groups.items()):
+        s = group[min(7, len(group) - 1)]
+        times[E] = [(oracle_solve_seconds(s, threads), s.problem.N_steps)]
+    v, est = mix_rate(times, groups)
+    wall = sum(t for ts in times.values() for t, _ in ts)
+    sample = (f"one complete forward+adjoint solve per beam energy ({', '.join(f'{E / 1e3:g} keV' for E in sorted(groups))}; "
+              f"{', '.join(str(g[0].problem.N_steps) for _E, g in sorted(groups.items()))} steps) on {threads} host threads, "
+              f"{wall:.1f} s of wall time; solves/s of the equal mix of the three energies")
+    return {"value": v, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample,
+            "seconds_per_solve": {f"{E / 1e3:g} keV": ts[0][0] for E, ts in sorted(times.items())}}
 
 
 def run_reference(args):
+    """The reference arm: complete forward + adjoint solves of the CPU oracle (the FP64
+    restatement of the reference's Julia march; Julia is not installed) on all host cores.  One
+    step = one complete solve; the steps cycle through the three beam energies (and through the
+    beam positions), the warm-up steps are complete solves at the lowest energy.  `value` is the
+    solves/s of the workload's equal mix of energies from the mean time per energy; `ms_per_step`
+    is the mean time of the timed solves, so steps x ms_per_step is the timed region."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     solves = workload(args.positions)
-    threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.warmup):
-        cpu_sample(solves, threads, args.cpu_sample_steps)
+    groups = by_energy(solves)
+    energies = sorted(groups)
+    threads = cpu_threads()
+    for w in range(args.warmup):
+        oracle_solve_seconds(groups[energies[0]][(7 + w) % len(groups[energies[0]])], threads)
+    times = {}
     walls = []
-    for _ in range(args.steps):
-        per, desc, wall = cpu_sample(solves, threads, args.cpu_sample_steps)
-        vals.append(cpu_solves_per_s(solves, per, threads))
-        walls.append(wall)
-    v = float(np.median(vals))
+    t_all = time.perf_counter()
+    for t in range(args.steps):
+        E = energies[t % len(energies)]
+        group = groups[E]
+        s = group[(7 + 3 * (t // len(energies))) % len(group)]
+        dt = oracle_solve_seconds(s, threads)
+        times.setdefault(E, []).append((dt, s.problem.N_steps))
+        walls.append(dt)
+    t_all = time.perf_counter() - t_all
+    v, est = mix_rate(times, groups)
+    sample = (f"{args.steps} complete forward+adjoint solves cycling {', '.join(f'{E / 1e3:g}' for E in energies)} keV "
+              f"on {threads} host threads ({args.warmup} warm-up solves at {energies[0] / 1e3:g} keV)")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(solves) / v,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(walls)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "solves_per_step": len(solves),
+        "config": {"workload": WORKLOAD, "solves_per_step": 1,
                    "energy_steps": sorted(set(s.problem.N_steps for s in solves)),
+                   "step": "one complete forward+adjoint solve; value = solves/s of the 60-solve mix "
+                           "(20 per energy) from the mean solve time per energy",
                    "reference_runtime": "Julia unavailable on this box: CPU FP64 restatement of the reference march"},
-        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port",
-                         "sample": desc},
+        "seconds_per_solve_by_energy_kev": {f"{E / 1e3:g}": float(np.mean([t for t, _ in ts]))
+                                            for E, ts in sorted(times.items())},
+        "estimated_energies_kev": [E / 1e3 for E in est],
+        "timed_region_s": t_all,
+        "cpu_baseline": {"value": v, "unit": "solves/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -406,7 +559,7 @@ def run_ours(args):
         g32 = rb32[i].cpu().numpy()
         g_err = max(g_err, float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))))
 
-    # ---------------- e2e through the host-pointer ABI with pinned buffers
+    # ---------------- e2e through the host-pointer ABI with pinned buffers, every timed step
     p_rho = torch.from_numpy(rho).pin_memory()
     p_noa = torch.from_numpy(noa).pin_memory()
     p_acs = torch.from_numpy(acs).pin_memory()
@@ -428,12 +581,50 @@ def run_ours(args):
 
     e2e_step()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), dist, dev)
     h2d = nsol * (rho.nbytes + noa.nbytes + acs.nbytes + 8 * nr)
     d2h = nsol * (8 * nr + 8 * (sz.n_rho + sz.n_noa + sz.n_acs))
+
+    # ---------------- FP32 batched e2e: the 60 solves as one request through the server's host-buffer ABI
+    served = None
+    fp32_e2e = None
+    # the batch's tapes hold most of the device memory: release them for the server
+    batch.close()
+    batch = None
+    torch.cuda.empty_cache()
+    ib_host = d_ibar.cpu().numpy()
+    items = [(descs32[i], rho, noa, acs, ib_host[i]) for i in range(nsol)]
+    outs = [(np.zeros(nr), np.zeros(sz.n_rho), np.zeros(sz.n_noa), np.zeros(max(sz.n_acs, 1)))
+            for _ in range(nsol)]
+    budget32 = int(0.8 * torch.cuda.mem_get_info(dev)[0])
+    with capi.Server(memory_budget=budget32) as srv:
+        srv.submit(items, adjoint=True, outputs=outs).wait()
+        fp32_e2e_times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            srv.submit(items, adjoint=True, outputs=outs).wait()
+            fp32_e2e_times.append(time.perf_counter() - t0)
+    fp32_e2e_s = max_over_ranks(float(np.mean(fp32_e2e_times)), dist, dev)
+    I32_e2e = np.array([o[0] for o in outs])
+    fp32_e2e = {"value": world * nsol / fp32_e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": rho.nbytes + noa.nbytes + acs.nbytes + 8 * nr * nsol,
+                "d2h_bytes_per_step": nsol * 8 * (nr + sz.n_rho + sz.n_noa + sz.n_acs),
+                "ms_per_step": 1e3 * fp32_e2e_s,
+                "max_rel_err_intensity_vs_device_batch": float(np.max(np.abs(I32_e2e - I32) / np.abs(I32))),
+                "form": "pn_submit of one 60-solve request (host buffers; the shared material uploaded once) "
+                        "+ wait, per step; the server builds the wave's batch in its arena"}
+
+    # ---------------- served stream (config 5), bounded: 48 requests at 200 requests/s, then at 90 % of capacity
+    if rank == 0 and not args.no_serve:
+        served = served_summary(args)
 
     # ---------------- roofline of the sub-step kernel (timed via the forward graph)
     fwd_ms = []
@@ -452,6 +643,9 @@ def run_ours(args):
     launches = sum(3 * n for _t, n in fwd_ms)
     t_launch = sum(t for t, _n in fwd_ms) / launches * 1e-3
     achieved = (bytes_step / 3) / t_launch / 1e9
+    flops_launch = fp64_flops_per_launch(solves[0])
+    fp64_achieved = flops_launch / t_launch / 1e12
+    fp64_peak = fp64_peak_tflops(dev, stream)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
@@ -465,16 +659,19 @@ def run_ours(args):
         traffic = prof.get("dram_bytes_per_launch")
     except Exception:
         pass
+    # the FP32 adjoint sweep: fused sub-steps of the adjoint state, the density integral and the
+    # forward steps the tape recomputes, over the adjoint time of the batch
+    adj_bytes = sum(s.problem.N_steps * algorithmic_bytes_adjoint_step(s, 4) for s in solves)
+    adj_bytes += binfo.recomputed_steps * bytes32_step
+    adj_ms = float(np.mean(b_ms)) - float(np.mean(b_fwd))
+    fp32_adj_gbs = adj_bytes / (adj_ms / 1e3) / 1e9
 
     gpu_launches = args.steps * sum(h.info().forward_kernels + h.info().adjoint_kernels for h in handles64)
     mcu = sum(2 * s.problem.N_steps for s in solves) * m_active
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        per, desc, wall = cpu_sample(solves, threads, args.cpu_sample_steps)
-        cpu = {"value": cpu_solves_per_s(solves, per, threads), "unit": "solves/s", "cores": threads,
-               "kind": "port", "sample": desc}
+        cpu = cpu_baseline_measure(solves)
 
     if rank == 0:
         line = {
@@ -492,7 +689,7 @@ def run_ours(args):
                              "speedup_vs_fp64_plain": fp32_value / value,
                              "latency_ms": {"p50": float(np.percentile(b_lat, 50)),
                                             "p99": float(np.percentile(b_lat, 99))},
-                             "forward_ms": float(np.mean(b_fwd)),
+                             "forward_ms": float(np.mean(b_fwd)), "adjoint_ms": adj_ms,
                              "max_rel_err_intensity_vs_fp64": k_err, "max_rel_err_rho_bar_vs_fp64": g_err,
                              "checkpoint_stride": binfo.checkpoint_stride,
                              "recomputed_steps": binfo.recomputed_steps,
@@ -505,26 +702,40 @@ def run_ours(args):
                                                   "note": "algorithmic bytes of all forward sub-steps of the 60 solves "
                                                           "(fused schedule: 3 M_even + 3 M_odd values and the densities "
                                                           "once per step) / forward time"},
+                             "adjoint_roofline": {"bound": "hbm", "achieved": fp32_adj_gbs, "peak": peak,
+                                                  "unit": "GB/s", "frac": fp32_adj_gbs / peak,
+                                                  "peak_source": peak_source,
+                                                  "kernel": "batch_tma_kernel<11, adjoint, 2D> + batch_tma_int_kernel<11>, "
+                                                            "adjoint sweep",
+                                                  "note": "per step: the fused sub-steps of the adjoint state, the "
+                                                          "density integral (tape and adjoint state of every class, "
+                                                          "densities, rho_bar read and written in FP64), plus the "
+                                                          "recomputed forward steps; over ms_per_step - forward_ms"},
                              "kernels_per_step": binfo.forward_kernels + binfo.adjoint_kernels,
+                             "e2e": fp32_e2e,
                              "form": "one pn_batch: one launch per sub-step covers all 60 solves"},
             "moment_cell_updates_per_s": world * mcu / (step_ms / 1e3),
             "e2e": {"value": world * nsol / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "steps": args.steps},
+            "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": fp64_achieved / fp64_peak, "traffic": traffic,
                          "kernel": "substep_kernel<double,11> (forward)",
-                         "algorithmic_bytes_per_launch": bytes_step / 3,
-                         "launch_us": t_launch * 1e6},
+                         "algorithmic_flops_per_launch": flops_launch,
+                         "peak_source": "measured in this run: pn_probe_fp64_fma (independent FP64 FMA chains)",
+                         "launch_us": t_launch * 1e6,
+                         "hbm": {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                 "algorithmic_bytes_per_launch": bytes_step / 3, "peak_source": peak_source}},
             "gpu_launches": gpu_launches,
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
         }
+        if served:
+            line["served"] = served
         if cpu:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
     for h in handles64:
         h.close()
-    batch.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -688,6 +899,41 @@ def serve_run(stream, budget, rate_scale=1.0, reqs=None):
     out["latency_ms_by_kind"] = {k: {"n": len(v), "p50": float(np.percentile(v, 50)),
                                      "p99": float(np.percentile(v, 99))} for k, v in sorted(by_kind.items())}
     return out
+
+
+def served_summary(args):
+    """The served stream for the default line, bounded to about a minute: the config-5 mix of
+    `--serve-requests` requests at the offered Poisson rate (`--serve-rate`, 200 requests/s), whose
+    saturated throughput is the largest rate the server sustains, then the same stream offered at
+    90 % of that rate for its latencies under a sustainable load."""
+    from pnepma_gb300.problem import PN_FP32
+    t_prep = time.perf_counter()
+    stream = ServedStream(args.serve_requests, args.serve_rate, PN_FP32)
+    t_prep = time.perf_counter() - t_prep
+    budget = int(args.serve_budget_gb * 1e9)
+    first = {}
+    for r in stream.reqs:
+        first.setdefault(r.kind, r)
+    serve_run(stream, budget, rate_scale=50.0, reqs=list(first.values()))   # warm-up: one request per kind
+    at_rate = serve_run(stream, budget)
+    capacity = at_rate["requests_per_s"]
+    sustained = serve_run(stream, budget, rate_scale=0.9 * capacity / args.serve_rate)
+    mix = {}
+    for r in stream.reqs:
+        mix[r.kind] = mix.get(r.kind, 0) + 1
+    return {"workload": "config5 stream: requests of 16 positions x {10, 15} keV forward+adjoint, FP32; "
+                        "1D N=7 200 cells / 2D N=11 128x64 / 3D N=5 64x64x48 at 50/40/10",
+            "requests": len(stream.reqs), "mix": mix, "memory_budget_bytes": budget, "host_prep_s": t_prep,
+            "offered_requests_per_s": at_rate["offered_requests_per_s"],
+            "achieved_requests_per_s": at_rate["requests_per_s"], "solves_per_s": at_rate["solves_per_s"],
+            "latency_ms_at_offered_rate": at_rate["latency_ms"],
+            "largest_sustained_requests_per_s": capacity,
+            "at_90pct_of_sustained": {"offered_requests_per_s": sustained["offered_requests_per_s"],
+                                      "achieved_requests_per_s": sustained["requests_per_s"],
+                                      "solves_per_s": sustained["solves_per_s"],
+                                      "latency_ms": sustained["latency_ms"],
+                                      "latency_ms_by_kind": sustained["latency_ms_by_kind"]},
+            "waves": at_rate["waves"], "max_waves_in_flight": at_rate["max_waves_in_flight"]}
 
 
 def fp64_sequential_seconds(stream):

@@ -248,7 +248,13 @@ enum pn_batch_flags {
   /* issue the kernels of every sweep on the caller's stream instead of capturing the sweeps as
      CUDA graphs at creation: cheaper for a batch that runs once (each call then launches 2-3
      kernels per energy step from the host) */
-  PN_BATCH_DIRECT_LAUNCH = 2
+  PN_BATCH_DIRECT_LAUNCH = 2,
+  /* test hook for the failure path of the bounded device-side waits (FP32 TMA groups): the first
+     tile wait of the batch's first sub-step launch is reported as run out after it has completed,
+     so the launch takes its timeout path (status PN_ERR_TIMEOUT, copies in flight drained, the CTA
+     returns) without any copy in flight; that call's results are then incomplete.  Later calls
+     run normally; the status word is cleared by every pn_batch_forward */
+  PN_BATCH_TEST_EXPIRE_WAIT = 4
 };
 
 typedef struct pn_batch_info {
@@ -267,8 +273,9 @@ int pn_batch_forward(pn_batch* b, const double* const* rho, const double* const*
                      const double* const* acs, double* const* intensities, void* stream);
 int pn_batch_adjoint(pn_batch* b, const double* const* intensities_bar, double* const* rho_bar,
                      double* const* noa_bar, double* const* acs_bar, void* stream);
-/* Fills *info.  Returns PN_ERR_TIMEOUT when a bounded device-side wait of an earlier launch ran
-   out (call it after that work has completed). */
+/* Fills *info.  Returns PN_ERR_TIMEOUT when a bounded device-side wait of the latest
+   pn_batch_forward or of the pn_batch_adjoint calls after it ran out (call it after that work has
+   completed). */
 int pn_batch_query(const pn_batch* b, pn_batch_info* info);
 void pn_batch_destroy(pn_batch* b);
 
@@ -455,6 +462,12 @@ const char* pn_last_error(const pn_handle* h);
 /* Self-test of the FP32 exponential factor phi1(c) = (e^c - 1) / c used by the FP32 kernels
    (no counterpart in the reference): evaluates it and the expm1f(c) / c form for n arguments. */
 int pn_selftest_phi1(int32_t n, const float* x, float* phi1_fast, float* phi1_ref);
+
+/* FP64 throughput probe (diagnostic; no counterpart in the reference): launches `blocks` blocks of
+   256 threads, each thread running 8 independent FP64 FMA chains for `iters` iterations
+   (blocks * 256 * iters * 16 flops) on `stream`; `out` is a device buffer of `blocks` doubles.
+   The benchmark times it with events to measure the FP64 roofline of the plain path. */
+int pn_probe_fp64_fma(int32_t blocks, int32_t iters, double* out, void* stream);
 
 /* ABI version and the compiled P_N orders (bit N set when order N is available). */
 int32_t pn_abi_version(void);

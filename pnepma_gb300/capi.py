@@ -29,6 +29,7 @@ class PnHandleInfo(ctypes.Structure):
 
 PN_BATCH_GENERIC_KERNELS = 1
 PN_BATCH_DIRECT_LAUNCH = 2
+PN_BATCH_TEST_EXPIRE_WAIT = 4
 
 
 class PnBatchOptions(ctypes.Structure):
@@ -73,7 +74,7 @@ SERVER_EXPORTS = ("pn_server_create", "pn_submit", "pn_poll", "pn_wait", "pn_ser
 EXPORTS = SERVER_EXPORTS + ("pn_batch_create", "pn_batch_forward", "pn_batch_adjoint", "pn_batch_query", "pn_batch_destroy",
            "pn_forward_noalloc", "pn_query_handle", "pn_query_sizes", "pn_create", "pn_forward", "pn_adjoint", "pn_forward_device", "pn_adjoint_device",
            "pn_generation_field", "pn_set_state", "pn_step", "pn_get_state", "pn_destroy", "pn_last_error",
-           "pn_abi_version", "pn_compiled_orders", "pn_material_create", "pn_material_fields",
+           "pn_abi_version", "pn_compiled_orders", "pn_probe_fp64_fma", "pn_material_create", "pn_material_fields",
            "pn_material_pullback", "pn_material_destroy")
 
 
@@ -134,6 +135,8 @@ def lib():
         L.pn_server_destroy.restype = None
         L.pn_selftest_phi1.argtypes = [ctypes.c_int32, P, P, P]
         L.pn_selftest_phi1.restype = ctypes.c_int
+        L.pn_probe_fp64_fma.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P]
+        L.pn_probe_fp64_fma.restype = ctypes.c_int
         L.pn_material_create.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int64)]
         L.pn_material_create.restype = ctypes.c_int
         L.pn_material_fields.argtypes = [P, P, P, P, P, P]
@@ -353,9 +356,12 @@ class Server:
             raise PnError(rc, lib().pn_last_error(None).decode())
         self._s = s
 
-    def submit(self, solves, adjoint: bool = True) -> Ticket:
+    def submit(self, solves, adjoint: bool = True, outputs=None) -> Ticket:
         """solves: list of (desc, rho, noa, acs, ibar) with host numpy inputs (ibar ignored for a
-        forward request).  Arrays passed as the same object are uploaded once per wave."""
+        forward request).  Arrays passed as the same object are uploaded once per wave.  `outputs`
+        optionally gives, per solve, contiguous float64 arrays (intensities, rho_bar, noa_bar,
+        acs_bar) of the sizes pn_query_sizes states, which receive the results instead of new
+        arrays."""
         n = len(solves)
         descs = (ctypes.c_void_p * n)()
         keep = {"descs": [], "in": [], "I": [], "rb": [], "nb": [], "ab": []}
@@ -377,6 +383,17 @@ class Server:
             arrs["noa"].append(host(noa))
             arrs["acs"].append(host(acs))
             arrs["ibar"].append(host(ibar) if adjoint else None)
+            if outputs is not None:
+                oI, orb, onb, oab = outputs[i]
+                for a, nmin in ((oI, d.n_xrays), (orb, z.n_rho), (onb, z.n_noa), (oab, z.n_acs)):
+                    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or a.size < nmin:
+                        raise ValueError("outputs must be contiguous float64 arrays of the queried sizes")
+                keep["I"].append(oI)
+                if adjoint:
+                    keep["rb"].append(orb)
+                    keep["nb"].append(onb)
+                    keep["ab"].append(oab)
+                continue
             keep["I"].append(np.zeros(d.n_xrays))
             if adjoint:
                 keep["rb"].append(np.zeros(z.n_rho))

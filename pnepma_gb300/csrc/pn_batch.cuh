@@ -624,7 +624,8 @@ class BatchGroup : public BatchGroupBase {
   int tma_int_grid = 0;
   CUtensorMap* dmaps = nullptr;
   void* drows = nullptr;
-  int* dstatus = nullptr;
+  int* dstatus = nullptr;          // [0] status of the latest calls, [1] test expiries left
+  bool test_expire = false;         // PN_BATCH_TEST_EXPIRE_WAIT
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
   // Creation never waits for the device: tables go up on `up`, whose event the first forward or
   // adjoint waits on in stream order, and the tape / density zeroing is enqueued with the first
@@ -877,6 +878,7 @@ class BatchGroup : public BatchGroupBase {
       if ((rc = upload(dtiles[list], tiles[list]))) return rc;
     }
     if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
+      test_expire = (flags & PN_BATCH_TEST_EXPIRE_WAIT) != 0;
       if (!(flags & PN_BATCH_GENERIC_KERNELS))
         if ((rc = build_tma())) return rc;
     } else {
@@ -1056,8 +1058,12 @@ class BatchGroup : public BatchGroupBase {
         S.scale_g = I.scale_g;
       }
       if ((rc = upload(dsolves, hs))) return rc;
-      if ((rc = alloc(dstatus, 1))) return rc;
-      PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), up));
+      if ((rc = alloc(dstatus, 2))) return rc;
+      {
+        // pageable source: staged before the call returns
+        const int st0[2] = {0, test_expire ? 1 : 0};
+        PN_CUDA(cudaMemcpyAsync(dstatus, st0, sizeof(st0), cudaMemcpyHostToDevice, up));
+      }
       // tiles over every target cell per list; partial slots are the eee tiles of list 0 in tile order
       n_ptiles = 0;
       for (int q = 0; q < n; ++q) {
@@ -1413,6 +1419,7 @@ class BatchGroup : public BatchGroupBase {
         a.rows = static_cast<const ArgRow<N>*>(drows);
         a.partial = part;
         a.status = dstatus;
+        a.test_expire = test_expire ? dstatus + 1 : nullptr;
         a.pr = pr;
         a.n_tiles = nb;
         a.mode = mode;
@@ -1567,6 +1574,8 @@ class BatchGroup : public BatchGroupBase {
   int forward(const BIo* io_host, cudaStream_t s) override {
     int rc;
     if ((rc = prepare(s))) return rc;
+    // the status word reports the waits of this forward and the adjoint that follows it
+    if (dstatus) PN_CUDA(cudaMemsetAsync(dstatus, 0, sizeof(int), s));
     if ((rc = put_io(io_host, s))) return rc;
     batch_load_kernel<T><<<dim3(256, n), 256, 0, s>>>(dinst, dio);
     PN_CUDA(cudaGetLastError());

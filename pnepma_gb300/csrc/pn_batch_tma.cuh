@@ -145,6 +145,7 @@ struct TLaunch {
   const ArgRow<N>* rows;
   double* partial;
   int* status;
+  int* test_expire;   // PN_BATCH_TEST_EXPIRE_WAIT: expiries left to report, else NULL
   int pr;
   int n_tiles;
   int mode, j, K;
@@ -750,7 +751,12 @@ __global__ void __launch_bounds__(TB, PN_TMA_MINB) batch_tma_kernel(const __grid
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tma_issue<N, ADJ, DIMS>(L, L.tiles[ta], smem + (ka % TSTAGES) * LY::STAGE, &full[ka % TSTAGES]);
     }
-    const bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
+    bool ok = mbar_wait_bounded(&full[s], (unsigned)((k / TSTAGES) & 1));
+    // test hook: report a wait that has completed (its copies have landed) as run out, once per
+    // batch, so that the failure path runs with no copy of this stage in flight
+    if (L.test_expire != nullptr && k == 0 && threadIdx.x == 0 && ok && *(volatile int*)L.test_expire > 0 &&
+        atomicSub(L.test_expire, 1) > 0)
+      ok = false;
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
         atomicExch(L.status, (int)PN_ERR_TIMEOUT);

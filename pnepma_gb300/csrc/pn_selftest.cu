@@ -45,3 +45,32 @@ extern "C" int pn_selftest_phi1(int32_t n, const float* x, float* phi1_fast, flo
   }
   return PN_OK;
 }
+
+// FP64 fused multiply-add throughput probe: every thread runs 8 independent FMA chains for `iters`
+// iterations (16 flops per iteration), so the FP64 pipe, not latency, bounds it.  The chains
+// converge to y / (1 - x) and stay finite; their sum is written so nothing is optimised away.
+static __global__ void __launch_bounds__(256) fp64_fma_kernel(int iters, double x, double y, double* out) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1.0, a2 = a0 + 2.0, a3 = a0 + 3.0;
+  double a4 = a0 + 4.0, a5 = a0 + 5.0, a6 = a0 + 6.0, a7 = a0 + 7.0;
+  for (int it = 0; it < iters; ++it) {
+    a0 = fma(a0, x, y); a1 = fma(a1, x, y); a2 = fma(a2, x, y); a3 = fma(a3, x, y);
+    a4 = fma(a4, x, y); a5 = fma(a5, x, y); a6 = fma(a6, x, y); a7 = fma(a7, x, y);
+  }
+  const double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+  if (s == 12345.678) out[blockIdx.x] = s;   // practically never taken; keeps the chains live
+  if (threadIdx.x == 0 && blockIdx.x == 0) out[0] = s;
+}
+
+extern "C" int pn_probe_fp64_fma(int32_t blocks, int32_t iters, double* out, void* stream) {
+  if (blocks < 1 || iters < 1 || !out) {
+    pn::set_last_error("blocks and iters must be positive and out a device buffer of `blocks` doubles");
+    return PN_ERR_INVALID;
+  }
+  fp64_fma_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, 0.999999, 1e-6, out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    pn::set_last_error(std::string("FP64 probe launch failed: ") + cudaGetErrorString(e));
+    return PN_ERR_CUDA;
+  }
+  return PN_OK;
+}

@@ -31,7 +31,7 @@ TOL64 = 1e-10            # FP64 plain vs the oracle, normwise and projections
 TOL64_ELEMENT = 1e-8     # FP64 plain, per element at magnitudes >= 1e-3 of the largest
 TOL32_K = 1e-4           # FP32 batch: intensities (k-ratios)
 TOL32_GRAD = 1e-3        # FP32 batch: cotangents, normwise and projections
-TOL32_ELEMENT = 2e-2     # FP32 batch: per element at magnitudes >= 1e-3 of the largest
+TOL32_ELEMENT = 1e-3     # FP32 batch: per element at magnitudes >= 1e-3 of the largest
 
 
 @pytest.fixture(scope="module")
