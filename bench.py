@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--profile-batch", action="store_true",
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
     ap.add_argument("--profile-positions", type=int, default=16, help="beam positions of --profile-batch")
+    ap.add_argument("--time-batch", action="store_true",
+                    help="time the FP32 batch of the 60-solve workload alone (forward and adjoint sweeps, rooflines)")
     ap.add_argument("--profile-budget-gb", type=float, default=6.0, help="tape budget of --profile-batch")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="energy steps of --profile-3d (0: the stable step count; fewer steps exceed the "
@@ -764,6 +766,76 @@ def run_profile(args):
                       "fp64": h.info().forward_kernels + h.info().adjoint_kernels}))
     h.close()
     h32.close()
+
+
+def run_time_batch(args):
+    """The FP32 batch of the 60-solve 2D workload alone: forward and adjoint sweeps timed with CUDA
+    events over --steps after --warmup, with the sweeps' HBM rooflines (a quick kernel check)."""
+    import torch
+    from pnepma_gb300 import capi
+    from pnepma_gb300.problem import PN_FP32
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    solves = workload(args.positions)
+    descs, keep = [], []
+    for s in solves:
+        s.problem.precision = PN_FP32
+        d, k = s.problem.descriptor(s.x_rays)
+        descs.append(d)
+        keep.append(k)
+    n = len(solves)
+    rho, noa, acs = solves[0].inputs()
+    nr = len(solves[0].x_rays)
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)
+    free_b, _ = torch.cuda.mem_get_info(dev)
+    b = capi.Batch(descs, keep, memory_budget=int(0.9 * free_b))
+    sz = capi.query_sizes(descs[0])
+    I = torch.zeros((n, nr), dtype=torch.float64, device=dev)
+    ib = torch.ones((n, nr), dtype=torch.float64, device=dev)
+    rb = [torch.zeros(sz.n_rho, dtype=torch.float64, device=dev) for _ in range(n)]
+    nb = [torch.zeros(sz.n_noa, dtype=torch.float64, device=dev) for _ in range(n)]
+    ab = [torch.zeros(sz.n_acs, dtype=torch.float64, device=dev) for _ in range(n)]
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fwd, adj = [], []
+    for it in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            b.forward([d_rho.data_ptr()] * n, [d_noa.data_ptr()] * n, [d_acs.data_ptr()] * n,
+                      [I[i].data_ptr() for i in range(n)], sp)
+            e1.record(stream)
+            if it == 0:
+                stream.synchronize()
+                ib.copy_(1.0 / I.abs())
+            b.adjoint([ib[i].data_ptr() for i in range(n)], [t.data_ptr() for t in rb], [t.data_ptr() for t in nb],
+                      [t.data_ptr() for t in ab], sp)
+            e2.record(stream)
+        stream.synchronize()
+        if it >= args.warmup:
+            fwd.append(e0.elapsed_time(e1))
+            adj.append(e1.elapsed_time(e2))
+    info = b.info()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    fb, _m = algorithmic_bytes_per_step(solves[0], 4, fused=info.tma_groups > 0)
+    fwd_bytes = fb * sum(s.problem.N_steps for s in solves)
+    adj_bytes = sum(s.problem.N_steps * algorithmic_bytes_adjoint_step(s, 4) for s in solves) + info.recomputed_steps * fb
+    f_ms, a_ms = float(np.mean(fwd)), float(np.mean(adj))
+    print(json.dumps({"time_batch": n, "forward_ms": f_ms, "adjoint_ms": a_ms, "solves_per_s": n / ((f_ms + a_ms) / 1e3),
+                      "forward_gbs": fwd_bytes / f_ms / 1e6, "forward_frac": fwd_bytes / f_ms / 1e6 / peak,
+                      "adjoint_gbs": adj_bytes / a_ms / 1e6, "adjoint_frac": adj_bytes / a_ms / 1e6 / peak,
+                      "stride": info.checkpoint_stride, "recomputed_steps": info.recomputed_steps,
+                      "kernels": info.forward_kernels + info.adjoint_kernels,
+                      "I0": I[0].tolist()}), flush=True)
+    b.close()
 
 
 def run_profile_batch(args):
@@ -1482,6 +1554,8 @@ def main():
         run_profile(args)
     elif args.profile_batch:
         run_profile_batch(args)
+    elif args.time_batch:
+        run_time_batch(args)
     elif args.profile_3d:
         run_profile_3d(args)
     elif args.serve:

@@ -940,8 +940,8 @@ class BatchGroup : public BatchGroupBase {
       if (occ_i < 1) return PN_OK;
       tma_int_grid = occ_i * sms;
       int occ_f = 0, occ_a = 0;
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, TB, LY::SMEM));
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, TB, LY::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, NTS, LY::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, NTS, LY::SMEM));
       if (occ_f < 1 || occ_a < 1) return PN_OK;
       tma_grid[0] = occ_f * sms;
       tma_grid[1] = occ_a * sms;
@@ -1428,9 +1428,9 @@ class BatchGroup : public BatchGroupBase {
         a.K = K;
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
         if (adj)
-          batch_tma_kernel<N, true, DIMS><<<grid, TB, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
+          batch_tma_kernel<N, true, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
         else
-          batch_tma_kernel<N, false, DIMS><<<grid, TB, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
+          batch_tma_kernel<N, false, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }

@@ -41,6 +41,10 @@ constexpr int TX = 32;              // tile width (points)
 #endif
 constexpr int TY = PN_TMA_TY;
 constexpr int TB = TX * TY;
+// the sub-step kernel updates two x-neighbouring points per thread with two-lane FP32
+// instructions (pn_f32x2.cuh): NTS threads per tile; the density integral keeps one point per thread
+constexpr int PPT = 2;
+constexpr int NTS = TB / PPT;
 constexpr int BW = TX + 8;          // neighbour box width: x0 - 4 .. x0 + 35 (a multiple of 4 floats)
 constexpr int XO = 4;               // the tile's first point in a neighbour box
 constexpr int PLO = TX * TY;        // floats per moment plane of a target / density box
@@ -369,7 +373,7 @@ __device__ __forceinline__ void tma_issue(const TLaunch<N>& L, const TTile& tt, 
 // they are never written to memory.  All threads call this; the caller syncs before reading.
 //   own: [n(C)][TY][TX], xb: [n(C^4)][TY][BW] (from x0 - 4), yb: [n(C^2)][TY+1][BW],
 //   zb: [n(C^1)][2][TY][TX]
-template <int N, int C, int KIND, int DIMS>
+template <int N, int C, int KIND, int DIMS, int NT>
 __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, const float* own,
                                             float* xb, float* yb, float* zb, double bc) {
   constexpr bool ADJ = KIND == 1;
@@ -392,7 +396,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
         const int gcol = left ? XO : ncx - tt.x0 + XO;
         const int icol = left ? XO + 1 : ncx - 1 - tt.x0 + XO;
         const bool src = !ADJ && !left;
-        for (int w = threadIdx.x; w < ey * nf; w += TB) {
+        for (int w = threadIdx.x; w < ey * nf; w += NT) {
           const int ty = w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
@@ -419,7 +423,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
         const int crow = left ? 0 : ey - 1;   // the face cells' row in the target box
         const int grow = left ? 0 : ey;       // the ghost row in the y box
         const int irow = left ? 1 : ey - 1;   // the first interior row of F
-        for (int w = threadIdx.x; w < nx * nf; w += TB) {
+        for (int w = threadIdx.x; w < nx * nf; w += NT) {
           const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
@@ -443,7 +447,7 @@ __device__ __forceinline__ void tile_ghosts(const BInst<float>& I, const TSolve&
         // every target point of the tile is on the face; the ghost plane and F's first interior
         // plane are the two planes of the z box
         const int gpl = left ? 0 : 1, ipl = left ? 1 : 0;
-        for (int w = threadIdx.x; w < ey * nx * nf; w += TB) {
+        for (int w = threadIdx.x; w < ey * nx * nf; w += NT) {
           const int r = w / (ey * nx), rest = w % (ey * nx);
           const int ty = rest / nx, tx = xv0 + rest % nx;
           float bv = 0.0f;
@@ -463,8 +467,8 @@ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
 // every lane keep half of its values and add its partner's copy of that half, so V values cost
 // V - 1 adds; the remaining lane bits then reduce the one value left.  Lane l ends with the sum of
 // value (l >> (5 - log2 V)); the first lane of each group writes it to red[w][value].
-template <int V>
-__device__ __forceinline__ void warp_partials(double* v, int lane, int w, int pr, double (&red)[TB / 32][MAXR]) {
+template <int V, int W>
+__device__ __forceinline__ void warp_partials(double* v, int lane, int w, int pr, double (&red)[W][MAXR]) {
   constexpr int levels = ilog2c(V);
   int base = 0;
 #pragma unroll
@@ -541,91 +545,196 @@ __device__ __forceinline__ void staged_advection(float* acc, const float* xn, co
   }
 }
 
+// The advection sum of the two points (tx, tx + 1) of a thread, two lanes per instruction: each
+// lane is staged_advection's arithmetic for its point.  x neighbours: the pair reads three
+// consecutive values of the neighbour box (the right value of the first point is the left value
+// of the second); y and z neighbours: aligned pairs.
+template <int N, int C, bool NEG, int DIMS>
+__device__ __forceinline__ void staged_advection2(f2* acc, const float* xn, const float* yn, const float* zn,
+                                                  int xr, int xl, int yr, int yl, int zo, const TSolve& I) {
+  {
+    constexpr int F = C ^ 4;
+    constexpr bool oddx = (C >> 2) & 1;   // then xr is even, else xl is
+    if constexpr (Ord<N>::n(F) > 0) {
+      const f2 ih = splat(I.inv_h[0]);
+      auto diff = [&](int q) -> f2 {
+        f2 a, b;
+        if constexpr (oddx) {
+          a = ld2(xn + q * PL4 + xr);
+          b = f2{xn[q * PL4 + xl], a.x};
+        } else {
+          b = ld2(xn + q * PL4 + xl);
+          a = f2{b.y, xn[q * PL4 + xr + 1]};
+        }
+        const f2 d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> f2 {
+        (void)kk;
+        return splat(float(lit));
+      };
+      Adv<N, C, 0>::template apply<f2>(acc, diff, coef);
+    }
+  }
+  {
+    constexpr int F = C ^ 2;
+    if constexpr (Ord<N>::n(F) > 0) {
+      const f2 ih = splat(I.inv_h[1]);
+      auto diff = [&](int q) -> f2 {
+        const f2 a = ld2(yn + q * PL5 + yr);
+        const f2 b = ld2(yn + q * PL5 + yl);
+        const f2 d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> f2 {
+        (void)kk;
+        return splat(float(lit));
+      };
+      Adv<N, C, 1>::template apply<f2>(acc, diff, coef);
+    }
+  }
+  if constexpr (DIMS == 7) {
+    constexpr int F = C ^ 1;
+    if constexpr (Ord<N>::n(F) > 0) {
+      const f2 ih = splat(I.inv_h[2]);
+      auto diff = [&](int q) -> f2 {
+        const f2 a = ld2(zn + q * PLZ + PLO + zo);
+        const f2 b = ld2(zn + q * PLZ + zo);
+        const f2 d = NEG ? (b - a) : (a - b);
+        return d * ih;
+      };
+      auto coef = [&](int kk, double lit) -> f2 {
+        (void)kk;
+        return splat(float(lit));
+      };
+      Adv<N, C, 2>::template apply<f2>(acc, diff, coef);
+    }
+  }
+}
+
+// cl_sums for two lanes (the same sums in the same order per lane)
+template <int N, unsigned MASK, int NE>
+__device__ __forceinline__ void cl_sums2_n(const f2* rr, const float (*c)[N + 1], f2* Cl) {
+#pragma unroll
+  for (int l = 0; l <= N; ++l) {
+    f2 cc = splat(0.0f);
+    if ((MASK >> l) & 1u) {
+#pragma unroll
+      for (int e = 0; e < NE; ++e) cc = fma(rr[e], splat(c[e][l]), cc);
+    }
+    Cl[l] = cc;
+  }
+}
+
+template <int N, unsigned MASK>
+__device__ __forceinline__ void cl_sums2(const f2* rr, const float (*c)[N + 1], int ne, f2* Cl) {
+  switch (ne) {
+    case 1: cl_sums2_n<N, MASK, 1>(rr, c, Cl); break;
+    case 2: cl_sums2_n<N, MASK, 2>(rr, c, Cl); break;
+    case 3: cl_sums2_n<N, MASK, 3>(rr, c, Cl); break;
+    default: cl_sums2_n<N, MASK, MAXE>(rr, c, Cl); break;
+  }
+}
+
 // One update of a staged tile: substep_cell's arithmetic with operands from shared memory; the new
 // values replace the old ones in the target box.  `ar` holds the step's coefficients, `dt` its
 // (half or full) energy step.  With `settle`, thread 0 waits for the reads of the tile's earlier
 // store after the ghosts are formed and before the target box is written.
 template <int N, int C, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                           double (&red)[TB / 32][MAXR], const ArgRow<N>& ar, float dt,
+                                           double (&red)[NTS / 32][MAXR], const ArgRow<N>& ar, float dt,
                                            bool settle) {
   using LY = TmaLayout<N, DIMS>;
   constexpr int n = Ord<N>::n(C);
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   float* own = reinterpret_cast<float*>(st + LY::OWN);
-  tile_ghosts<N, C, ADJ ? 1 : 0, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
-                                       reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
-                                       ADJ ? 0.0 : ar.bc);
+  tile_ghosts<N, C, ADJ ? 1 : 0, DIMS, NTS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                                            reinterpret_cast<float*>(st + LY::YN),
+                                            reinterpret_cast<float*>(st + LY::ZN), ADJ ? 0.0 : ar.bc);
   if (settle && threadIdx.x == 0) bulk_wait_read();
   __syncthreads();
   const float* xn = reinterpret_cast<const float*>(st + LY::XN);
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
   const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
-  const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+  // this thread's points: (tx, ty) and (tx + 1, ty)
+  const int tx = PPT * (threadIdx.x % (TX / PPT)), ty = threadIdx.x / (TX / PPT);
   const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
-  const bool valid = tx >= xv0 && tx < xv1 && ty < ey;
+  const bool v0 = tx >= xv0 && tx < xv1 && ty < ey;
+  const bool v1 = tx + 1 >= xv0 && tx + 1 < xv1 && ty < ey;
   const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
   double part[MAXR];
 #pragma unroll
   for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
   if constexpr (n > 0) {
-    if (valid) {
+    if (v0 || v1) {
       const int i = tt.x0 + tx, j = tt.y0 + ty;
-      const int lo = ty * TX + tx;                              // the point in the target / density / z boxes
-      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
+      const int lo = ty * TX + tx;                              // the pair in the target / density / z boxes
+      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours of the first point
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;          // rows j, j - 1 (odd) or j + 1, j of the y box
-      // the eee cell's per-line weights (intensity or adjoint source), loaded before the stencil
+      // the eee cells' per-line weights (intensity or adjoint source), loaded before the stencil
       // so that their latency overlaps it
       long long ce = 0;
-      double wl[MAXR];
+      double wl0[MAXR], wl1[MAXR];
       if constexpr (C == 0) {
         ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
         const double* wsrc = ADJ ? I.wsrc : I.wint;
+        const bool use = ADJ || want_part;
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r) wl[r] = (r < I.nr && (ADJ || want_part)) ? wsrc[ce * I.nr + r] : 0.0;
+        for (int r = 0; r < MAXR; ++r) {
+          wl0[r] = (r < I.nr && use && v0) ? wsrc[ce * I.nr + r] : 0.0;
+          wl1[r] = (r < I.nr && use && v1) ? wsrc[(ce + 1) * I.nr + r] : 0.0;
+        }
       }
-      float acc[n];
+      f2 acc[n];
 #pragma unroll
-      for (int m = 0; m < n; ++m) acc[m] = 0.0f;
-      staged_advection<N, C, ADJ, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
-      float rr[MAXE];
-      float S = 0.0f;
+      for (int m = 0; m < n; ++m) acc[m] = splat(0.0f);
+      staged_advection2<N, C, ADJ, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
+      f2 rr[MAXE];
+      f2 S = splat(0.0f);
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
-        rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
-        S = fmaf(rr[e], ar.s[e], S);
+        rr[e] = e < tt.ne ? ld2(rh + e * PLO + lo) : splat(0.0f);
+        S = fma(rr[e], splat(ar.s[e]), S);
       }
-      const float invS = recip(S);
-      const float dts = dt * invS;
+      const f2 invS{recip(S.x), recip(S.y)};
+      const f2 dts = splat(dt) * invS;
       constexpr unsigned mask = Ord<N>::deg_mask(C);
-      float Cl[N + 1];
-      float gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
-      cl_sums<float, N, mask>(rr, ar.c, tt.ne, Cl);
+      f2 Cl[N + 1];
+      f2 gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
+      cl_sums2<N, mask>(rr, ar.c, tt.ne, Cl);
 #pragma unroll
-      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(-(Cl[l] * dts)) : 0.0f;
-      float q0 = 0.0f;
+      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(neg(Cl[l] * dts)) : splat(0.0f);
+      f2 q0 = splat(0.0f);
       if constexpr (ADJ && C == 0) {
-        double q = 0.0;
+        double qa = 0.0, qb = 0.0;
 #pragma unroll
         for (int r = 0; r < MAXR; ++r)
-          if (r < I.nr) q = fma(-ar.sig[r], wl[r], q);
-        q0 = float(q);
+          if (r < I.nr) {
+            qa = fma(-ar.sig[r], wl0[r], qa);
+            qb = fma(-ar.sig[r], wl1[r], qb);
+          }
+        q0 = f2{float(qa), float(qb)};
       }
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
-        const float u = own[m * PLO + lo];
-        const float q = (m == 0) ? q0 : 0.0f;
-        const float num = (q - acc[m]) - Cl[l] * u;
-        const float unew = fmaf(num, gl[l], u);
-        own[m * PLO + lo] = unew;
+        const f2 u = ld2(own + m * PLO + lo);
+        const f2 q = (m == 0) ? q0 : splat(0.0f);
+        const f2 num = fma(neg(Cl[l]), u, q - acc[m]);   // (q - A u) - C_l u
+        f2 unew = fma(num, gl[l], u);
+        if (!v0) unew.x = u.x;   // lanes outside the target cells keep their loaded values
+        if (!v1) unew.y = u.y;
+        st2(own + m * PLO + lo, unew);
         if constexpr (C == 0 && !ADJ) {
           if (m == 0 && want_part) {
 #pragma unroll
             for (int r = 0; r < MAXR; ++r)
-              if (r < I.nr) part[r] += wl[r] * double(unew);
+              if (r < I.nr) {
+                if (v0) part[r] += wl0[r] * double(unew.x);
+                if (v1) part[r] += wl1[r] * double(unew.y);
+              }
           }
         }
       }
@@ -643,7 +752,7 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
     if (threadIdx.x < L.pr) {
       double v = 0.0;
 #pragma unroll
-      for (int q = 0; q < TB / 32; ++q) v += red[q][threadIdx.x];
+      for (int q = 0; q < NTS / 32; ++q) v += red[q][threadIdx.x];
       L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
     }
   }
@@ -665,7 +774,7 @@ __device__ __forceinline__ void tma_store_target(const TLaunch<N>& L, const TTil
 
 template <int N, int C, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[TB / 32][MAXR]) {
+                                         double (&red)[NTS / 32][MAXR]) {
   using LY = TmaLayout<N, DIMS>;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   const ArgRow<N>* rows = reinterpret_cast<const ArgRow<N>*>(st + LY::ARG);
@@ -696,7 +805,7 @@ __device__ __forceinline__ void tma_cell(const TLaunch<N>& L, const TTile& tt, u
 
 template <int N, bool ADJ, int DIMS>
 __device__ __forceinline__ void tma_cell_of(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                            double (&red)[TB / 32][MAXR]) {
+                                            double (&red)[NTS / 32][MAXR]) {
   if constexpr (DIMS == 7) {
     switch (tt.cls) {
       case 0: tma_cell<N, 0, ADJ, DIMS>(L, tt, st, red); break;
@@ -719,11 +828,11 @@ __device__ __forceinline__ void tma_cell_of(const TLaunch<N>& L, const TTile& tt
 }
 
 template <int N, bool ADJ, int DIMS>
-__global__ void __launch_bounds__(TB, PN_TMA_MINB) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
+__global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
   using LY = TmaLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
-  __shared__ double red[TB / 32][MAXR];
+  __shared__ double red[NTS / 32][MAXR];
   // tensor copies need 128-byte aligned destinations: refuse (uniformly) rather than fault
   if ((smem_u32(smem) & 127u) != 0u) {
     if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
@@ -846,7 +955,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   double* rbs = reinterpret_cast<double*>(st + LY::RBAR);
   {
     const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, 2, DIMS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+    tile_ghosts<N, C, 2, DIMS, TB>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
                                reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN), ar0.bc);
     __syncthreads();
   }

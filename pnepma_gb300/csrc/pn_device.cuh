@@ -27,6 +27,7 @@
 #include <stdint.h>
 
 #include "generated/pn_stencils.cuh"
+#include "pn_f32x2.cuh"
 
 namespace pn {
 
@@ -166,11 +167,33 @@ __device__ __forceinline__ double phi1(double c) {
 // (truncation below 2e-9 relative); otherwise the fast exponential and division (ex2.approx-based
 // __expf, __fdividef), whose relative error is ~1e-6 at |c| = 1/4, where e^c - 1 cancels most,
 // and smaller beyond.  pn_selftest_phi1 compares it with expm1f(c) / c on the device.
+// The Horner steps are written as explicit FMAs so that the scalar form and the two-lane form
+// (phi1 of an f2, the tile kernels) round identically.
+__device__ __forceinline__ float phi1_series(float c) {
+  float t = fmaf(c, 1.0f / 5040.0f, 1.0f / 720.0f);
+  t = fmaf(c, t, 1.0f / 120.0f);
+  t = fmaf(c, t, 1.0f / 24.0f);
+  t = fmaf(c, t, 1.0f / 6.0f);
+  t = fmaf(c, t, 0.5f);
+  return fmaf(c, t, 1.0f);
+}
+
 __device__ __forceinline__ float phi1(float c) {
-  const float t = 1.0f + c * (0.5f + c * (1.0f / 6.0f + c * (1.0f / 24.0f + c * (1.0f / 120.0f +
-                  c * (1.0f / 720.0f + c * (1.0f / 5040.0f))))));
-  if (fabsf(c) <= 0.25f) return t;
+  if (fabsf(c) <= 0.25f) return phi1_series(c);
   return __fdividef(__expf(c) - 1.0f, c);
+}
+
+// both lanes of an f2: the series on both at once, a lane beyond 1/4 by the scalar form
+__device__ __forceinline__ f2 phi1(f2 c) {
+  f2 t = fma(c, splat(1.0f / 5040.0f), splat(1.0f / 720.0f));
+  t = fma(c, t, splat(1.0f / 120.0f));
+  t = fma(c, t, splat(1.0f / 24.0f));
+  t = fma(c, t, splat(1.0f / 6.0f));
+  t = fma(c, t, splat(0.5f));
+  t = fma(c, t, splat(1.0f));
+  if (fabsf(c.x) > 0.25f) t.x = __fdividef(__expf(c.x) - 1.0f, c.x);
+  if (fabsf(c.y) > 0.25f) t.y = __fdividef(__expf(c.y) - 1.0f, c.y);
+  return t;
 }
 
 // the reference form in FP32, for the self-test
@@ -531,7 +554,7 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
       if constexpr (DIMS != 0) u = upre[m];
       else u = uo[m * gt.ms];
       const T q = (m == 0) ? q0 : T(0);
-      const T num = (q - acc[m]) - Cl[l] * u;
+      const T num = fma(-Cl[l], u, q - acc[m]);   // (q - A u) - C_l u
       const T unew = fma(num, gl[l], u);
       un[m * gt.ms] = unew;
       if constexpr (C == 0 && !ADJ) {
