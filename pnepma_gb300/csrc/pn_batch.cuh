@@ -936,7 +936,7 @@ class BatchGroup : public BatchGroupBase {
       PN_CUDA(cudaFuncSetAttribute(batch_tma_int_kernel<N, DIMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    LI::SMEM));
       int occ_i = 0;
-      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_i, batch_tma_int_kernel<N, DIMS>, TB, LI::SMEM));
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_i, batch_tma_int_kernel<N, DIMS>, NTS, LI::SMEM));
       if (occ_i < 1) return PN_OK;
       tma_int_grid = occ_i * sms;
       int occ_f = 0, occ_a = 0;
@@ -1459,7 +1459,7 @@ class BatchGroup : public BatchGroupBase {
         a.n_tiles = nb;
         a.it = j;
         a.K = K;
-        batch_tma_int_kernel<N, DIMS><<<std::min(nb, tma_int_grid), TB, TmaIntLayout<N, DIMS>::SMEM, ls>>>(a);
+        batch_tma_int_kernel<N, DIMS><<<std::min(nb, tma_int_grid), NTS, TmaIntLayout<N, DIMS>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
       }

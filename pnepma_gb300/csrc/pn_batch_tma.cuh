@@ -904,14 +904,14 @@ template <int N, int DIMS>
 struct TmaIntLayout {
   using B = TmaLayout<N, DIMS>;
   static constexpr int NO = B::NO;
+  // the tape state's target box and its neighbours, the densities; the adjoint state and rho_bar
+  // are read (and rho_bar written) per point from global memory
   static constexpr int OWN = 0;
-  static constexpr int LAM = OWN + B::al(NO * PLO * 4);
-  static constexpr int XN = LAM + B::al(NO * PLO * 4);
+  static constexpr int XN = OWN + B::al(NO * PLO * 4);
   static constexpr int YN = XN + B::al(NO * PL4 * 4);
   static constexpr int ZN = YN + B::al(NO * PL5 * 4);
   static constexpr int RHO = ZN + (DIMS == 7 ? B::al(NO * PLZ * 4) : 0);
-  static constexpr int RBAR = RHO + B::al(MAXE * PLO * 4);   // FP64
-  static constexpr int ARG = RBAR + B::al(MAXE * PLO * 8);
+  static constexpr int ARG = RHO + B::al(MAXE * PLO * 4);
   static constexpr int TIL = ARG + (int)sizeof(IntRow<N>);
   static constexpr int SOL = TIL + (int)sizeof(TTile);
   static constexpr int STAGE = B::al(SOL + (int)sizeof(TSolve));
@@ -926,20 +926,18 @@ __device__ __forceinline__ void tma_issue_int(const TILaunch<N>& L, const TTile&
   const int n_own = class_moments<N>(c), n_x = class_moments<N>(cx), n_y = class_moments<N>(cy);
   const int n_z = DIMS == 7 ? class_moments<N>(cz) : 0;
   const int slot = slot_index(tt.ns, tt.n_full, tt.n_ck, L.it, L.K, true);
-  const unsigned bytes = 4u * (unsigned)(2 * PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
-                         8u * (unsigned)(PLO * tt.ne) + (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
+  const unsigned bytes = 4u * (unsigned)(PLO * n_own + PL4 * n_x + PL5 * n_y + PLZ * n_z + PLO * tt.ne) +
+                         (unsigned)(sizeof(IntRow<N>) + sizeof(TTile) + sizeof(TSolve));
   const int ya = tt.y0 - ((c >> 1) & 1);
   const int za = tt.z - (c & 1);
   const int xa = tt.x0 - XO;
   mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
   tma_load_5d(st + LY::OWN, mp + c * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, bar);
-  tma_load_4d(st + LY::LAM, mp + c * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
   if (n_x > 0) tma_load_5d(st + LY::XN, mp + cx * TM_KINDS + TM_ST_X, xa, tt.y0, tt.z, 0, slot, bar);
   if (n_y > 0) tma_load_5d(st + LY::YN, mp + cy * TM_KINDS + TM_ST_Y, tt.x0, ya, tt.z, 0, slot, bar);
   if (n_z > 0) tma_load_5d(st + LY::ZN, mp + cz * TM_KINDS + TM_ST_Z, tt.x0, tt.y0, za, 0, slot, bar);
   tma_load_4d(st + LY::RHO, mp + c * TM_KINDS + TM_RHO, tt.x0, tt.y0, tt.z, 0, bar);
-  tma_load_4d(st + LY::RBAR, mp + c * TM_KINDS + TM_RBAR, tt.x0, tt.y0, tt.z, 0, bar);
   bulk_load(st + LY::ARG, L.rows + tt.arg_int + L.it, (unsigned)sizeof(IntRow<N>), bar);
   bulk_load(st + LY::TIL, &tt, (unsigned)sizeof(TTile), bar);
   bulk_load(st + LY::SOL, L.solves + tt.inst, (unsigned)sizeof(TSolve), bar);
@@ -952,18 +950,20 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
   constexpr bool oddx = (C >> 2) & 1;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
   const float* own = reinterpret_cast<const float*>(st + LY::OWN);
-  double* rbs = reinterpret_cast<double*>(st + LY::RBAR);
   {
     const IntRow<N>& ar0 = *reinterpret_cast<const IntRow<N>*>(st + LY::ARG);
-    tile_ghosts<N, C, 2, DIMS, TB>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
-                               reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN), ar0.bc);
+    tile_ghosts<N, C, 2, DIMS, NTS>(L.inst[tt.inst], I, tt, own, reinterpret_cast<float*>(st + LY::XN),
+                                    reinterpret_cast<float*>(st + LY::YN), reinterpret_cast<float*>(st + LY::ZN),
+                                    ar0.bc);
     __syncthreads();
   }
   if constexpr (n > 0) {
-    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    // this thread's points: (tx, ty) and (tx + 1, ty), two lanes per instruction
+    const int tx = PPT * (threadIdx.x % (TX / PPT)), ty = threadIdx.x / (TX / PPT);
     const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
-    if (tx >= xv0 && tx < xv1 && ty < ey) {
-      const float* lam = reinterpret_cast<const float*>(st + LY::LAM);
+    const bool v0 = tx >= xv0 && tx < xv1 && ty < ey;
+    const bool v1 = tx + 1 >= xv0 && tx + 1 < xv1 && ty < ey;
+    if (v0 || v1) {
       const float* xn = reinterpret_cast<const float*>(st + LY::XN);
       const float* yn = reinterpret_cast<const float*>(st + LY::YN);
       const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
@@ -973,68 +973,86 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const int lo = ty * TX + tx;
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;
-      // the eee cell's line sums, loaded before the stencil so that their latency overlaps it
+      // the pair's place in the class's device layout (x fastest, pitch px); x is even, so the
+      // adjoint state's pairs are 8-byte and rho_bar's 16-byte aligned
+      const long long p = ((long long)tt.z * I.n1[C] + j) * I.px[C] + i;
+      const long long ms = I.ms[C];
+      // the adjoint state of the pair, loaded before the stencil so that its latency overlaps it
+      const float* la = I.lam + I.dev_off[C] + p;
+      f2 lam[n];
+#pragma unroll
+      for (int m = 0; m < n; ++m) lam[m] = ld2(la + m * ms);
+      // the eee cells' line sums
       long long ce = 0;
-      double wl[MAXR];
+      double wl0[MAXR], wl1[MAXR];
       if constexpr (C == 0) {
         ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r) wl[r] = r < I.nr ? I.wsum[ce * I.nr + r] : 0.0;
+        for (int r = 0; r < MAXR; ++r) {
+          wl0[r] = (r < I.nr && v0) ? I.wsum[ce * I.nr + r] : 0.0;
+          wl1[r] = (r < I.nr && v1) ? I.wsum[(ce + 1) * I.nr + r] : 0.0;
+        }
       }
-      float acc[n];
+      f2 acc[n];
 #pragma unroll
-      for (int m = 0; m < n; ++m) acc[m] = 0.0f;
-      staged_advection<N, C, false, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
-      float rr[MAXE];
-      float S = 0.0f;
+      for (int m = 0; m < n; ++m) acc[m] = splat(0.0f);
+      staged_advection2<N, C, false, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
+      f2 rr[MAXE];
+      f2 S = splat(0.0f);
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
-        rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
-        S = fmaf(rr[e], ar.s[e], S);
+        rr[e] = e < tt.ne ? ld2(rh + e * PLO + lo) : splat(0.0f);
+        S = fma(rr[e], splat(ar.s[e]), S);
       }
-      const float invS = recip(S);
+      const f2 invS{recip(S.x), recip(S.y)};
       constexpr unsigned mask = Ord<N>::deg_mask(C);
-      float Cl[N + 1];
-      cl_sums<float, N, mask>(rr, ar.c, tt.ne, Cl);
-      float P = 0.0f;
-      float R[N + 1];
+      f2 Cl[N + 1];
+      cl_sums2<N, mask>(rr, ar.c, tt.ne, Cl);
+      f2 P = splat(0.0f);
+      f2 R[N + 1];
 #pragma unroll
-      for (int l = 0; l <= N; ++l) R[l] = 0.0f;
+      for (int l = 0; l <= N; ++l) R[l] = splat(0.0f);
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
-        const float u = own[m * PLO + lo];
-        const float lm = lam[m * PLO + lo];
-        P = fmaf(lm, -acc[m] - Cl[l] * u, P);   // 1/S applied once, below (integrate_cell's order)
-        R[l] = fmaf(lm, u, R[l]);
+        const f2 u = ld2(own + m * PLO + lo);
+        P = fma(lam[m], fma(neg(Cl[l]), u, neg(acc[m])), P);   // 1/S applied once, below (integrate_cell's order)
+        R[l] = fma(lam[m], u, R[l]);
       }
-      P *= invS;
+      P = P * invS;
+      double* rb = I.rbar[C] + p;
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
         if (e < tt.ne) {
           // this step's increment in FP32, accumulated in FP64 (integrate_cell's arithmetic)
-          float v = ar.s[e] * P;
+          f2 v = splat(ar.s[e]) * P;
 #pragma unroll
           for (int l = 0; l <= N; ++l)
-            if ((mask >> l) & 1u) v += ar.c[e][l] * R[l];
-          const double old = rbs[e * PLO + lo];   // this point's rho_bar, staged with the tile
-          rbs[e * PLO + lo] = old + double(v) * ar.wfac;
+            if ((mask >> l) & 1u) v = fma(splat(ar.c[e][l]), R[l], v);
+          double* q = rb + e * ms;
+          if (v0 && v1) {
+            double2 o = *reinterpret_cast<const double2*>(q);
+            o.x = fma(double(v.x), ar.wfac, o.x);
+            o.y = fma(double(v.y), ar.wfac, o.y);
+            *reinterpret_cast<double2*>(q) = o;
+          } else if (v0) {
+            q[0] = fma(double(v.x), ar.wfac, q[0]);
+          } else {
+            q[1] = fma(double(v.y), ar.wfac, q[1]);
+          }
         }
       }
       if constexpr (C == 0) {
-        const double u0 = double(own[lo]);
 #pragma unroll
         for (int r = 0; r < MAXR; ++r)
-          if (r < I.nr) I.wsum[ce * I.nr + r] = fma(ar.coef[r], u0, wl[r]);
+          if (r < I.nr) {
+            if (v0) I.wsum[ce * I.nr + r] = fma(ar.coef[r], double(own[lo]), wl0[r]);
+            if (v1) I.wsum[(ce + 1) * I.nr + r] = fma(ar.coef[r], double(own[lo + 1]), wl1[r]);
+          }
       }
     }
   }
-  __syncthreads();   // the rho_bar box holds the new values
-  if (threadIdx.x == 0) {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tma_store_4d(L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS + TM_RBAR, tt.x0, tt.y0, tt.z, 0, rbs);
-    bulk_commit();
-  }
+  __syncthreads();   // the stage is reused by the next tile
 }
 
 template <int N, int DIMS>
@@ -1061,7 +1079,7 @@ __device__ __forceinline__ void tma_int_cell_of(const TILaunch<N>& L, const TTil
 }
 
 template <int N, int DIMS>
-__global__ void __launch_bounds__(TB, 2) batch_tma_int_kernel(const __grid_constant__ TILaunch<N> L) {
+__global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_int_kernel(const __grid_constant__ TILaunch<N> L) {
   using LY = TmaIntLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];

@@ -273,6 +273,11 @@ __device__ __forceinline__ long long eee_cell(const Geom& g, int i, int j, int k
   return ((long long)k * g.n[1] + j) * g.n[0] + i;
 }
 
+// rows of a boundary block evaluated together by a face thread
+#ifndef PN_GHOST_ROWS
+#define PN_GHOST_ROWS 7
+#endif
+
 // Ghost of class F = switch(C, d) next to target cell (i,j,k) of class C (C even along d, cell on
 // a face along d).  Writes the ghost into F's storage.  `left` selects the face at index 0.
 template <class T, int N, int C, int D>
@@ -306,15 +311,32 @@ __device__ __forceinline__ void ghost_fill(T* const* rd, const Geom* g, const do
     const double* B = bmat[D][F];
     const bool src = source && D == 0 && !left;
     const double* bm = src ? beam[F] + ((long long)k * gf.n[1] + j) * nf : nullptr;
+    // PN_GHOST_ROWS rows of B v at a time in FP64 (whose long FMA latency the chains would
+    // otherwise expose): independent dot products in flight, each still summed over q in order,
+    // so the values do not depend on the chunking.  FP32 keeps one row (its registers are full).
+    constexpr int RC = sizeof(T) == 8 ? PN_GHOST_ROWS : 1;
 #pragma unroll 1
-    for (int r = 0; r < nf; ++r) {
-      T bv = T(0);
+    for (int r0 = 0; r0 < nf; r0 += RC) {
+      T bv[RC];
 #pragma unroll
-      for (int q = 0; q < nt; ++q) bv = fma(T(B[r * nt + q]), v[q], bv);
-      const T gval = src ? T(bm[r] * bc_scaled) : T(0);
-      const T interior = fi[r * gf.ms];
-      const T gh = left ? T(2) * (gval - bv) - interior : T(2) * (bv + gval) - interior;
-      fg[r * gf.ms] = gh;
+      for (int rr = 0; rr < RC; ++rr) bv[rr] = T(0);
+#pragma unroll
+      for (int q = 0; q < nt; ++q) {
+        const T vq = v[q];
+#pragma unroll
+        for (int rr = 0; rr < RC; ++rr)
+          if (r0 + rr < nf) bv[rr] = fma(T(B[(r0 + rr) * nt + q]), vq, bv[rr]);
+      }
+#pragma unroll
+      for (int rr = 0; rr < RC; ++rr) {
+        const int r = r0 + rr;
+        if (r < nf) {
+          const T gval = src ? T(bm[r] * bc_scaled) : T(0);
+          const T interior = fi[r * gf.ms];
+          const T gh = left ? T(2) * (gval - bv[rr]) - interior : T(2) * (bv[rr] + gval) - interior;
+          fg[r * gf.ms] = gh;
+        }
+      }
     }
   }
 }
@@ -672,7 +694,7 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
         lm = la[m * gt.ms];
       }
       // P = sum_m lambda_m du_m with du = (-A u - C_l u) / S: the 1/S applied once, below
-      P = fma(lm, -acc[m] - Cl[l] * u, P);
+      P = fma(lm, fma(-Cl[l], u, -acc[m]), P);
       R[l] = fma(lm, u, R[l]);
     }
     P *= invS;
@@ -684,8 +706,8 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
         T v = a.s[e] * P;
 #pragma unroll
         for (int l = 0; l <= N; ++l)
-          if ((mask >> l) & 1u) v += a.c[e][l] * R[l];
-        rb[e * gt.ms] += double(v) * a.wfac;
+          if ((mask >> l) & 1u) v = fma(T(a.c[e][l]), R[l], v);
+        rb[e * gt.ms] = fma(double(v), a.wfac, rb[e * gt.ms]);
       }
     }
     if constexpr (C == 0) {
