@@ -41,10 +41,17 @@ constexpr int TX = 32;              // tile width (points)
 #endif
 constexpr int TY = PN_TMA_TY;
 constexpr int TB = TX * TY;
-// the sub-step kernel updates two x-neighbouring points per thread with two-lane FP32
-// instructions (pn_f32x2.cuh): NTS threads per tile; the density integral keeps one point per thread
-constexpr int PPT = 2;
+// points per thread of the sub-step and density-integral tiles: 1, or 2 x-neighbouring points
+// with two-lane FP32 instructions (pn_f32x2.cuh; 36 % fewer instructions, but half the warps per
+// SM within the same shared memory, which measured slower on the 2D P11 workload); NTS threads
+// per tile
+#ifndef PN_TMA_PPT
+#define PN_TMA_PPT 1
+#endif
+constexpr int PPT = PN_TMA_PPT;
 constexpr int NTS = TB / PPT;
+using LN = Lanes<PPT>;
+using LV = LN::V;
 constexpr int BW = TX + 8;          // neighbour box width: x0 - 4 .. x0 + 35 (a multiple of 4 floats)
 constexpr int XO = 4;               // the tile's first point in a neighbour box
 constexpr int PLO = TX * TY;        // floats per moment plane of a target / density box
@@ -488,151 +495,88 @@ __device__ __forceinline__ void warp_partials(double* v, int lane, int w, int pr
   if ((lane & ((32 >> levels) - 1)) == 0 && base < pr) red[w][base] = v[0];
 }
 
-// the advection sum of one point from the staged boxes: x, then y, then z (advection_sum's order)
+// The advection sum of the thread's point(s) from the staged boxes: x, then y, then z
+// (advection_sum's order and arithmetic, lane by lane).  With two points per thread the x
+// neighbours come from three consecutive values of the neighbour box; y and z neighbours are
+// aligned pairs.
 template <int N, int C, bool NEG, int DIMS>
-__device__ __forceinline__ void staged_advection(float* acc, const float* xn, const float* yn, const float* zn,
+__device__ __forceinline__ void staged_advection(LV* acc, const float* xn, const float* yn, const float* zn,
                                                  int xr, int xl, int yr, int yl, int zo, const TSolve& I) {
-  {
-    constexpr int F = C ^ 4;
-    if constexpr (Ord<N>::n(F) > 0) {
-      const float ih = I.inv_h[0];
-      auto diff = [&](int q) -> float {
-        const float a = xn[q * PL4 + xr];
-        const float b = xn[q * PL4 + xl];
-        const float d = NEG ? (b - a) : (a - b);
-        return d * ih;
-      };
-      auto coef = [&](int kk, double lit) -> float {
-        (void)kk;
-        return float(lit);
-      };
-      Adv<N, C, 0>::template apply<float>(acc, diff, coef);
-    }
-  }
-  {
-    constexpr int F = C ^ 2;
-    if constexpr (Ord<N>::n(F) > 0) {
-      const float ih = I.inv_h[1];
-      auto diff = [&](int q) -> float {
-        const float a = yn[q * PL5 + yr];
-        const float b = yn[q * PL5 + yl];
-        const float d = NEG ? (b - a) : (a - b);
-        return d * ih;
-      };
-      auto coef = [&](int kk, double lit) -> float {
-        (void)kk;
-        return float(lit);
-      };
-      Adv<N, C, 1>::template apply<float>(acc, diff, coef);
-    }
-  }
-  if constexpr (DIMS == 7) {
-    constexpr int F = C ^ 1;
-    if constexpr (Ord<N>::n(F) > 0) {
-      const float ih = I.inv_h[2];
-      auto diff = [&](int q) -> float {   // planes: 1 = j (odd) / j + 1 (even), 0 = j - 1 / j
-        const float a = zn[q * PLZ + PLO + zo];
-        const float b = zn[q * PLZ + zo];
-        const float d = NEG ? (b - a) : (a - b);
-        return d * ih;
-      };
-      auto coef = [&](int kk, double lit) -> float {
-        (void)kk;
-        return float(lit);
-      };
-      Adv<N, C, 2>::template apply<float>(acc, diff, coef);
-    }
-  }
-}
-
-// The advection sum of the two points (tx, tx + 1) of a thread, two lanes per instruction: each
-// lane is staged_advection's arithmetic for its point.  x neighbours: the pair reads three
-// consecutive values of the neighbour box (the right value of the first point is the left value
-// of the second); y and z neighbours: aligned pairs.
-template <int N, int C, bool NEG, int DIMS>
-__device__ __forceinline__ void staged_advection2(f2* acc, const float* xn, const float* yn, const float* zn,
-                                                  int xr, int xl, int yr, int yl, int zo, const TSolve& I) {
   {
     constexpr int F = C ^ 4;
     constexpr bool oddx = (C >> 2) & 1;   // then xr is even, else xl is
     if constexpr (Ord<N>::n(F) > 0) {
-      const f2 ih = splat(I.inv_h[0]);
-      auto diff = [&](int q) -> f2 {
-        f2 a, b;
-        if constexpr (oddx) {
-          a = ld2(xn + q * PL4 + xr);
-          b = f2{xn[q * PL4 + xl], a.x};
-        } else {
-          b = ld2(xn + q * PL4 + xl);
-          a = f2{b.y, xn[q * PL4 + xr + 1]};
-        }
-        const f2 d = NEG ? (b - a) : (a - b);
+      const LV ih = LN::splat(I.inv_h[0]);
+      auto diff = [&](int q) -> LV {
+        LV a, b;
+        LN::xpair(xn + q * PL4, xr, xl, oddx, a, b);
+        const LV d = NEG ? (b - a) : (a - b);
         return d * ih;
       };
-      auto coef = [&](int kk, double lit) -> f2 {
+      auto coef = [&](int kk, double lit) -> LV {
         (void)kk;
-        return splat(float(lit));
+        return LN::splat(float(lit));
       };
-      Adv<N, C, 0>::template apply<f2>(acc, diff, coef);
+      Adv<N, C, 0>::template apply<LV>(acc, diff, coef);
     }
   }
   {
     constexpr int F = C ^ 2;
     if constexpr (Ord<N>::n(F) > 0) {
-      const f2 ih = splat(I.inv_h[1]);
-      auto diff = [&](int q) -> f2 {
-        const f2 a = ld2(yn + q * PL5 + yr);
-        const f2 b = ld2(yn + q * PL5 + yl);
-        const f2 d = NEG ? (b - a) : (a - b);
+      const LV ih = LN::splat(I.inv_h[1]);
+      auto diff = [&](int q) -> LV {
+        const LV a = LN::ld(yn + q * PL5 + yr);
+        const LV b = LN::ld(yn + q * PL5 + yl);
+        const LV d = NEG ? (b - a) : (a - b);
         return d * ih;
       };
-      auto coef = [&](int kk, double lit) -> f2 {
+      auto coef = [&](int kk, double lit) -> LV {
         (void)kk;
-        return splat(float(lit));
+        return LN::splat(float(lit));
       };
-      Adv<N, C, 1>::template apply<f2>(acc, diff, coef);
+      Adv<N, C, 1>::template apply<LV>(acc, diff, coef);
     }
   }
   if constexpr (DIMS == 7) {
     constexpr int F = C ^ 1;
     if constexpr (Ord<N>::n(F) > 0) {
-      const f2 ih = splat(I.inv_h[2]);
-      auto diff = [&](int q) -> f2 {
-        const f2 a = ld2(zn + q * PLZ + PLO + zo);
-        const f2 b = ld2(zn + q * PLZ + zo);
-        const f2 d = NEG ? (b - a) : (a - b);
+      const LV ih = LN::splat(I.inv_h[2]);
+      auto diff = [&](int q) -> LV {   // planes: 1 = j (odd) / j + 1 (even), 0 = j - 1 / j
+        const LV a = LN::ld(zn + q * PLZ + PLO + zo);
+        const LV b = LN::ld(zn + q * PLZ + zo);
+        const LV d = NEG ? (b - a) : (a - b);
         return d * ih;
       };
-      auto coef = [&](int kk, double lit) -> f2 {
+      auto coef = [&](int kk, double lit) -> LV {
         (void)kk;
-        return splat(float(lit));
+        return LN::splat(float(lit));
       };
-      Adv<N, C, 2>::template apply<f2>(acc, diff, coef);
+      Adv<N, C, 2>::template apply<LV>(acc, diff, coef);
     }
   }
 }
 
-// cl_sums for two lanes (the same sums in the same order per lane)
+// cl_sums for the thread's lanes (the same sums in the same order per lane)
 template <int N, unsigned MASK, int NE>
-__device__ __forceinline__ void cl_sums2_n(const f2* rr, const float (*c)[N + 1], f2* Cl) {
+__device__ __forceinline__ void cl_sums_lanes_n(const LV* rr, const float (*c)[N + 1], LV* Cl) {
 #pragma unroll
   for (int l = 0; l <= N; ++l) {
-    f2 cc = splat(0.0f);
+    LV cc = LN::splat(0.0f);
     if ((MASK >> l) & 1u) {
 #pragma unroll
-      for (int e = 0; e < NE; ++e) cc = fma(rr[e], splat(c[e][l]), cc);
+      for (int e = 0; e < NE; ++e) cc = fma(rr[e], LN::splat(c[e][l]), cc);
     }
     Cl[l] = cc;
   }
 }
 
 template <int N, unsigned MASK>
-__device__ __forceinline__ void cl_sums2(const f2* rr, const float (*c)[N + 1], int ne, f2* Cl) {
+__device__ __forceinline__ void cl_sums_lanes(const LV* rr, const float (*c)[N + 1], int ne, LV* Cl) {
   switch (ne) {
-    case 1: cl_sums2_n<N, MASK, 1>(rr, c, Cl); break;
-    case 2: cl_sums2_n<N, MASK, 2>(rr, c, Cl); break;
-    case 3: cl_sums2_n<N, MASK, 3>(rr, c, Cl); break;
-    default: cl_sums2_n<N, MASK, MAXE>(rr, c, Cl); break;
+    case 1: cl_sums_lanes_n<N, MASK, 1>(rr, c, Cl); break;
+    case 2: cl_sums_lanes_n<N, MASK, 2>(rr, c, Cl); break;
+    case 3: cl_sums_lanes_n<N, MASK, 3>(rr, c, Cl); break;
+    default: cl_sums_lanes_n<N, MASK, MAXE>(rr, c, Cl); break;
   }
 }
 
@@ -658,83 +602,87 @@ __device__ __forceinline__ void tma_update(const TLaunch<N>& L, const TTile& tt,
   const float* yn = reinterpret_cast<const float*>(st + LY::YN);
   const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
   const float* rh = reinterpret_cast<const float*>(st + LY::RHO);
-  // this thread's points: (tx, ty) and (tx + 1, ty)
+  // this thread's points: (tx + k, ty), k < PPT
   const int tx = PPT * (threadIdx.x % (TX / PPT)), ty = threadIdx.x / (TX / PPT);
   const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
-  const bool v0 = tx >= xv0 && tx < xv1 && ty < ey;
-  const bool v1 = tx + 1 >= xv0 && tx + 1 < xv1 && ty < ey;
+  bool vk[PPT];
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    vk[k] = tx + k >= xv0 && tx + k < xv1 && ty < ey;
+    any = any || vk[k];
+  }
   const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
   double part[MAXR];
 #pragma unroll
   for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
   if constexpr (n > 0) {
-    if (v0 || v1) {
+    if (any) {
       const int i = tt.x0 + tx, j = tt.y0 + ty;
-      const int lo = ty * TX + tx;                              // the pair in the target / density / z boxes
-      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours of the first point
+      const int lo = ty * TX + tx;                              // the point(s) in the target / density / z boxes
+      const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;   // x neighbours: i, i - 1 (odd) or i + 1, i
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;          // rows j, j - 1 (odd) or j + 1, j of the y box
       // the eee cells' per-line weights (intensity or adjoint source), loaded before the stencil
       // so that their latency overlaps it
       long long ce = 0;
-      double wl0[MAXR], wl1[MAXR];
+      double wl[PPT][MAXR];
       if constexpr (C == 0) {
         ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
         const double* wsrc = ADJ ? I.wsrc : I.wint;
         const bool use = ADJ || want_part;
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r) {
-          wl0[r] = (r < I.nr && use && v0) ? wsrc[ce * I.nr + r] : 0.0;
-          wl1[r] = (r < I.nr && use && v1) ? wsrc[(ce + 1) * I.nr + r] : 0.0;
-        }
-      }
-      f2 acc[n];
+        for (int k = 0; k < PPT; ++k)
 #pragma unroll
-      for (int m = 0; m < n; ++m) acc[m] = splat(0.0f);
-      staged_advection2<N, C, ADJ, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
-      f2 rr[MAXE];
-      f2 S = splat(0.0f);
+          for (int r = 0; r < MAXR; ++r) wl[k][r] = (r < I.nr && use && vk[k]) ? wsrc[(ce + k) * I.nr + r] : 0.0;
+      }
+      LV acc[n];
+#pragma unroll
+      for (int m = 0; m < n; ++m) acc[m] = LN::splat(0.0f);
+      staged_advection<N, C, ADJ, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
+      LV rr[MAXE];
+      LV S = LN::splat(0.0f);
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
-        rr[e] = e < tt.ne ? ld2(rh + e * PLO + lo) : splat(0.0f);
-        S = fma(rr[e], splat(ar.s[e]), S);
+        rr[e] = e < tt.ne ? LN::ld(rh + e * PLO + lo) : LN::splat(0.0f);
+        S = fma(rr[e], LN::splat(ar.s[e]), S);
       }
-      const f2 invS{recip(S.x), recip(S.y)};
-      const f2 dts = splat(dt) * invS;
+      const LV invS = LN::rcp(S);
+      const LV dts = LN::splat(dt) * invS;
       constexpr unsigned mask = Ord<N>::deg_mask(C);
-      f2 Cl[N + 1];
-      f2 gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
-      cl_sums2<N, mask>(rr, ar.c, tt.ne, Cl);
+      LV Cl[N + 1];
+      LV gl[N + 1];   // dt phi1_l / S (substep_cell's factors)
+      cl_sums_lanes<N, mask>(rr, ar.c, tt.ne, Cl);
 #pragma unroll
-      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(neg(Cl[l] * dts)) : splat(0.0f);
-      f2 q0 = splat(0.0f);
+      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(LN::neg(Cl[l] * dts)) : LN::splat(0.0f);
+      LV q0 = LN::splat(0.0f);
       if constexpr (ADJ && C == 0) {
-        double qa = 0.0, qb = 0.0;
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r)
-          if (r < I.nr) {
-            qa = fma(-ar.sig[r], wl0[r], qa);
-            qb = fma(-ar.sig[r], wl1[r], qb);
-          }
-        q0 = f2{float(qa), float(qb)};
+        for (int k = 0; k < PPT; ++k) {
+          double q = 0.0;
+#pragma unroll
+          for (int r = 0; r < MAXR; ++r)
+            if (r < I.nr) q = fma(-ar.sig[r], wl[k][r], q);
+          LN::set(q0, k, float(q));
+        }
       }
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
-        const f2 u = ld2(own + m * PLO + lo);
-        const f2 q = (m == 0) ? q0 : splat(0.0f);
-        const f2 num = fma(neg(Cl[l]), u, q - acc[m]);   // (q - A u) - C_l u
-        f2 unew = fma(num, gl[l], u);
-        if (!v0) unew.x = u.x;   // lanes outside the target cells keep their loaded values
-        if (!v1) unew.y = u.y;
-        st2(own + m * PLO + lo, unew);
+        const LV u = LN::ld(own + m * PLO + lo);
+        const LV q = (m == 0) ? q0 : LN::splat(0.0f);
+        const LV num = fma(LN::neg(Cl[l]), u, q - acc[m]);   // (q - A u) - C_l u
+        LV unew = fma(num, gl[l], u);
+#pragma unroll
+        for (int k = 0; k < PPT; ++k)
+          if (!vk[k]) LN::set(unew, k, LN::get(u, k));   // lanes outside the target cells keep their values
+        LN::st(own + m * PLO + lo, unew);
         if constexpr (C == 0 && !ADJ) {
           if (m == 0 && want_part) {
 #pragma unroll
-            for (int r = 0; r < MAXR; ++r)
-              if (r < I.nr) {
-                if (v0) part[r] += wl0[r] * double(unew.x);
-                if (v1) part[r] += wl1[r] * double(unew.y);
-              }
+            for (int k = 0; k < PPT; ++k)
+#pragma unroll
+              for (int r = 0; r < MAXR; ++r)
+                if (r < I.nr && vk[k]) part[r] += wl[k][r] * double(LN::get(unew, k));
           }
         }
       }
@@ -958,12 +906,17 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
     __syncthreads();
   }
   if constexpr (n > 0) {
-    // this thread's points: (tx, ty) and (tx + 1, ty), two lanes per instruction
+    // this thread's points: (tx + k, ty), k < PPT
     const int tx = PPT * (threadIdx.x % (TX / PPT)), ty = threadIdx.x / (TX / PPT);
     const int xv0 = tt.ext & 255, xv1 = (tt.ext >> 8) & 255, ey = (tt.ext >> 16) & 255;
-    const bool v0 = tx >= xv0 && tx < xv1 && ty < ey;
-    const bool v1 = tx + 1 >= xv0 && tx + 1 < xv1 && ty < ey;
-    if (v0 || v1) {
+    bool vk[PPT];
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      vk[k] = tx + k >= xv0 && tx + k < xv1 && ty < ey;
+      any = any || vk[k];
+    }
+    if (any) {
       const float* xn = reinterpret_cast<const float*>(st + LY::XN);
       const float* yn = reinterpret_cast<const float*>(st + LY::YN);
       const float* zn = reinterpret_cast<const float*>(st + LY::ZN);
@@ -973,50 +926,49 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const int lo = ty * TX + tx;
       const int xr = ty * BW + tx + XO + (oddx ? 0 : 1), xl = xr - 1;
       const int yr = (ty + 1) * TX + tx, yl = yr - TX;
-      // the pair's place in the class's device layout (x fastest, pitch px); x is even, so the
-      // adjoint state's pairs are 8-byte and rho_bar's 16-byte aligned
+      // the point(s)' place in the class's device layout (x fastest, pitch px); with two points
+      // x is even, so the adjoint state's pairs are 8-byte and rho_bar's 16-byte aligned
       const long long p = ((long long)tt.z * I.n1[C] + j) * I.px[C] + i;
       const long long ms = I.ms[C];
-      // the adjoint state of the pair, loaded before the stencil so that its latency overlaps it
+      // the adjoint state, loaded before the stencil so that its latency overlaps it
       const float* la = I.lam + I.dev_off[C] + p;
-      f2 lam[n];
+      LV lam[n];
 #pragma unroll
-      for (int m = 0; m < n; ++m) lam[m] = ld2(la + m * ms);
+      for (int m = 0; m < n; ++m) lam[m] = LN::ld(la + m * ms);
       // the eee cells' line sums
       long long ce = 0;
-      double wl0[MAXR], wl1[MAXR];
+      double wl[PPT][MAXR];
       if constexpr (C == 0) {
         ce = ((long long)tt.z * I.n1[0] + j) * I.n0[0] + i;
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r) {
-          wl0[r] = (r < I.nr && v0) ? I.wsum[ce * I.nr + r] : 0.0;
-          wl1[r] = (r < I.nr && v1) ? I.wsum[(ce + 1) * I.nr + r] : 0.0;
-        }
-      }
-      f2 acc[n];
+        for (int k = 0; k < PPT; ++k)
 #pragma unroll
-      for (int m = 0; m < n; ++m) acc[m] = splat(0.0f);
-      staged_advection2<N, C, false, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
-      f2 rr[MAXE];
-      f2 S = splat(0.0f);
+          for (int r = 0; r < MAXR; ++r) wl[k][r] = (r < I.nr && vk[k]) ? I.wsum[(ce + k) * I.nr + r] : 0.0;
+      }
+      LV acc[n];
+#pragma unroll
+      for (int m = 0; m < n; ++m) acc[m] = LN::splat(0.0f);
+      staged_advection<N, C, false, DIMS>(acc, xn, yn, zn, xr, xl, yr, yl, lo, I);
+      LV rr[MAXE];
+      LV S = LN::splat(0.0f);
 #pragma unroll
       for (int e = 0; e < MAXE; ++e) {
-        rr[e] = e < tt.ne ? ld2(rh + e * PLO + lo) : splat(0.0f);
-        S = fma(rr[e], splat(ar.s[e]), S);
+        rr[e] = e < tt.ne ? LN::ld(rh + e * PLO + lo) : LN::splat(0.0f);
+        S = fma(rr[e], LN::splat(ar.s[e]), S);
       }
-      const f2 invS{recip(S.x), recip(S.y)};
+      const LV invS = LN::rcp(S);
       constexpr unsigned mask = Ord<N>::deg_mask(C);
-      f2 Cl[N + 1];
-      cl_sums2<N, mask>(rr, ar.c, tt.ne, Cl);
-      f2 P = splat(0.0f);
-      f2 R[N + 1];
+      LV Cl[N + 1];
+      cl_sums_lanes<N, mask>(rr, ar.c, tt.ne, Cl);
+      LV P = LN::splat(0.0f);
+      LV R[N + 1];
 #pragma unroll
-      for (int l = 0; l <= N; ++l) R[l] = splat(0.0f);
+      for (int l = 0; l <= N; ++l) R[l] = LN::splat(0.0f);
 #pragma unroll
       for (int m = 0; m < n; ++m) {
         const int l = degree_of<N, C>(m);
-        const f2 u = ld2(own + m * PLO + lo);
-        P = fma(lam[m], fma(neg(Cl[l]), u, neg(acc[m])), P);   // 1/S applied once, below (integrate_cell's order)
+        const LV u = LN::ld(own + m * PLO + lo);
+        P = fma(lam[m], fma(LN::neg(Cl[l]), u, LN::neg(acc[m])), P);   // 1/S applied once, below (integrate_cell's order)
         R[l] = fma(lam[m], u, R[l]);
       }
       P = P * invS;
@@ -1025,30 +977,31 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       for (int e = 0; e < MAXE; ++e) {
         if (e < tt.ne) {
           // this step's increment in FP32, accumulated in FP64 (integrate_cell's arithmetic)
-          f2 v = splat(ar.s[e]) * P;
+          LV v = LN::splat(ar.s[e]) * P;
 #pragma unroll
           for (int l = 0; l <= N; ++l)
-            if ((mask >> l) & 1u) v = fma(splat(ar.c[e][l]), R[l], v);
+            if ((mask >> l) & 1u) v = fma(LN::splat(ar.c[e][l]), R[l], v);
           double* q = rb + e * ms;
-          if (v0 && v1) {
-            double2 o = *reinterpret_cast<const double2*>(q);
-            o.x = fma(double(v.x), ar.wfac, o.x);
-            o.y = fma(double(v.y), ar.wfac, o.y);
-            *reinterpret_cast<double2*>(q) = o;
-          } else if (v0) {
-            q[0] = fma(double(v.x), ar.wfac, q[0]);
-          } else {
-            q[1] = fma(double(v.y), ar.wfac, q[1]);
+          if constexpr (PPT == 2) {
+            if (vk[0] && vk[1]) {
+              double2 o = *reinterpret_cast<const double2*>(q);
+              o.x = fma(double(LN::get(v, 0)), ar.wfac, o.x);
+              o.y = fma(double(LN::get(v, 1)), ar.wfac, o.y);
+              *reinterpret_cast<double2*>(q) = o;
+              continue;
+            }
           }
+#pragma unroll
+          for (int k = 0; k < PPT; ++k)
+            if (vk[k]) q[k] = fma(double(LN::get(v, k)), ar.wfac, q[k]);
         }
       }
       if constexpr (C == 0) {
 #pragma unroll
-        for (int r = 0; r < MAXR; ++r)
-          if (r < I.nr) {
-            if (v0) I.wsum[ce * I.nr + r] = fma(ar.coef[r], double(own[lo]), wl0[r]);
-            if (v1) I.wsum[(ce + 1) * I.nr + r] = fma(ar.coef[r], double(own[lo + 1]), wl1[r]);
-          }
+        for (int k = 0; k < PPT; ++k)
+#pragma unroll
+          for (int r = 0; r < MAXR; ++r)
+            if (r < I.nr && vk[k]) I.wsum[(ce + k) * I.nr + r] = fma(ar.coef[r], double(own[lo + k]), wl[k][r]);
       }
     }
   }

@@ -275,7 +275,7 @@ __device__ __forceinline__ long long eee_cell(const Geom& g, int i, int j, int k
 
 // rows of a boundary block evaluated together by a face thread
 #ifndef PN_GHOST_ROWS
-#define PN_GHOST_ROWS 7
+#define PN_GHOST_ROWS 1
 #endif
 
 // Ghost of class F = switch(C, d) next to target cell (i,j,k) of class C (C even along d, cell on
@@ -311,9 +311,9 @@ __device__ __forceinline__ void ghost_fill(T* const* rd, const Geom* g, const do
     const double* B = bmat[D][F];
     const bool src = source && D == 0 && !left;
     const double* bm = src ? beam[F] + ((long long)k * gf.n[1] + j) * nf : nullptr;
-    // PN_GHOST_ROWS rows of B v at a time in FP64 (whose long FMA latency the chains would
-    // otherwise expose): independent dot products in flight, each still summed over q in order,
-    // so the values do not depend on the chunking.  FP32 keeps one row (its registers are full).
+    // PN_GHOST_ROWS rows of B v at a time in FP64: independent dot products in flight, each still
+    // summed over q in order, so the values do not depend on the chunking (7 rows measured 10 %
+    // slower on the 2D P11 solve than 1: register pressure).  FP32 keeps one row.
     constexpr int RC = sizeof(T) == 8 ? PN_GHOST_ROWS : 1;
 #pragma unroll 1
     for (int r0 = 0; r0 < nf; r0 += RC) {
