@@ -170,6 +170,7 @@ struct BSub {
   T inv_h[3];
   T* cache[8];        // unused by the batched kernels (cache_mode 0)
   int cache_mode;
+  static constexpr int pre_ghosts = 0;   // face threads form their ghosts
 };
 
 template <class T, int N>
@@ -191,6 +192,7 @@ struct BInt {
   double coef[MAXR];
   T inv_h[3];
   static constexpr bool line_sums = true;
+  static constexpr int pre_ghosts = 0;   // face threads form their ghosts
 };
 
 // Slot of state j: the zero state past the end of the march, a kept state, a checkpoint, or a

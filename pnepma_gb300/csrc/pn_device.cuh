@@ -101,6 +101,7 @@ struct SubArgs {
   // (same coefficients, densities and dt): planes 1/S, C_0..C_N, phi1_0..phi1_N per class
   T* cache[8];
   int cache_mode;             // 0 none, 1 compute and store, 2 load
+  int pre_ghosts;             // 1: ghost_kernel wrote the face ghosts before this launch
   Seg seg[MAXSEG];
   T tab[Ord<N>::n_tab];       // advection nnz values divided by the grid step
 };
@@ -130,6 +131,7 @@ struct IntArgs {
   int xel[MAXR];
   double coef[MAXR];          // dE * dvol * sigma_r * w   (times ibar_r in the kernel)
   static constexpr bool line_sums = false;   // accumulate acs_bar / noa_bar directly
+  int pre_ghosts;             // 1: ghost_kernel wrote the face ghosts before this launch
   Seg seg[MAXSEG];
   T tab[Ord<N>::n_tab];
 };
@@ -360,6 +362,94 @@ __device__ __forceinline__ void ghosts_for_cell(T* const* rd, const Geom* g, con
   }
 }
 
+// --------------------------------------------------------------------------------------------
+// face ghosts ahead of a launch
+// --------------------------------------------------------------------------------------------
+// A ghost line: the ghost of F = switch(C, dim) next to face cell `cell` (packed) of target class
+// C, on the face at index 0 (`left`) or at the last index along dim.
+struct GLine {
+  int cls, dim, left, cell;
+};
+
+template <class T>
+struct GhostArgs {
+  Geom g[8];
+  T* rd[8];                   // target classes (read) and their switched classes (ghosts written)
+  const double* bmat[3][8];
+  const double* beam[8];
+  double bc_scaled;
+  int source;                 // forward problem: beam source on the right x face
+  const GLine* lines;
+  int n_lines;
+};
+
+// Component r of one ghost line: ghost_fill's arithmetic for that component (the same dot product
+// over q in the same order), so the values are those the face threads would form.
+template <class T, int N, int C, int D>
+__device__ __forceinline__ void ghost_component(const GhostArgs<T>& a, int i, int j, int k, bool left, int r) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nt = Ord<N>::n(C);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nt == 0 || nf == 0 || ((C >> (2 - D)) & 1)) {
+    (void)a; (void)i; (void)j; (void)k; (void)left; (void)r;
+  } else {
+    if (r >= nf) return;
+    const Geom& gt = a.g[C];
+    const Geom& gf = a.g[F];
+    const T* ut = a.rd[C] + lin(gt, i, j, k);
+    int cg[3] = {i, j, k};
+    int ci[3] = {i, j, k};
+    if (left) {
+      cg[D] = 0;
+      ci[D] = 1;
+    } else {
+      cg[D] = cg[D] + 1;
+    }
+    T* fg = a.rd[F] + lin(gf, cg[0], cg[1], cg[2]);
+    const T* fi = a.rd[F] + lin(gf, ci[0], ci[1], ci[2]);
+    const double* B = a.bmat[D][F];
+    T bv = T(0);
+#pragma unroll
+    for (int q = 0; q < nt; ++q) bv = fma(T(B[r * nt + q]), ut[q * gt.ms], bv);
+    const bool src = a.source && D == 0 && !left;
+    const T gval = src ? T(a.beam[F][((long long)k * gf.n[1] + j) * nf + r] * a.bc_scaled) : T(0);
+    const T interior = fi[r * gf.ms];
+    fg[r * gf.ms] = left ? T(2) * (gval - bv) - interior : T(2) * (bv + gval) - interior;
+  }
+}
+
+template <class T, int N, int C>
+__device__ __forceinline__ void ghost_line(const GhostArgs<T>& a, const GLine& gl, int r) {
+  const int i = gl.cell & 2047, j = (gl.cell >> 11) & 2047, k = (gl.cell >> 22) & 1023;
+  switch (gl.dim) {
+    case 0: ghost_component<T, N, C, 0>(a, i, j, k, gl.left != 0, r); break;
+    case 1: ghost_component<T, N, C, 1>(a, i, j, k, gl.left != 0, r); break;
+    default: ghost_component<T, N, C, 2>(a, i, j, k, gl.left != 0, r); break;
+  }
+}
+
+// One warp per ghost line, lane r forms component r.  Launched before a sub-step (or density
+// integral) whose face cells then skip ghosts_for_cell: the boundary products, which made the face
+// threads several times slower than the interior ones and their SMs the last to finish, spread
+// over a full grid.
+template <class T, int N>
+__global__ void __launch_bounds__(256) ghost_kernel(const __grid_constant__ GhostArgs<T> a) {
+  const int line = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int r = threadIdx.x & 31;
+  if (line >= a.n_lines) return;
+  const GLine gl = a.lines[line];
+  switch (gl.cls) {
+    case 0: ghost_line<T, N, 0>(a, gl, r); break;
+    case 1: ghost_line<T, N, 1>(a, gl, r); break;
+    case 2: ghost_line<T, N, 2>(a, gl, r); break;
+    case 3: ghost_line<T, N, 3>(a, gl, r); break;
+    case 4: ghost_line<T, N, 4>(a, gl, r); break;
+    case 5: ghost_line<T, N, 5>(a, gl, r); break;
+    case 6: ghost_line<T, N, 6>(a, gl, r); break;
+    default: ghost_line<T, N, 7>(a, gl, r); break;
+  }
+}
+
 // acc[m] += sum over active axes of A_d[C] (f_r - f_l) / h_d  (sign flipped for the adjoint).
 // LIT = false: coefficients from `tab`, already divided by h_d.  LIT = true: the literal closed-form
 // coefficient compiled into the stencil, with the difference multiplied by inv_h.
@@ -501,7 +591,7 @@ __device__ __forceinline__ void substep_cell(const A& a, int i, int j, int k, bo
     return;
   } else {
     T* const* rd = a.rd;
-    if (face) ghosts_for_cell<T, N, C>(const_cast<T* const*>(rd), a.g, a.act, a.bmat, a.beam,
+    if (face && !a.pre_ghosts) ghosts_for_cell<T, N, C>(const_cast<T* const*>(rd), a.g, a.act, a.bmat, a.beam,
                                        a.bc * a.scale_g, !ADJ, i, j, k);
     const Geom& gt = a.g[C];
     const long long p = lin(gt, i, j, k);
@@ -645,7 +735,7 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
   if constexpr (n == 0) {
     return;
   } else {
-    if (face) ghosts_for_cell<T, N, C>(a.u, a.g, a.act, a.bmat, a.beam, a.bc * a.scale_g, true, i, j, k);
+    if (face && !a.pre_ghosts) ghosts_for_cell<T, N, C>(a.u, a.g, a.act, a.bmat, a.beam, a.bc * a.scale_g, true, i, j, k);
     const Geom& gt = a.g[C];
     const long long p = lin(gt, i, j, k);
     T upre[DIMS != 0 ? n : 1];

@@ -177,6 +177,9 @@ class Solver : public SolverBase {
   int nblk_par[2] = {0, 0};
   std::vector<Seg> segs_all;
   int nblk_all = 0;
+  // ghost lines of the face cells, per parity of the target class (sub-steps) and all (integral)
+  GLine* glines_d = nullptr;
+  int gl_off[2] = {0, 0}, gl_n[2] = {0, 0};
 
   cudaStream_t stream = nullptr;
   // the even classes' density integral of an adjoint iteration runs on `side`, beside the odd
@@ -488,6 +491,29 @@ class Solver : public SolverBase {
       per_class.push_back(t);
     }
     int rc;
+    // ghost lines in ghosts_for_cell's order per face cell: parity 0's, then parity 1's (the
+    // integral of every class takes both ranges, which are adjacent)
+    std::vector<GLine> lines;
+    for (int par = 0; par < 2; ++par) {
+      gl_off[par] = (int)lines.size();
+      for (const Tmp& t : per_class) {
+        if (class_parity(t.cls) != par) continue;
+        for (int f = 0; f < t.n_face; ++f) {
+          const int cell = all_faces[(size_t)t.face_off + f];
+          const int cc[3] = {cell & 2047, (cell >> 11) & 2047, (cell >> 22) & 1023};
+          for (int k = 0; k < 3; ++k) {
+            if (!L.act[k] || class_bit(t.cls, k)) continue;
+            if (cc[k] == 0) lines.push_back(GLine{t.cls, k, 1, cell});
+            if (cc[k] == L.shape[t.cls][k] - 1) lines.push_back(GLine{t.cls, k, 0, cell});
+          }
+        }
+      }
+      gl_n[par] = (int)lines.size() - gl_off[par];
+    }
+    if ((rc = alloc(glines_d, (long long)std::max<size_t>(lines.size(), 1)))) return rc;
+    if (!lines.empty())
+      PN_CUDA(cudaMemcpyAsync(glines_d, lines.data(), sizeof(GLine) * lines.size(), cudaMemcpyHostToDevice, stream));
+    // `lines` is pageable host memory: staged before the copy call returns
     if ((rc = alloc(faces_d, (long long)std::max<size_t>(all_faces.size(), 1)))) return rc;
     if (!all_faces.empty())
       PN_CUDA(cudaMemcpyAsync(faces_d, all_faces.data(), sizeof(int) * all_faces.size(), cudaMemcpyHostToDevice, stream));
@@ -549,6 +575,27 @@ class Solver : public SolverBase {
     }
   }
 
+  // the ghosts of the face cells of lines [off, off + n) on stream st (see ghost_kernel)
+  int launch_ghosts(T* const* rd, bool adj, double bc, int off, int n, cudaStream_t st) {
+    if (n <= 0) return PN_OK;
+    GhostArgs<T> g;
+    std::memset(&g, 0, sizeof(g));
+    common_geom(g.g);
+    for (int cl = 0; cl < 8; ++cl) {
+      g.rd[cl] = rd[cl];
+      for (int k = 0; k < 3; ++k) g.bmat[k][cl] = adj ? bmat_a[k][cl] : bmat_f[k][cl];
+      g.beam[cl] = beam_p[cl];
+    }
+    g.bc_scaled = bc * scale_g;
+    g.source = adj ? 0 : 1;
+    g.lines = glines_d + off;
+    g.n_lines = n;
+    ghost_kernel<T, N><<<(n * 32 + 255) / 256, 256, 0, st>>>(g);
+    PN_CUDA(cudaGetLastError());
+    ++n_launch;
+    return PN_OK;
+  }
+
   // one sub-step for the classes of parity `par`; own_rd/own_wr are the target slot pointers, from_rd
   // the slot holding the other parity
   int launch_substep(int par, bool adj, double dt, const double* s, const double* c, double bc, T* own_rd,
@@ -591,6 +638,9 @@ class Solver : public SolverBase {
     a.cache_mode = (par == 1 && cache_d != nullptr) ? cache_mode : 0;
     for (int cl = 0; cl < 8; ++cl) a.cache[cl] = cache_cls[cl];
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
+    int rc;
+    if ((rc = launch_ghosts(a.rd, adj, bc, gl_off[par], gl_n[par], stream))) return rc;
+    a.pre_ghosts = 1;
     const int nb = nblk_par[par];
     if (adj)
       substep_kernel<T, N, true><<<nb, PBLOCK, 0, stream>>>(a);
@@ -640,6 +690,12 @@ class Solver : public SolverBase {
       a.coef[r] = dE * dvol * adj_sigma[(long long)j * L.nr + r] * adj_weight[j];
     }
     for (int q = 0; q < Ord<N>::n_tab; ++q) a.tab[q] = T(tab_h[q]);
+    // the integral forms the forward problem's ghosts on the tape state
+    int rc;
+    const int goff = par < 0 ? 0 : gl_off[par];
+    const int gn = par < 0 ? gl_n[0] + gl_n[1] : gl_n[par];
+    if ((rc = launch_ghosts(a.u, false, a.bc, goff, gn, st ? st : stream))) return rc;
+    a.pre_ghosts = 1;
     integrate_kernel<T, N><<<par < 0 ? nblk_all : nblk_par[par], PBLOCK, 0, st ? st : stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
