@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--profile-batch", action="store_true",
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
     ap.add_argument("--profile-positions", type=int, default=16, help="beam positions of --profile-batch")
+    ap.add_argument("--batch-flags", type=int, default=0,
+                    help="pn_batch flags of --time-batch / --profile-batch (e.g. 16: one launch per step)")
     ap.add_argument("--time-batch", action="store_true",
                     help="time the FP32 batch of the 60-solve workload alone (forward and adjoint sweeps, rooflines)")
     ap.add_argument("--profile-budget-gb", type=float, default=6.0, help="tape budget of --profile-batch")
@@ -789,7 +791,7 @@ def run_time_batch(args):
     dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
     d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)
     free_b, _ = torch.cuda.mem_get_info(dev)
-    b = capi.Batch(descs, keep, memory_budget=int(0.9 * free_b))
+    b = capi.Batch(descs, keep, memory_budget=int(0.9 * free_b), flags=args.batch_flags)
     sz = capi.query_sizes(descs[0])
     I = torch.zeros((n, nr), dtype=torch.float64, device=dev)
     ib = torch.ones((n, nr), dtype=torch.float64, device=dev)
@@ -851,7 +853,7 @@ def run_profile_batch(args):
         d, k = s.problem.descriptor(s.x_rays)
         descs.append(d)
         keep.append(k)
-    b = capi.Batch(descs, keep, memory_budget=int(args.profile_budget_gb * (1 << 30)))
+    b = capi.Batch(descs, keep, memory_budget=int(args.profile_budget_gb * (1 << 30)), flags=args.batch_flags)
     rho, noa, acs = solves[0].inputs()
     dv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     d_rho, d_noa, d_acs = dv(rho), dv(noa), dv(acs)

@@ -254,7 +254,15 @@ enum pn_batch_flags {
      so the launch takes its timeout path (status PN_ERR_TIMEOUT, copies in flight drained, the CTA
      returns) without any copy in flight; that call's results are then incomplete.  Later calls
      run normally; the status word is cleared by every pn_batch_forward */
-  PN_BATCH_TEST_EXPIRE_WAIT = 4
+  PN_BATCH_TEST_EXPIRE_WAIT = 4,
+  /* FP32 TMA groups: one kernel launch per sub-step (or fused pair) and per density integral,
+     instead of one persistent cooperative launch per sweep in which the tiles of a solve's steps
+     wait on per-solve completion counters (identical results; for comparison and the autotuner) */
+  PN_BATCH_STEP_LAUNCHES = 16,
+  /* bits 8..11: resident CTAs per SM of the persistent TMA tile kernels, 1..15 (0: as many as the
+     shared memory and registers allow); fewer CTAs each walk more tiles.  One of the autotuner's
+     choices (tiles per CTA) */
+  PN_BATCH_CTAS_PER_SM_SHIFT = 8
 };
 
 typedef struct pn_batch_info {

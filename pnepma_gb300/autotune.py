@@ -8,11 +8,14 @@ The configurations are the batch engine's own runtime choices:
   kernels (``PN_BATCH_GENERIC_KERNELS``);
 * the launch mode: sweeps captured as CUDA graphs at creation, the default, or kernels issued from
   the host on every call (``PN_BATCH_DIRECT_LAUNCH``);
-* the tape schedule: the automatic choice within the memory budget, or a fixed checkpoint stride.
+* the tape schedule: the automatic choice within the memory budget, or a fixed checkpoint stride;
+* the persistent grid of the TMA tile kernels: resident CTAs per SM (``PN_BATCH_CTAS_PER_SM_SHIFT``
+  bits of the flags), i.e. how many tiles each CTA walks.
 
-Tile shapes are compile-time constants of the TMA boxes and are not among the choices.  A
-configuration that does not change anything for a batch is skipped: the kernel family only
-matters for FP32 groups with two or three active axes.
+The tile box (32 x 4 points) and the points per thread are compile-time constants of the TMA
+kernels (``PN_TMA_TY``, ``PN_TMA_PPT``) and are not among the runtime choices.  A configuration
+that does not change anything for a batch is skipped: the kernel family and the CTA count only
+matter for FP32 groups with two or three active axes.
 """
 from __future__ import annotations
 
@@ -25,6 +28,7 @@ import numpy as np
 
 PN_BATCH_GENERIC_KERNELS = 1
 PN_BATCH_DIRECT_LAUNCH = 2
+PN_BATCH_CTAS_PER_SM_SHIFT = 8
 PN_FP32 = 1
 
 
@@ -33,11 +37,16 @@ class Config:
     flags: int = 0
     checkpoint_stride: int = 0
 
+    @property
+    def ctas_per_sm(self) -> int:
+        return (self.flags >> PN_BATCH_CTAS_PER_SM_SHIFT) & 15
+
     def label(self) -> str:
         kern = "generic" if self.flags & PN_BATCH_GENERIC_KERNELS else "tma"
         launch = "direct" if self.flags & PN_BATCH_DIRECT_LAUNCH else "graphs"
         tape = f"K={self.checkpoint_stride}" if self.checkpoint_stride else "K=auto"
-        return f"{kern}/{launch}/{tape}"
+        ctas = f"/ctas={self.ctas_per_sm}" if self.ctas_per_sm else ""
+        return f"{kern}/{launch}/{tape}{ctas}"
 
 
 DEFAULT_CANDIDATES = (
@@ -46,6 +55,8 @@ DEFAULT_CANDIDATES = (
     Config(PN_BATCH_GENERIC_KERNELS, 0),
     Config(0, 2),
     Config(0, 4),
+    Config(3 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
+    Config(4 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
 )
 
 
@@ -63,8 +74,9 @@ def batch_key(descs) -> str:
 
 def applies(cfg: Config, descs) -> bool:
     """False when the configuration runs the batch exactly as the default does."""
-    if cfg.flags & PN_BATCH_GENERIC_KERNELS:
-        return any(d.precision == PN_FP32 and sum(d.n_points[k] > 1 for k in range(3)) >= 2 for d in descs)
+    tiles = any(d.precision == PN_FP32 and sum(d.n_points[k] > 1 for k in range(3)) >= 2 for d in descs)
+    if cfg.flags & PN_BATCH_GENERIC_KERNELS or cfg.ctas_per_sm:
+        return tiles
     return True
 
 

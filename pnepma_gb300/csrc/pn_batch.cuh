@@ -628,6 +628,21 @@ class BatchGroup : public BatchGroupBase {
   void* drows = nullptr;
   int* dstatus = nullptr;          // [0] status of the latest calls, [1] test expiries left
   bool test_expire = false;         // PN_BATCH_TEST_EXPIRE_WAIT
+  int cta_cap = 0;                  // resident CTAs per SM of the tile kernels (0: occupancy)
+  // one persistent launch per sweep (TMA groups replayed as graphs, see batch_sweep_kernel): the
+  // steps of each sweep are planned once before the graphs are captured
+  bool sweep = false;
+  bool planning = false;            // record() collects the TMA steps only, launching nothing
+  std::vector<TStep> rec_steps;
+  struct SweepPlan {
+    TStep* steps = nullptr;
+    int* dep = nullptr;
+    int* need = nullptr;
+    int n_steps = 0, n_items = 0;
+  };
+  SweepPlan plans[2];               // forward, adjoint
+  int* done_d = nullptr;            // [step][solve] completed tiles, zeroed before every sweep
+  int sweep_grid = 0;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
   // Creation never waits for the device: tables go up on `up`, whose event the first forward or
   // adjoint waits on in stream order, and the tape / density zeroing is enqueued with the first
@@ -881,6 +896,7 @@ class BatchGroup : public BatchGroupBase {
     }
     if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       test_expire = (flags & PN_BATCH_TEST_EXPIRE_WAIT) != 0;
+      cta_cap = (flags >> PN_BATCH_CTAS_PER_SM_SHIFT) & 15;
       if (!(flags & PN_BATCH_GENERIC_KERNELS))
         if ((rc = build_tma())) return rc;
     } else {
@@ -894,6 +910,10 @@ class BatchGroup : public BatchGroupBase {
     PN_CUDA(cudaEventRecord(ev_up, up));
     const auto t3 = clk();
     direct = (flags & PN_BATCH_DIRECT_LAUNCH) != 0;
+    if (!direct && use_tma && !(flags & PN_BATCH_STEP_LAUNCHES)) {
+      if ((rc = plan_sweeps())) return rc;
+      PN_CUDA(cudaEventRecord(ev_up, up));   // the plans' uploads
+    }
     if (!direct) {
       if ((rc = capture(gf, true))) return rc;
       if ((rc = capture(ga, false))) return rc;
@@ -945,6 +965,12 @@ class BatchGroup : public BatchGroupBase {
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, NTS, LY::SMEM));
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, NTS, LY::SMEM));
       if (occ_f < 1 || occ_a < 1) return PN_OK;
+      if (cta_cap > 0) {
+        occ_f = std::min(occ_f, cta_cap);
+        occ_a = std::min(occ_a, cta_cap);
+        occ_i = std::min(occ_i, cta_cap);
+        tma_int_grid = occ_i * sms;
+      }
       tma_grid[0] = occ_f * sms;
       tma_grid[1] = occ_a * sms;
       // coefficient rows: forward then adjoint, per solve
@@ -1428,6 +1454,10 @@ class BatchGroup : public BatchGroupBase {
         a.j = j;
         a.sub = sub;
         a.K = K;
+        if (sweep) {
+          rec_steps.push_back(TStep{adj ? (int)TS_ADJ : (int)TS_FWD, list, mode, j, sub, nb, 0, 0, part});
+          return PN_OK;
+        }
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
         if (adj)
           batch_tma_kernel<N, true, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
@@ -1461,6 +1491,10 @@ class BatchGroup : public BatchGroupBase {
         a.n_tiles = nb;
         a.it = j;
         a.K = K;
+        if (sweep) {
+          rec_steps.push_back(TStep{(int)TS_INT, 2, BM_ADJOINT, j, 0, nb, 0, 0, nullptr});
+          return PN_OK;
+        }
         batch_tma_int_kernel<N, DIMS><<<std::min(nb, tma_int_grid), NTS, TmaIntLayout<N, DIMS>::SMEM, ls>>>(a);
         PN_CUDA(cudaGetLastError());
         ++nl;
@@ -1506,16 +1540,23 @@ class BatchGroup : public BatchGroupBase {
     int rc;
     dim3 gz(64, n);
     if (fwd) {
-      batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 0);
-      PN_CUDA(cudaGetLastError());
+      if (!planning) {
+        batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 0);
+        PN_CUDA(cudaGetLastError());
+      }
       if ((rc = fwd_steps(max_ns - 1, 0, BM_FORWARD, true))) return rc;
-      batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, ls>>>(dinst, partial, max_ns, n_ptiles, pr);
-      batch_final_kernel<T><<<n, 32, 0, ls>>>(dinst);
-      PN_CUDA(cudaGetLastError());
+      if ((rc = flush_sweep(true))) return rc;
+      if (!planning) {
+        batch_reduce_kernel<T><<<dim3(max_ns, n), 128, 0, ls>>>(dinst, partial, max_ns, n_ptiles, pr);
+        batch_final_kernel<T><<<n, 32, 0, ls>>>(dinst);
+        PN_CUDA(cudaGetLastError());
+      }
       nl += 3;
     } else {
-      batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 1);
-      PN_CUDA(cudaGetLastError());
+      if (!planning) {
+        batch_zero_kernel<T><<<gz, 256, 0, ls>>>(dinst, 1);
+        PN_CUDA(cudaGetLastError());
+      }
       nl += 1;
       // iterations on the kept head, then segments [s0, s0 + K) after recomputing s0 + 1 .. s0 + K - 1;
       // iteration max_ns is the final accumulation of the longest solves on the zero state
@@ -1527,6 +1568,127 @@ class BatchGroup : public BatchGroupBase {
         for (int a = s0; a < std::min(s0 + K, max_ns + 1); ++a)
           if ((rc = adj_iter(a))) return rc;
       }
+      if ((rc = flush_sweep(false))) return rc;
+    }
+    return PN_OK;
+  }
+
+  // The recorded TMA steps of a sweep: while planning, turned into the sweep's plan (item offsets,
+  // and per step and solve the step it waits for and its tile count); while capturing, one
+  // cooperative launch of batch_sweep_kernel over the planned steps.
+  int flush_sweep(bool fwd) {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
+      if (!sweep || rec_steps.empty()) return PN_OK;
+      SweepPlan& P = plans[fwd ? 0 : 1];
+      if (planning) {
+        const int ns = (int)rec_steps.size();
+        std::vector<int> dep((size_t)ns * n, -1), need((size_t)ns * n, 0), last(n, -1);
+        int items = 0;
+        for (int k = 0; k < ns; ++k) {
+          TStep& st = rec_steps[k];
+          st.first = items;
+          items += st.n_tiles;
+          int prev = 0;
+          for (int q = 0; q < n && prev < st.n_tiles; ++q) {
+            const int end = std::min(tend[st.list][q], st.n_tiles);
+            const int cnt = end - prev;
+            prev = end;
+            if (cnt <= 0) continue;
+            dep[(size_t)k * n + q] = last[q];
+            need[(size_t)k * n + q] = cnt;
+            last[q] = k;
+          }
+        }
+        // dep holds step indices; the kernel reads the tile count of the step it waits for
+        std::vector<int> need_dep((size_t)ns * n, 0);
+        for (int k = 0; k < ns; ++k)
+          for (int q = 0; q < n; ++q) {
+            const int d = dep[(size_t)k * n + q];
+            if (d >= 0) need_dep[(size_t)k * n + q] = need[(size_t)d * n + q];
+          }
+        int rc;
+        if ((rc = upload(P.steps, rec_steps))) return rc;
+        if ((rc = upload(P.dep, dep))) return rc;
+        if ((rc = upload(P.need, need_dep))) return rc;
+        P.n_steps = ns;
+        P.n_items = items;
+        rec_steps.clear();
+        return PN_OK;
+      }
+      if ((int)rec_steps.size() != P.n_steps) {
+        err = "internal: the sweep differs from its plan";
+        return PN_ERR_INVALID;
+      }
+      rec_steps.clear();
+      PN_CUDA(cudaMemsetAsync(done_d, 0, sizeof(int) * (size_t)P.n_steps * n, ls));
+      TSweep<N> S;
+      std::memset(&S, 0, sizeof(S));
+      S.inst = dinst;
+      S.solves = dsolves;
+      for (int l = 0; l < 3; ++l) S.tiles[l] = dttl[l];
+      S.maps = dmaps;
+      S.rows = static_cast<const ArgRow<N>*>(drows);
+      S.irows = static_cast<const IntRow<N>*>(dirows);
+      S.status = dstatus;
+      S.test_expire = test_expire ? dstatus + 1 : nullptr;
+      S.steps = P.steps;
+      S.dep = P.dep;
+      S.need = P.need;
+      S.done = done_d;
+      S.n_steps = P.n_steps;
+      S.n_items = P.n_items;
+      S.n_solves = n;
+      S.pr = pr;
+      S.K = K;
+      cudaLaunchConfig_t cfg;
+      std::memset(&cfg, 0, sizeof(cfg));
+      cfg.gridDim = dim3((unsigned)std::min(P.n_items, sweep_grid));
+      cfg.blockDim = dim3(NTS);
+      cfg.dynamicSmemBytes = sweep_smem();
+      cfg.stream = ls;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeCooperative;
+      at[0].val.cooperative = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      PN_CUDA(cudaLaunchKernelEx(&cfg, batch_sweep_kernel<N, DIMS>, S));
+      ++nl;
+    } else {
+      (void)fwd;
+    }
+    return PN_OK;
+  }
+
+  static constexpr int sweep_smem() {
+    return TmaLayout<N, DIMS>::SMEM > TmaIntLayout<N, DIMS>::SMEM ? TmaLayout<N, DIMS>::SMEM
+                                                                    : TmaIntLayout<N, DIMS>::SMEM;
+  }
+
+  // plan both sweeps (before the graphs are captured) and size the persistent grid
+  int plan_sweeps() {
+    if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
+      int rc;
+      PN_CUDA(cudaFuncSetAttribute(batch_sweep_kernel<N, DIMS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   sweep_smem()));
+      int occ = 0;
+      PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_sweep_kernel<N, DIMS>, NTS, sweep_smem()));
+      if (cta_cap > 0) occ = std::min(occ, cta_cap);
+      if (occ < 1) {
+        sweep = false;
+        return PN_OK;
+      }
+      sweep_grid = occ * sms;
+      sweep = true;
+      planning = true;
+      ls = nullptr;
+      rc = record(true);
+      if (!rc) rc = record(false);
+      planning = false;
+      rec_steps.clear();
+      nl = 0;
+      if (rc) return rc;
+      const long long cells = (long long)std::max(plans[0].n_steps, plans[1].n_steps) * n;
+      if ((rc = alloc(done_d, std::max(cells, 1LL)))) return rc;
     }
     return PN_OK;
   }

@@ -934,7 +934,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
       const float* la = I.lam + I.dev_off[C] + p;
       LV lam[n];
 #pragma unroll
-      for (int m = 0; m < n; ++m) lam[m] = LN::ld(la + m * ms);
+      for (int m = 0; m < n; ++m) lam[m] = LN::ldcg(la + m * ms);   // L2: earlier steps of a sweep launch wrote it
       // the eee cells' line sums
       long long ce = 0;
       double wl[PPT][MAXR];
@@ -943,7 +943,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
 #pragma unroll
         for (int k = 0; k < PPT; ++k)
 #pragma unroll
-          for (int r = 0; r < MAXR; ++r) wl[k][r] = (r < I.nr && vk[k]) ? I.wsum[(ce + k) * I.nr + r] : 0.0;
+          for (int r = 0; r < MAXR; ++r) wl[k][r] = (r < I.nr && vk[k]) ? __ldcg(&I.wsum[(ce + k) * I.nr + r]) : 0.0;
       }
       LV acc[n];
 #pragma unroll
@@ -984,7 +984,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
           double* q = rb + e * ms;
           if constexpr (PPT == 2) {
             if (vk[0] && vk[1]) {
-              double2 o = *reinterpret_cast<const double2*>(q);
+              double2 o = __ldcg(reinterpret_cast<const double2*>(q));
               o.x = fma(double(LN::get(v, 0)), ar.wfac, o.x);
               o.y = fma(double(LN::get(v, 1)), ar.wfac, o.y);
               *reinterpret_cast<double2*>(q) = o;
@@ -993,7 +993,7 @@ __device__ __forceinline__ void tma_int_cell(const TILaunch<N>& L, const TTile& 
           }
 #pragma unroll
           for (int k = 0; k < PPT; ++k)
-            if (vk[k]) q[k] = fma(double(LN::get(v, k)), ar.wfac, q[k]);
+            if (vk[k]) q[k] = fma(double(LN::get(v, k)), ar.wfac, __ldcg(q + k));
         }
       }
       if constexpr (C == 0) {
@@ -1075,6 +1075,183 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_int_kernel(const _
     unsigned char* st = smem + s * LY::STAGE;
     const TTile& tt = *reinterpret_cast<const TTile*>(st + LY::TIL);
     tma_int_cell_of<N, DIMS>(L, tt, st);
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------------------------
+// one persistent launch per sweep
+// ---------------------------------------------------------------------------------------------
+// A sweep (a forward march, or an adjoint march with its density integrals and recomputed
+// segments) is a sequence of steps; a step is what one launch of batch_tma_kernel or
+// batch_tma_int_kernel covers.  batch_sweep_kernel runs every tile of every step in one
+// cooperative launch: the tiles of all steps form one item list (step-major), which the CTAs walk
+// in grid-stride order.  Before its loads, an item of solve q waits (bounded) until the last
+// earlier step that had tiles of q has completed all of them (per-step, per-solve counters
+// released after the tile's stores have landed).  A solve's steps therefore keep their order
+// while the steps of different solves, and the end of one step and the start of the next,
+// overlap.  Every CTA is resident (cooperative launch) and handles its items in increasing order,
+// and every item waits only on items of earlier steps, so the CTA holding the lowest unfinished
+// item can always proceed.
+enum { TS_FWD = 0, TS_ADJ = 1, TS_INT = 2 };
+
+struct TStep {
+  int kind;       // TS_FWD / TS_ADJ sub-step (or fused pair), TS_INT density integral
+  int list;       // tile list
+  int mode, j, sub;
+  int n_tiles;
+  int first;      // index of the step's first item
+  int pad_;
+  double* partial;
+};
+
+template <int N>
+struct TSweep {
+  const BInst<float>* inst;
+  const TSolve* solves;
+  const TTile* tiles[3];
+  const CUtensorMap* maps;
+  const ArgRow<N>* rows;
+  const IntRow<N>* irows;
+  double* partial_unused_;
+  int* status;
+  int* test_expire;
+  const TStep* steps;
+  const int* dep;        // [step][solve]: the last earlier step with tiles of the solve, or -1
+  const int* need;       // [step][solve]: tiles of the solve in that earlier step
+  int* done;             // [step][solve]: tiles of the solve completed
+  int n_steps, n_items, n_solves;
+  int pr, K;
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// wait (at most ~1 s) until *p >= need
+__device__ __forceinline__ bool wait_count(const int* p, int need) {
+  if (ld_acquire(p) >= need) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (ld_acquire(p) >= need) return true;
+    if (global_ns() - t0 > 1000000000ull) return false;
+    __nanosleep(100);
+  }
+}
+
+template <int N, int DIMS>
+__global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __grid_constant__ TSweep<N> S) {
+  static_assert(TSTAGES == 1, "the sweep kernel stages one tile per CTA");
+  using LY = TmaLayout<N, DIMS>;
+  using LI = TmaIntLayout<N, DIMS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long full[1];
+  __shared__ double red[NTS / 32][MAXR];
+  __shared__ TLaunch<N> L;
+  __shared__ TILaunch<N> IL;
+  __shared__ int sh_kind;
+  if ((smem_u32(smem) & 127u) != 0u) {
+    if (threadIdx.x == 0) atomicExch(S.status, (int)PN_ERR_INVALID);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    mbar_init(&full[0], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  int k = 0;   // step of the current item (items are visited in increasing order)
+  unsigned phase = 0;
+  for (int w = blockIdx.x; w < S.n_items; w += gridDim.x) {
+    bool ok = true;
+    if (threadIdx.x == 0) {
+      while (k + 1 < S.n_steps && S.steps[k + 1].first <= w) ++k;
+      const TStep st = S.steps[k];
+      const TTile* tl = S.tiles[st.list] + (w - st.first);
+      const int q = tl->inst;
+      const int d = S.dep[(long long)k * S.n_solves + q];
+      if (d >= 0) {
+        ok = wait_count(S.done + (long long)d * S.n_solves + q, S.need[(long long)k * S.n_solves + q]);
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+      }
+      sh_kind = st.kind;
+      if (st.kind == TS_INT) {
+        IL.inst = S.inst;
+        IL.solves = S.solves;
+        IL.tiles = S.tiles[st.list];
+        IL.maps = S.maps;
+        IL.rows = S.irows;
+        IL.status = S.status;
+        IL.n_tiles = st.n_tiles;
+        IL.it = st.j;
+        IL.K = S.K;
+      } else {
+        L.inst = S.inst;
+        L.solves = S.solves;
+        L.tiles = S.tiles[st.list];
+        L.maps = S.maps;
+        L.rows = S.rows;
+        L.partial = st.partial;
+        L.status = S.status;
+        L.test_expire = S.test_expire;
+        L.pr = S.pr;
+        L.n_tiles = st.n_tiles;
+        L.mode = st.mode;
+        L.j = st.j;
+        L.K = S.K;
+        L.sub = st.sub;
+      }
+      if (ok) {
+        bulk_wait_read();   // the previous item's stores have read the stage
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (st.kind == TS_INT) tma_issue_int<N, DIMS>(IL, *tl, smem, &full[0]);
+        else if (st.kind == TS_ADJ) tma_issue<N, true, DIMS>(L, *tl, smem, &full[0]);
+        else tma_issue<N, false, DIMS>(L, *tl, smem, &full[0]);
+      }
+    }
+    if (__syncthreads_or(!ok)) {   // a dependency did not complete in time: nothing was issued
+      if (threadIdx.x == 0) {
+        atomicExch(S.status, (int)PN_ERR_TIMEOUT);
+        bulk_wait_all();
+      }
+      __syncthreads();
+      return;
+    }
+    ok = mbar_wait_bounded(&full[0], phase);
+    if (threadIdx.x == 0 && ok && sh_kind != TS_INT && S.test_expire != nullptr && w == (int)blockIdx.x &&
+        *(volatile int*)S.test_expire > 0 && atomicSub(S.test_expire, 1) > 0)
+      ok = false;   // test hook: report the first (completed) wait as run out, as batch_tma_kernel does
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(S.status, (int)PN_ERR_TIMEOUT);
+        mbar_wait_bounded(&full[0], phase);   // let the copies in flight land
+        bulk_wait_all();
+      }
+      __syncthreads();
+      return;
+    }
+    phase ^= 1u;
+    const int kind = sh_kind;
+    if (kind == TS_INT) {
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + LI::TIL);
+      tma_int_cell_of<N, DIMS>(IL, tt, smem);
+    } else {
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + LY::TIL);
+      if (kind == TS_ADJ) tma_cell_of<N, true, DIMS>(L, tt, smem, red);
+      else tma_cell_of<N, false, DIMS>(L, tt, smem, red);
+    }
+    // publish the tile: its tensor stores have landed (sub-steps), its rho_bar and line sums are
+    // written (the integral's threads synchronised at its end)
+    if (threadIdx.x == 0) {
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + (kind == TS_INT ? LI::TIL : LY::TIL));
+      const int q = tt.inst;
+      bulk_wait_all();
+      __threadfence();
+      asm volatile("fence.proxy.async.global;" ::: "memory");
+      asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(S.done + (long long)k * S.n_solves + q) : "memory");
+    }
+    __syncthreads();   // the stage's tile record is not read again before the next issue
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }

@@ -74,6 +74,8 @@ struct Lanes<1> {
   using V = float;
   static __device__ __forceinline__ V splat(float v) { return v; }
   static __device__ __forceinline__ V ld(const float* p) { return *p; }
+  // global memory another CTA of the same launch may have written: cached at L2 only
+  static __device__ __forceinline__ V ldcg(const float* p) { return __ldcg(p); }
   static __device__ __forceinline__ void st(float* p, V v) { *p = v; }
   static __device__ __forceinline__ float get(V v, int) { return v; }
   static __device__ __forceinline__ void set(V& v, int, float x) { v = x; }
@@ -91,6 +93,10 @@ struct Lanes<2> {
   using V = f2;
   static __device__ __forceinline__ V splat(float v) { return pn::splat(v); }
   static __device__ __forceinline__ V ld(const float* p) { return ld2(p); }
+  static __device__ __forceinline__ V ldcg(const float* p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return f2{v.x, v.y};
+  }
   static __device__ __forceinline__ void st(float* p, V v) { st2(p, v); }
   static __device__ __forceinline__ float get(V v, int k) { return k ? v.y : v.x; }
   static __device__ __forceinline__ void set(V& v, int k, float x) {
