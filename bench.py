@@ -60,7 +60,7 @@ def parse():
                     help="run one FP32 batch (16 positions at 10 keV, 6 GiB of tapes) twice for a profiler")
     ap.add_argument("--profile-positions", type=int, default=16, help="beam positions of --profile-batch")
     ap.add_argument("--batch-flags", type=int, default=0,
-                    help="pn_batch flags of --time-batch / --profile-batch (e.g. 16: one launch per step)")
+                    help="pn_batch flags of --time-batch / --profile-batch (e.g. 16: one persistent launch per sweep)")
     ap.add_argument("--time-batch", action="store_true",
                     help="time the FP32 batch of the 60-solve workload alone (forward and adjoint sweeps, rooflines)")
     ap.add_argument("--profile-budget-gb", type=float, default=6.0, help="tape budget of --profile-batch")

@@ -255,10 +255,12 @@ enum pn_batch_flags {
      returns) without any copy in flight; that call's results are then incomplete.  Later calls
      run normally; the status word is cleared by every pn_batch_forward */
   PN_BATCH_TEST_EXPIRE_WAIT = 4,
-  /* FP32 TMA groups: one kernel launch per sub-step (or fused pair) and per density integral,
-     instead of one persistent cooperative launch per sweep in which the tiles of a solve's steps
-     wait on per-solve completion counters (identical results; for comparison and the autotuner) */
-  PN_BATCH_STEP_LAUNCHES = 16,
+  /* FP32 TMA groups: one persistent cooperative launch per sweep (batch_sweep_kernel), in which
+     the tiles of a solve's steps wait on per-solve completion counters, instead of one kernel
+     launch per sub-step (or fused pair) and per density integral.  Identical results; measured
+     slower on the 2D P11 workload (each tile waits for its stores to land before it releases
+     its counter), so off by default and one of the autotuner's choices */
+  PN_BATCH_SWEEP_LAUNCH = 16,
   /* bits 8..11: resident CTAs per SM of the persistent TMA tile kernels, 1..15 (0: as many as the
      shared memory and registers allow); fewer CTAs each walk more tiles.  One of the autotuner's
      choices (tiles per CTA) */

@@ -6,8 +6,9 @@ The configurations are the batch engine's own runtime choices:
 
 * the kernel family: TMA tile kernels, the default for FP32 2D and 3D groups, or the generic
   kernels (``PN_BATCH_GENERIC_KERNELS``);
-* the launch mode: sweeps captured as CUDA graphs at creation, the default, or kernels issued from
-  the host on every call (``PN_BATCH_DIRECT_LAUNCH``);
+* the launch mode: sweeps captured as CUDA graphs at creation, the default, kernels issued from
+  the host on every call (``PN_BATCH_DIRECT_LAUNCH``), or the TMA steps of each sweep as one
+  persistent cooperative launch (``PN_BATCH_SWEEP_LAUNCH``);
 * the tape schedule: the automatic choice within the memory budget, or a fixed checkpoint stride;
 * the persistent grid of the TMA tile kernels: resident CTAs per SM (``PN_BATCH_CTAS_PER_SM_SHIFT``
   bits of the flags), i.e. how many tiles each CTA walks.
@@ -28,6 +29,7 @@ import numpy as np
 
 PN_BATCH_GENERIC_KERNELS = 1
 PN_BATCH_DIRECT_LAUNCH = 2
+PN_BATCH_SWEEP_LAUNCH = 16
 PN_BATCH_CTAS_PER_SM_SHIFT = 8
 PN_FP32 = 1
 
@@ -43,7 +45,8 @@ class Config:
 
     def label(self) -> str:
         kern = "generic" if self.flags & PN_BATCH_GENERIC_KERNELS else "tma"
-        launch = "direct" if self.flags & PN_BATCH_DIRECT_LAUNCH else "graphs"
+        launch = ("direct" if self.flags & PN_BATCH_DIRECT_LAUNCH else
+                  "sweep" if self.flags & PN_BATCH_SWEEP_LAUNCH else "graphs")
         tape = f"K={self.checkpoint_stride}" if self.checkpoint_stride else "K=auto"
         ctas = f"/ctas={self.ctas_per_sm}" if self.ctas_per_sm else ""
         return f"{kern}/{launch}/{tape}{ctas}"
@@ -55,6 +58,7 @@ DEFAULT_CANDIDATES = (
     Config(PN_BATCH_GENERIC_KERNELS, 0),
     Config(0, 2),
     Config(0, 4),
+    Config(PN_BATCH_SWEEP_LAUNCH, 0),
     Config(3 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
     Config(4 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
 )
@@ -75,7 +79,7 @@ def batch_key(descs) -> str:
 def applies(cfg: Config, descs) -> bool:
     """False when the configuration runs the batch exactly as the default does."""
     tiles = any(d.precision == PN_FP32 and sum(d.n_points[k] > 1 for k in range(3)) >= 2 for d in descs)
-    if cfg.flags & PN_BATCH_GENERIC_KERNELS or cfg.ctas_per_sm:
+    if cfg.flags & (PN_BATCH_GENERIC_KERNELS | PN_BATCH_SWEEP_LAUNCH) or cfg.ctas_per_sm:
         return tiles
     return True
 

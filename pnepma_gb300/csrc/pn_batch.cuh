@@ -910,7 +910,7 @@ class BatchGroup : public BatchGroupBase {
     PN_CUDA(cudaEventRecord(ev_up, up));
     const auto t3 = clk();
     direct = (flags & PN_BATCH_DIRECT_LAUNCH) != 0;
-    if (!direct && use_tma && !(flags & PN_BATCH_STEP_LAUNCHES)) {
+    if (!direct && use_tma && (flags & PN_BATCH_SWEEP_LAUNCH)) {
       if ((rc = plan_sweeps())) return rc;
       PN_CUDA(cudaEventRecord(ev_up, up));   // the plans' uploads
     }

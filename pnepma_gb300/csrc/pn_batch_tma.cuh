@@ -1130,6 +1130,16 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
   return v;
 }
 
+// release one completed tile of a sweep: its tensor stores have landed (bulk_wait_all), the
+// generic writes of its threads (observed by thread 0 through the CTA barrier) are fenced, then
+// the counter is incremented with release semantics
+__device__ __forceinline__ void release_tile(int* counter, bool generic_writes) {
+  bulk_wait_all();
+  if (generic_writes) __threadfence();
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(counter) : "memory");
+}
+
 // wait (at most ~1 s) until *p >= need
 __device__ __forceinline__ bool wait_count(const int* p, int need) {
   if (ld_acquire(p) >= need) return true;
@@ -1163,6 +1173,11 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
   __syncthreads();
   int k = 0;   // step of the current item (items are visited in increasing order)
   unsigned phase = 0;
+  // thread 0: the counter of the previous item, released once its stores have landed -- after the
+  // next item's loads are issued (their latency covers the stores'), or before thread 0 blocks on
+  // a dependency, so that a CTA never waits while holding a tile
+  long long pend = -1;
+  bool pend_generic = false;
   for (int w = blockIdx.x; w < S.n_items; w += gridDim.x) {
     bool ok = true;
     if (threadIdx.x == 0) {
@@ -1172,7 +1187,17 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
       const int q = tl->inst;
       const int d = S.dep[(long long)k * S.n_solves + q];
       if (d >= 0) {
-        ok = wait_count(S.done + (long long)d * S.n_solves + q, S.need[(long long)k * S.n_solves + q]);
+        const int* cnt = S.done + (long long)d * S.n_solves + q;
+        const int need = S.need[(long long)k * S.n_solves + q];
+        if (ld_acquire(cnt) < need) {
+          // about to block: release the tile this CTA still holds first, so that no two CTAs
+          // can wait on each other's held tiles
+          if (pend >= 0) {
+            release_tile(S.done + pend, pend_generic);
+            pend = -1;
+          }
+          ok = wait_count(cnt, need);
+        }
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
       sh_kind = st.kind;
@@ -1232,6 +1257,10 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
       return;
     }
     phase ^= 1u;
+    if (threadIdx.x == 0 && pend >= 0) {
+      release_tile(S.done + pend, pend_generic);
+      pend = -1;
+    }
     const int kind = sh_kind;
     if (kind == TS_INT) {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LI::TIL);
@@ -1241,19 +1270,19 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
       if (kind == TS_ADJ) tma_cell_of<N, true, DIMS>(L, tt, smem, red);
       else tma_cell_of<N, false, DIMS>(L, tt, smem, red);
     }
-    // publish the tile: its tensor stores have landed (sub-steps), its rho_bar and line sums are
-    // written (the integral's threads synchronised at its end)
+    // the tile is released later (see pend): its tensor stores (sub-steps) or its rho_bar and
+    // line sums (the integral's threads synchronised at its end) are then visible
     if (threadIdx.x == 0) {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + (kind == TS_INT ? LI::TIL : LY::TIL));
-      const int q = tt.inst;
-      bulk_wait_all();
-      __threadfence();
-      asm volatile("fence.proxy.async.global;" ::: "memory");
-      asm volatile("red.release.gpu.global.add.s32 [%0], 1;" ::"l"(S.done + (long long)k * S.n_solves + q) : "memory");
+      pend = (long long)k * S.n_solves + tt.inst;
+      pend_generic = kind == TS_INT;
     }
     __syncthreads();   // the stage's tile record is not read again before the next issue
   }
-  if (threadIdx.x == 0) bulk_wait_all();
+  if (threadIdx.x == 0) {
+    if (pend >= 0) release_tile(S.done + pend, pend_generic);
+    bulk_wait_all();
+  }
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -211,14 +211,14 @@ def test_budgeted_tape_gives_the_full_tape_results(gpu_lib):
 
 
 def test_sweep_launch_matches_step_launches(gpu_lib):
-    """One persistent launch per sweep (the default for TMA groups) against one launch per step
-    (PN_BATCH_STEP_LAUNCHES): the same tiles with the same arithmetic in the same order per solve,
-    so identical states and gradients; intensities agree to rounding (partials per tile)."""
+    """One persistent launch per sweep (PN_BATCH_SWEEP_LAUNCH) against one launch per step (the
+    default): the same tiles with the same arithmetic in the same order per solve, so identical
+    states and gradients; intensities agree to rounding."""
     torch = pytest.importorskip("torch")
     solves = tma_solves() + tma_solves_3d()[:2]
     for K in (1, 3):
-        ref = run_batch(torch, solves, K=K, flags=capi.PN_BATCH_STEP_LAUNCHES)
-        got = run_batch(torch, solves, K=K, ibar=ref[1])
+        ref = run_batch(torch, solves, K=K)
+        got = run_batch(torch, solves, K=K, ibar=ref[1], flags=capi.PN_BATCH_SWEEP_LAUNCH)
         assert got[5].tma_groups == ref[5].tma_groups > 0
         assert got[5].forward_kernels < ref[5].forward_kernels
         for x, y in zip(got[0], ref[0]):
