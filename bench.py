@@ -992,6 +992,7 @@ def served_summary(args):
     at_rate = serve_run(stream, budget)
     capacity = at_rate["requests_per_s"]
     sustained = serve_run(stream, budget, rate_scale=0.9 * capacity / args.serve_rate)
+    seq_s, per_solve_ms = fp64_sequential_seconds(stream)
     mix = {}
     for r in stream.reqs:
         mix[r.kind] = mix.get(r.kind, 0) + 1
@@ -1007,7 +1008,11 @@ def served_summary(args):
                                       "solves_per_s": sustained["solves_per_s"],
                                       "latency_ms": sustained["latency_ms"],
                                       "latency_ms_by_kind": sustained["latency_ms_by_kind"]},
-            "waves": at_rate["waves"], "max_waves_in_flight": at_rate["max_waves_in_flight"]}
+            "waves": at_rate["waves"], "max_waves_in_flight": at_rate["max_waves_in_flight"],
+            "fp64_plain_sequential": {"solves_per_s": at_rate["solves"] / seq_s, "per_solve_ms": per_solve_ms,
+                                      "method": "one FP64 plain solve per (kind, step count), CUDA events, summed "
+                                                "over the stream's solves"},
+            "speedup_vs_fp64_plain_sequential": at_rate["solves_per_s"] / (at_rate["solves"] / seq_s)}
 
 
 def fp64_sequential_seconds(stream):
