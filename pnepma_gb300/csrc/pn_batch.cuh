@@ -644,6 +644,9 @@ class BatchGroup : public BatchGroupBase {
   int* done_d = nullptr;            // [step][solve] completed tiles, zeroed before every sweep
   int sweep_grid = 0;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
+  // 2D groups update both target classes of a parity per tile (pn_batch_par.cuh)
+  static constexpr bool kPar = DIMS == 3 && PPT == 1;
+  int par_smem = 0;                // dynamic shared memory of a parity tile (the group's elements)
   // Creation never waits for the device: tables go up on `up`, whose event the first forward or
   // adjoint waits on in stream order, and the tape / density zeroing is enqueued with the first
   // forward; graphs are captured on `cap`, which has no work of its own.
@@ -964,6 +967,16 @@ class BatchGroup : public BatchGroupBase {
       int occ_f = 0, occ_a = 0;
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, NTS, LY::SMEM));
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, NTS, LY::SMEM));
+      if constexpr (kPar) {
+        int ne_max = 1;
+        for (int q = 0; q < n; ++q) ne_max = std::max(ne_max, hinst[q].ne);
+        par_smem = ParLayout<N>::smem(ne_max);
+        if (par_smem + 2048 > smem_optin) return PN_OK;
+        PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, par_smem));
+        PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, par_smem));
+        PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_par_kernel<N, false>, TB, par_smem));
+        PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_par_kernel<N, true>, TB, par_smem));
+      }
       if (occ_f < 1 || occ_a < 1) return PN_OK;
       if (cta_cap > 0) {
         occ_f = std::min(occ_f, cta_cap);
@@ -1049,6 +1062,11 @@ class BatchGroup : public BatchGroupBase {
           if (DIMS == 7)
             ok = ok && encode_f32(&m[TM_ST_Z], I.slots + I.dev_off[c], 5, st_dims, st_str, boxz) &&
                  encode_f32(&m[TM_LAM_Z], I.lam + I.dev_off[c], 4, st_dims, st_str, boxz);
+          if (kPar) {
+            const int boxn[5] = {NBW, NBH, 1, nm, 1};
+            ok = ok && encode_f32(&m[TM_ST_N], I.slots + I.dev_off[c], 5, st_dims, st_str, boxn) &&
+                 encode_f32(&m[TM_LAM_N], I.lam + I.dev_off[c], 4, st_dims, st_str, boxn);
+          }
           const long long rho_dims[4] = {I.shape[c][0], I.shape[c][1], I.shape[c][2], I.ne};
           const int boxr[4] = {TX, TY, 1, I.ne};
           ok = ok && encode_f32(&m[TM_RHO], const_cast<T*>(I.rho[c]), 4, rho_dims, st_str, boxr);
@@ -1103,6 +1121,45 @@ class BatchGroup : public BatchGroupBase {
         for (int q = 0; q < n; ++q) {
           const BInst<T>& I = hinst[q];
           if (list == 0) hinst[q].ptile0 = n_ptiles;
+          if (kPar && list < 2) {
+            // parity tiles: every 32 x 4 position of the grid, both targets of the parity
+            const int A = par_a(list), B = par_b(list);
+            auto ext_of = [&](int c, int x0, int y0) {
+              if (!I.active[c] || class_moments_host(c) == 0) return 0;
+              const int lox = class_bit(c, 0) ? 1 : 0, hix = class_bit(c, 0) ? I.shape[c][0] - 1 : I.shape[c][0];
+              const int loy = class_bit(c, 1) ? 1 : 0, hiy = class_bit(c, 1) ? I.shape[c][1] - 1 : I.shape[c][1];
+              const int xv0 = std::max(lox - x0, 0), xv1 = std::min(hix - x0, TX);
+              const int yv0 = std::max(loy - y0, 0), yv1 = std::min(hiy - y0, TY);
+              return (xv1 > xv0 && yv1 > yv0) ? par_ext(xv0, xv1, yv0, yv1) : 0;
+            };
+            const int ny = I.shape[0][1], nx = I.shape[0][0];   // the eee grid covers both targets' cells
+            for (int y0 = 0; y0 < ny; y0 += TY)
+              for (int x0 = 0; x0 < nx; x0 += TX) {
+                const int ea = ext_of(A, x0, y0), eb = ext_of(B, x0, y0);
+                if (!ea && !eb) continue;
+                TTile tt;
+                std::memset(&tt, 0, sizeof(tt));
+                tt.inst = q;
+                tt.cls = list;   // the parity
+                tt.x0 = x0;
+                tt.y0 = y0;
+                tt.ext = ea;
+                tt.pad_[0] = eb;
+                tt.pslot = (list == 0 && ea) ? n_ptiles++ : -1;
+                tt.ns = I.ns;
+                tt.n_ck = I.n_ck;
+                tt.n_full = I.n_full;
+                tt.ne = I.ne;
+                tt.arg_fwd = arg_fwd[q];
+                tt.arg_adj = arg_adj[q];
+                tt.arg_int = arg_int[q];
+                tt.z = 0;
+                ttl[list].push_back(tt);
+              }
+            if (list == 0) hinst[q].n_ptile = n_ptiles - hinst[q].ptile0;
+            tend[list][q] = (int)ttl[list].size();
+            continue;
+          }
           for (int c = 0; c < 8; ++c) {
             if (!I.active[c] || (list < 2 && class_parity(c) != list) || class_moments_host(c) == 0) continue;
             int lo3[3], hi3[3];
@@ -1459,10 +1516,17 @@ class BatchGroup : public BatchGroupBase {
           return PN_OK;
         }
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
-        if (adj)
-          batch_tma_kernel<N, true, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
-        else
-          batch_tma_kernel<N, false, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
+        if constexpr (kPar) {
+          if (adj)
+            batch_par_kernel<N, true><<<grid, TB, par_smem, ls>>>(a);
+          else
+            batch_par_kernel<N, false><<<grid, TB, par_smem, ls>>>(a);
+        } else {
+          if (adj)
+            batch_tma_kernel<N, true, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
+          else
+            batch_tma_kernel<N, false, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
+        }
         PN_CUDA(cudaGetLastError());
         ++nl;
       }
@@ -1659,9 +1723,9 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
-  static constexpr int sweep_smem() {
-    return TmaLayout<N, DIMS>::SMEM > TmaIntLayout<N, DIMS>::SMEM ? TmaLayout<N, DIMS>::SMEM
-                                                                    : TmaIntLayout<N, DIMS>::SMEM;
+  int sweep_smem() const {
+    const int sub = kPar ? par_smem : TmaLayout<N, DIMS>::SMEM;
+    return std::max(sub, (int)TmaIntLayout<N, DIMS>::SMEM);
   }
 
   // plan both sweeps (before the graphs are captured) and size the persistent grid

@@ -144,7 +144,9 @@ constexpr int PLZ = 2 * PLO;        // floats per moment plane of a z-neighbour 
 enum {
   TM_ST_T = 0, TM_ST_X = 1, TM_ST_Y = 2, TM_ST_Z = 3,
   TM_LAM_T = 4, TM_LAM_X = 5, TM_LAM_Y = 6, TM_LAM_Z = 7,
-  TM_RHO = 8, TM_RBAR = 9, TM_KINDS = 10
+  TM_RHO = 8, TM_RBAR = 9,
+  TM_ST_N = 10, TM_LAM_N = 11,   // 36 x 5 neighbour boxes of the 2D parity tiles (pn_batch_par.cuh)
+  TM_KINDS = 12
 };
 
 template <int N>
@@ -1079,6 +1081,12 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_int_kernel(const _
   if (threadIdx.x == 0) bulk_wait_all();
 }
 
+}  // namespace pn
+
+#include "pn_batch_par.cuh"   // 2D parity tiles (used by the sweep kernel below)
+
+namespace pn {
+
 // ---------------------------------------------------------------------------------------------
 // one persistent launch per sweep
 // ---------------------------------------------------------------------------------------------
@@ -1154,6 +1162,7 @@ __device__ __forceinline__ bool wait_count(const int* p, int need) {
 template <int N, int DIMS>
 __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __grid_constant__ TSweep<N> S) {
   static_assert(TSTAGES == 1, "the sweep kernel stages one tile per CTA");
+  constexpr bool PAR = DIMS == 3 && PPT == 1;   // 2D: parity tiles for the sub-steps
   using LY = TmaLayout<N, DIMS>;
   using LI = TmaIntLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1231,7 +1240,10 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
         bulk_wait_read();   // the previous item's stores have read the stage
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         if (st.kind == TS_INT) tma_issue_int<N, DIMS>(IL, *tl, smem, &full[0]);
-        else if (st.kind == TS_ADJ) tma_issue<N, true, DIMS>(L, *tl, smem, &full[0]);
+        else if constexpr (PAR) {
+          if (st.kind == TS_ADJ) par_issue<N, true>(L, *tl, smem, &full[0]);
+          else par_issue<N, false>(L, *tl, smem, &full[0]);
+        } else if (st.kind == TS_ADJ) tma_issue<N, true, DIMS>(L, *tl, smem, &full[0]);
         else tma_issue<N, false, DIMS>(L, *tl, smem, &full[0]);
       }
     }
@@ -1265,6 +1277,10 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
     if (kind == TS_INT) {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LI::TIL);
       tma_int_cell_of<N, DIMS>(IL, tt, smem);
+    } else if constexpr (PAR) {
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
+      if (kind == TS_ADJ) par_tile<N, true>(L, tt, smem, red);
+      else par_tile<N, false>(L, tt, smem, red);
     } else {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LY::TIL);
       if (kind == TS_ADJ) tma_cell_of<N, true, DIMS>(L, tt, smem, red);
@@ -1273,7 +1289,7 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
     // the tile is released later (see pend): its tensor stores (sub-steps) or its rho_bar and
     // line sums (the integral's threads synchronised at its end) are then visible
     if (threadIdx.x == 0) {
-      const TTile& tt = *reinterpret_cast<const TTile*>(smem + (kind == TS_INT ? LI::TIL : LY::TIL));
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + (kind == TS_INT ? LI::TIL : PAR ? ParLayout<N>::TIL : LY::TIL));
       pend = (long long)k * S.n_solves + tt.inst;
       pend_generic = kind == TS_INT;
     }
