@@ -629,6 +629,7 @@ class BatchGroup : public BatchGroupBase {
   int* dstatus = nullptr;          // [0] status of the latest calls, [1] test expiries left
   bool test_expire = false;         // PN_BATCH_TEST_EXPIRE_WAIT
   int cta_cap = 0;                  // resident CTAs per SM of the tile kernels (0: occupancy)
+  bool class_tiles = false;         // PN_BATCH_CLASS_TILES
   // one persistent launch per sweep (TMA groups replayed as graphs, see batch_sweep_kernel): the
   // steps of each sweep are planned once before the graphs are captured
   bool sweep = false;
@@ -644,9 +645,11 @@ class BatchGroup : public BatchGroupBase {
   int* done_d = nullptr;            // [step][solve] completed tiles, zeroed before every sweep
   int sweep_grid = 0;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
-  // 2D groups update both target classes of a parity per tile (pn_batch_par.cuh)
+  // 2D groups update both target classes of a parity per tile (pn_batch_par.cuh) when two stages
+  // of the group's parity tiles fit in shared memory
   static constexpr bool kPar = DIMS == 3 && PPT == 1;
-  int par_smem = 0;                // dynamic shared memory of a parity tile (the group's elements)
+  bool par = false;
+  int par_stage = 0;               // shared memory of one parity-tile stage (the group's elements)
   // Creation never waits for the device: tables go up on `up`, whose event the first forward or
   // adjoint waits on in stream order, and the tape / density zeroing is enqueued with the first
   // forward; graphs are captured on `cap`, which has no work of its own.
@@ -900,6 +903,7 @@ class BatchGroup : public BatchGroupBase {
     if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       test_expire = (flags & PN_BATCH_TEST_EXPIRE_WAIT) != 0;
       cta_cap = (flags >> PN_BATCH_CTAS_PER_SM_SHIFT) & 15;
+      class_tiles = (flags & PN_BATCH_CLASS_TILES) != 0;
       if (!(flags & PN_BATCH_GENERIC_KERNELS))
         if ((rc = build_tma())) return rc;
     } else {
@@ -967,15 +971,25 @@ class BatchGroup : public BatchGroupBase {
       int occ_f = 0, occ_a = 0;
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_tma_kernel<N, false, DIMS>, NTS, LY::SMEM));
       PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_tma_kernel<N, true, DIMS>, NTS, LY::SMEM));
+      par = false;
       if constexpr (kPar) {
         int ne_max = 1;
         for (int q = 0; q < n; ++q) ne_max = std::max(ne_max, hinst[q].ne);
-        par_smem = ParLayout<N>::smem(ne_max);
-        if (par_smem + 2048 > smem_optin) return PN_OK;
-        PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, par_smem));
-        PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, par_smem));
-        PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, batch_par_kernel<N, false>, TB, par_smem));
-        PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, batch_par_kernel<N, true>, TB, par_smem));
+        par_stage = (ParLayout<N>::smem(ne_max) + 127) / 128 * 128;
+        if (2 * par_stage + 2048 <= smem_optin && !class_tiles) {
+          PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2 * par_stage));
+          PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2 * par_stage));
+          int pf = 0, pa = 0;
+          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, batch_par_kernel<N, false>, PAR_NT, 2 * par_stage));
+          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, batch_par_kernel<N, true>, PAR_NT, 2 * par_stage));
+          if (pf >= 1 && pa >= 1) {
+            par = true;
+            occ_f = pf;
+            occ_a = pa;
+          }
+        }
       }
       if (occ_f < 1 || occ_a < 1) return PN_OK;
       if (cta_cap > 0) {
@@ -1062,7 +1076,7 @@ class BatchGroup : public BatchGroupBase {
           if (DIMS == 7)
             ok = ok && encode_f32(&m[TM_ST_Z], I.slots + I.dev_off[c], 5, st_dims, st_str, boxz) &&
                  encode_f32(&m[TM_LAM_Z], I.lam + I.dev_off[c], 4, st_dims, st_str, boxz);
-          if (kPar) {
+          if (par) {
             const int boxn[5] = {NBW, NBH, 1, nm, 1};
             ok = ok && encode_f32(&m[TM_ST_N], I.slots + I.dev_off[c], 5, st_dims, st_str, boxn) &&
                  encode_f32(&m[TM_LAM_N], I.lam + I.dev_off[c], 4, st_dims, st_str, boxn);
@@ -1121,7 +1135,7 @@ class BatchGroup : public BatchGroupBase {
         for (int q = 0; q < n; ++q) {
           const BInst<T>& I = hinst[q];
           if (list == 0) hinst[q].ptile0 = n_ptiles;
-          if (kPar && list < 2) {
+          if (par && list < 2) {
             // parity tiles: every 32 x 4 position of the grid, both targets of the parity
             const int A = par_a(list), B = par_b(list);
             auto ext_of = [&](int c, int x0, int y0) {
@@ -1516,11 +1530,13 @@ class BatchGroup : public BatchGroupBase {
           return PN_OK;
         }
         const int grid = std::min(nb, tma_grid[adj ? 1 : 0]);
-        if constexpr (kPar) {
-          if (adj)
-            batch_par_kernel<N, true><<<grid, TB, par_smem, ls>>>(a);
-          else
-            batch_par_kernel<N, false><<<grid, TB, par_smem, ls>>>(a);
+        if (par) {
+          if constexpr (kPar) {
+            if (adj)
+              batch_par_kernel<N, true><<<grid, PAR_NT, 2 * par_stage, ls>>>(a);
+            else
+              batch_par_kernel<N, false><<<grid, PAR_NT, 2 * par_stage, ls>>>(a);
+          }
         } else {
           if (adj)
             batch_tma_kernel<N, true, DIMS><<<grid, NTS, TmaLayout<N, DIMS>::SMEM, ls>>>(a);
@@ -1704,6 +1720,7 @@ class BatchGroup : public BatchGroupBase {
       S.n_solves = n;
       S.pr = pr;
       S.K = K;
+      S.par = par ? 1 : 0;
       cudaLaunchConfig_t cfg;
       std::memset(&cfg, 0, sizeof(cfg));
       cfg.gridDim = dim3((unsigned)std::min(P.n_items, sweep_grid));
@@ -1724,7 +1741,7 @@ class BatchGroup : public BatchGroupBase {
   }
 
   int sweep_smem() const {
-    const int sub = kPar ? par_smem : TmaLayout<N, DIMS>::SMEM;
+    const int sub = par ? par_stage : TmaLayout<N, DIMS>::SMEM;
     return std::max(sub, (int)TmaIntLayout<N, DIMS>::SMEM);
   }
 

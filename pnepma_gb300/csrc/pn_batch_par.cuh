@@ -15,9 +15,10 @@
 
 namespace pn {
 
-// resident CTAs per SM the parity-tile kernel is compiled for (shared memory allows four)
+// resident CTAs per SM the two-stage parity-tile kernel is compiled for (P11: shared memory
+// allows two)
 #ifndef PN_PAR_MINB
-#define PN_PAR_MINB 4
+#define PN_PAR_MINB 2
 #endif
 
 constexpr int NBW = 36;            // neighbour box width: x0 - 4 .. x0 + 31, or x0 .. x0 + 35
@@ -114,7 +115,7 @@ __device__ __forceinline__ void par_issue(const TLaunch<N>& L, const TTile& tt, 
 // The single-axis ghost points target C reads, computed into the shared neighbour boxes
 // (ghost_fill's arithmetic, as tile_ghosts).  own: C's target box; fx / fy: the boxes of C ^ 4 and
 // C ^ 2.  All threads call this; the caller syncs before reading.
-template <int N, int C, int KIND>
+template <int N, int C, int KIND, int NT>
 __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, int ext,
                                            const float* own, float* fx, float* fy, double bc) {
   constexpr bool ADJ = KIND == 1;
@@ -137,7 +138,7 @@ __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& 
         const int icol = left ? 1 : ncx - 1 - tt.x0;      // its box starts at x0)
         const bool src = !ADJ && !left;
         const int nrow = yhi - ylo;
-        for (int w = threadIdx.x; w < nrow * nf; w += TB) {
+        for (int w = threadIdx.x; w < nrow * nf; w += NT) {
           const int ty = ylo + w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
@@ -166,7 +167,7 @@ __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& 
         const int crow = left ? 0 : ncy - 1 - tt.y0;       // the face cells' row in the target box
         const int grow = left ? 0 : ncy - tt.y0;           // F's ghost and first interior row (F odd in y:
         const int irow = left ? 1 : ncy - 1 - tt.y0;       // its box starts at y0)
-        for (int w = threadIdx.x; w < nx * nf; w += TB) {
+        for (int w = threadIdx.x; w < nx * nf; w += NT) {
           const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
@@ -225,10 +226,10 @@ __device__ __forceinline__ void par_advection(float* acc, const float* fx, const
 template <int N, int C, bool ADJ>
 __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, int ext, float* own, const float* fx,
                                           const float* fy, const float* rh, const TSolve& I, const ArgRow<N>& ar,
-                                          float dt, double* part) {
+                                          float dt, double* part, int pt) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n > 0) {
-    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int tx = pt % TX, ty = pt / TX;
     const int xv0 = ext & 255, xv1 = (ext >> 8) & 255, ylo = (ext >> 16) & 255, yhi = (ext >> 24) & 255;
     if (!(tx >= xv0 && tx < xv1 && ty >= ylo && ty < yhi)) return;
     const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
@@ -307,10 +308,14 @@ __device__ __forceinline__ void par_store(const TLaunch<N>& L, const TTile& tt, 
     tma_store_5d(mp + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, box);
 }
 
-// One parity tile: one sub-step, or the two of a fused launch, on both targets.
-template <int N, int P, bool ADJ>
+// One parity tile: one sub-step, or the two of a fused launch, on both targets.  With NT = TB
+// threads each thread updates one point of each target; with NT = 2 TB warps 0-3 update A and
+// warps 4-7 update B.  Thread 0 calls `pre` once, after the first pass's ghosts (the two-stage
+// kernel issues the next tile's loads there).
+template <int N, int P, bool ADJ, int NT, class Pre>
 __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                           double (&red)[TB / 32][MAXR]) {
+                                           double (&red)[TB / 32][MAXR], Pre& pre) {
+  static_assert(NT == TB || NT == 2 * TB, "one or two threads per tile position");
   using LY = ParLayout<N>;
   constexpr int A = par_a(P), B = par_b(P), F1 = A ^ 4, F2 = A ^ 2;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
@@ -334,21 +339,33 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
     const ArgRow<N>& ar = rows[pass];
     const float dt = L.sub == 2 ? I.dE : half;
     // ghosts: A reads F1 along x and F2 along y, B reads F2 along x and F1 along y
-    par_ghosts<N, A, ADJ ? 1 : 0>(inst, I, tt, extA, ownA, nb1, nb2, ADJ ? 0.0 : ar.bc);
-    par_ghosts<N, B, ADJ ? 1 : 0>(inst, I, tt, extB, ownB, nb2, nb1, ADJ ? 0.0 : ar.bc);
-    if (second && threadIdx.x == 0) bulk_wait_read();   // the first pass's stores have read the boxes
+    par_ghosts<N, A, ADJ ? 1 : 0, NT>(inst, I, tt, extA, ownA, nb1, nb2, ADJ ? 0.0 : ar.bc);
+    par_ghosts<N, B, ADJ ? 1 : 0, NT>(inst, I, tt, extB, ownB, nb2, nb1, ADJ ? 0.0 : ar.bc);
+    if (threadIdx.x == 0) {
+      if (pass == p0) pre();
+      if (second) bulk_wait_read();   // the first pass's stores have read the boxes
+    }
     __syncthreads();
     double part[MAXR];
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
-    par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part);
-    par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part);
+    if constexpr (NT == TB) {
+      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x);
+      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x);
+    } else if (threadIdx.x < TB) {   // warp-uniform
+      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x);
+    } else {
+      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x - TB);
+    }
     if (!ADJ && A == 0 && L.partial != nullptr && tt.pslot >= 0) {   // block-uniform
-      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-      if (L.pr <= 1) warp_partials<1>(part, lane, w, L.pr, red);
-      else if (L.pr <= 2) warp_partials<2>(part, lane, w, L.pr, red);
-      else if (L.pr <= 4) warp_partials<4>(part, lane, w, L.pr, red);
-      else warp_partials<8>(part, lane, w, L.pr, red);
+      // A's threads (the first TB) hold the partials: the same reduction as batch_tma_kernel's
+      if (threadIdx.x < TB) {   // warp-uniform
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (L.pr <= 1) warp_partials<1>(part, lane, w, L.pr, red);
+        else if (L.pr <= 2) warp_partials<2>(part, lane, w, L.pr, red);
+        else if (L.pr <= 4) warp_partials<4>(part, lane, w, L.pr, red);
+        else warp_partials<8>(part, lane, w, L.pr, red);
+      }
       __syncthreads();
       if (threadIdx.x < L.pr) {
         double v = 0.0;
@@ -375,53 +392,67 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
   (void)F1; (void)F2;
 }
 
-template <int N, bool ADJ>
+template <int N, bool ADJ, int NT, class Pre>
 __device__ __forceinline__ void par_tile(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[TB / 32][MAXR]) {
-  if (tt.cls == 0) par_tile_p<N, 0, ADJ>(L, tt, st, red);
-  else par_tile_p<N, 1, ADJ>(L, tt, st, red);
+                                         double (&red)[TB / 32][MAXR], Pre& pre) {
+  if (tt.cls == 0) par_tile_p<N, 0, ADJ, NT>(L, tt, st, red, pre);
+  else par_tile_p<N, 1, ADJ, NT>(L, tt, st, red, pre);
 }
 
-// Persistent CTAs over a launch's parity tiles (batch_tma_kernel's structure; 2D groups).
+// Persistent CTAs over a launch's parity tiles, two stages each: the next tile's loads are issued
+// into the other stage once the current tile's ghosts are formed, so that they land while the
+// current tile is updated.  2 TB threads: one per target point of a tile.  The dynamic shared
+// memory holds the two stages (its size / 2 each, a multiple of 128 bytes).
+constexpr int PAR_NT = 2 * TB;
+
 template <int N, bool ADJ>
-__global__ void __launch_bounds__(TB, PN_PAR_MINB) batch_par_kernel(const __grid_constant__ TLaunch<N> L) {
+__global__ void __launch_bounds__(PAR_NT, PN_PAR_MINB) batch_par_kernel(const __grid_constant__ TLaunch<N> L) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) unsigned long long full[1];
+  __shared__ __align__(8) unsigned long long full[2];
   __shared__ double red[TB / 32][MAXR];
-  if ((smem_u32(smem) & 127u) != 0u) {
+  unsigned dyn;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+  const unsigned SB = dyn / 2;
+  if ((smem_u32(smem) & 127u) != 0u || (SB & 127u) != 0u) {
     if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
     return;
   }
   if (threadIdx.x == 0) {
     mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   const int G = gridDim.x;
-  unsigned phase = 0;
+  if (threadIdx.x == 0 && (int)blockIdx.x < L.n_tiles) par_issue<N, ADJ>(L, L.tiles[blockIdx.x], smem, &full[0]);
   for (int k = 0; (int)blockIdx.x + k * G < L.n_tiles; ++k) {
-    const int t = blockIdx.x + k * G;
-    if (threadIdx.x == 0) {
-      bulk_wait_read();   // the stores issued from the stage have read it
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      par_issue<N, ADJ>(L, L.tiles[t], smem, &full[0]);
-    }
-    bool ok = mbar_wait_bounded(&full[0], phase);
+    // tile k lives in stage k & 1, use k >> 1 of its barrier; no other loads are in flight
+    const int s = k & 1;
+    const unsigned phase = (unsigned)(k >> 1) & 1u;
+    unsigned char* st = smem + s * SB;
+    bool ok = mbar_wait_bounded(&full[s], phase);
     if (L.test_expire != nullptr && k == 0 && threadIdx.x == 0 && ok && *(volatile int*)L.test_expire > 0 &&
         atomicSub(L.test_expire, 1) > 0)
       ok = false;   // test hook: report a completed wait as run out (see batch_tma_kernel)
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
         atomicExch(L.status, (int)PN_ERR_TIMEOUT);
-        mbar_wait_bounded(&full[0], phase);   // let the copies in flight land
+        mbar_wait_bounded(&full[s], phase);   // let the copies in flight land
         bulk_wait_all();
       }
       __syncthreads();
       return;
     }
-    phase ^= 1u;
-    const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
-    par_tile<N, ADJ>(L, tt, smem, red);
+    const TTile& tt = *reinterpret_cast<const TTile*>(st + ParLayout<N>::TIL);
+    const int tn = (int)blockIdx.x + (k + 1) * G;
+    auto pre = [&]() {
+      if (tn < L.n_tiles) {
+        bulk_wait_read();   // the previous tile's stores have read the other stage
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        par_issue<N, ADJ>(L, L.tiles[tn], smem + (s ^ 1) * SB, &full[s ^ 1]);
+      }
+    };
+    par_tile<N, ADJ, PAR_NT>(L, tt, st, red, pre);
   }
   if (threadIdx.x == 0) bulk_wait_all();
 }

@@ -1130,6 +1130,7 @@ struct TSweep {
   int* done;             // [step][solve]: tiles of the solve completed
   int n_steps, n_items, n_solves;
   int pr, K;
+  int par;               // the sub-step lists hold parity tiles (2D)
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -1162,7 +1163,7 @@ __device__ __forceinline__ bool wait_count(const int* p, int need) {
 template <int N, int DIMS>
 __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __grid_constant__ TSweep<N> S) {
   static_assert(TSTAGES == 1, "the sweep kernel stages one tile per CTA");
-  constexpr bool PAR = DIMS == 3 && PPT == 1;   // 2D: parity tiles for the sub-steps
+  constexpr bool PAR_OK = DIMS == 3 && PPT == 1;   // 2D groups may use parity tiles (S.par)
   using LY = TmaLayout<N, DIMS>;
   using LI = TmaIntLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -1240,9 +1241,11 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
         bulk_wait_read();   // the previous item's stores have read the stage
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         if (st.kind == TS_INT) tma_issue_int<N, DIMS>(IL, *tl, smem, &full[0]);
-        else if constexpr (PAR) {
-          if (st.kind == TS_ADJ) par_issue<N, true>(L, *tl, smem, &full[0]);
-          else par_issue<N, false>(L, *tl, smem, &full[0]);
+        else if (PAR_OK && S.par) {
+          if constexpr (PAR_OK) {
+            if (st.kind == TS_ADJ) par_issue<N, true>(L, *tl, smem, &full[0]);
+            else par_issue<N, false>(L, *tl, smem, &full[0]);
+          }
         } else if (st.kind == TS_ADJ) tma_issue<N, true, DIMS>(L, *tl, smem, &full[0]);
         else tma_issue<N, false, DIMS>(L, *tl, smem, &full[0]);
       }
@@ -1277,10 +1280,13 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
     if (kind == TS_INT) {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LI::TIL);
       tma_int_cell_of<N, DIMS>(IL, tt, smem);
-    } else if constexpr (PAR) {
-      const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
-      if (kind == TS_ADJ) par_tile<N, true>(L, tt, smem, red);
-      else par_tile<N, false>(L, tt, smem, red);
+    } else if (PAR_OK && S.par) {
+      if constexpr (PAR_OK) {
+        const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
+        auto none = []() {};
+        if (kind == TS_ADJ) par_tile<N, true, NTS>(L, tt, smem, red, none);
+        else par_tile<N, false, NTS>(L, tt, smem, red, none);
+      }
     } else {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LY::TIL);
       if (kind == TS_ADJ) tma_cell_of<N, true, DIMS>(L, tt, smem, red);
@@ -1289,7 +1295,8 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
     // the tile is released later (see pend): its tensor stores (sub-steps) or its rho_bar and
     // line sums (the integral's threads synchronised at its end) are then visible
     if (threadIdx.x == 0) {
-      const TTile& tt = *reinterpret_cast<const TTile*>(smem + (kind == TS_INT ? LI::TIL : PAR ? ParLayout<N>::TIL : LY::TIL));
+      const int til = kind == TS_INT ? LI::TIL : (PAR_OK && S.par) ? ParLayout<N>::TIL : LY::TIL;
+      const TTile& tt = *reinterpret_cast<const TTile*>(smem + til);
       pend = (long long)k * S.n_solves + tt.inst;
       pend_generic = kind == TS_INT;
     }
