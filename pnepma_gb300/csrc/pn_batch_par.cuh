@@ -221,12 +221,14 @@ __device__ __forceinline__ void par_advection(float* acc, const float* fx, const
   }
 }
 
-// One point of target C (tma_update's arithmetic): the new values replace the old ones in C's
-// target box.  Intensity partials (eee, forward) accumulate into part.
+// One point of target C (tma_update's arithmetic).  The new values go to memory at `dst` (C's
+// state slot or adjoint state; none if null), one coalesced store per moment, and with `keep`
+// also replace the old ones in C's target box (read again by the second pass of a fused launch).
+// Intensity partials (eee, forward) accumulate into part.
 template <int N, int C, bool ADJ>
 __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, int ext, float* own, const float* fx,
                                           const float* fy, const float* rh, const TSolve& I, const ArgRow<N>& ar,
-                                          float dt, double* part, int pt) {
+                                          float dt, double* part, int pt, float* dst, bool keep) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n > 0) {
     const int tx = pt % TX, ty = pt / TX;
@@ -263,6 +265,8 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
       rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
       S = fmaf(rr[e], ar.s[e], S);
     }
+    float* const gp = dst == nullptr ? nullptr : dst + (long long)j * I.px[C] + i;
+    const long long gms = I.ms[C];
     const float invS = recip(S);
     const float dts = dt * invS;
     constexpr unsigned mask = Ord<N>::deg_mask(C);
@@ -286,7 +290,8 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
       const float q = (m == 0) ? q0 : 0.0f;
       const float num = fmaf(-Cl[l], u, q - acc[m]);   // (q - A u) - C_l u
       const float unew = fmaf(num, gl[l], u);
-      own[m * PLO + lo] = unew;
+      if (keep) own[m * PLO + lo] = unew;
+      if (gp != nullptr) gp[m * gms] = unew;
       if constexpr (C == 0 && !ADJ) {
         if (m == 0 && want_part) {
 #pragma unroll
@@ -298,23 +303,14 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
   }
 }
 
-// store target class C's box from `box` (thread 0): the adjoint state, or state slot `slot`
-template <int N, bool ADJ>
-__device__ __forceinline__ void par_store(const TLaunch<N>& L, const TTile& tt, int C, const unsigned char* box, int slot) {
-  const CUtensorMap* mp = L.maps + ((long long)tt.inst * 8 + C) * TM_KINDS;
-  if (ADJ)
-    tma_store_4d(mp + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, box);
-  else
-    tma_store_5d(mp + TM_ST_T, tt.x0, tt.y0, tt.z, 0, slot, box);
-}
-
 // One parity tile: one sub-step, or the two of a fused launch, on both targets.  With NT = TB
 // threads each thread updates one point of each target; with NT = 2 TB warps 0-3 update A and
-// warps 4-7 update B.  Thread 0 calls `pre` once, after the first pass's ghosts (the two-stage
-// kernel issues the next tile's loads there).
-template <int N, int P, bool ADJ, int NT, class Pre>
+// warps 4-7 update B.  The threads store their points' new values themselves (no tensor store
+// reads the stage afterwards, so the stage can be refilled once the tile's threads are past its
+// last barrier).
+template <int N, int P, bool ADJ, int NT>
 __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                           double (&red)[TB / 32][MAXR], Pre& pre) {
+                                           double (&red)[TB / 32][MAXR]) {
   static_assert(NT == TB || NT == 2 * TB, "one or two threads per tile position");
   using LY = ParLayout<N>;
   constexpr int A = par_a(P), B = par_b(P), F1 = A ^ 4, F2 = A ^ 2;
@@ -341,21 +337,34 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
     // ghosts: A reads F1 along x and F2 along y, B reads F2 along x and F1 along y
     par_ghosts<N, A, ADJ ? 1 : 0, NT>(inst, I, tt, extA, ownA, nb1, nb2, ADJ ? 0.0 : ar.bc);
     par_ghosts<N, B, ADJ ? 1 : 0, NT>(inst, I, tt, extB, ownB, nb2, nb1, ADJ ? 0.0 : ar.bc);
-    if (threadIdx.x == 0) {
-      if (pass == p0) pre();
-      if (second) bulk_wait_read();   // the first pass's stores have read the boxes
-    }
     __syncthreads();
+    // where the new values go: the adjoint state, or the state slot this pass writes (if any)
+    float* gA = nullptr;
+    float* gB = nullptr;
+    if (ADJ) {
+      gA = I.lam + I.dev_off[A];
+      gB = I.lam + I.dev_off[B];
+    } else {
+      int slot = -1;
+      if (!fused) slot = sub_slots(tt, L.mode, L.j, L.sub, L.K).out;
+      else if (second || state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
+        slot = slot_index(tt.ns, tt.n_full, tt.n_ck, second ? L.j - 1 : L.j, L.K, segment);
+      if (slot >= 0) {
+        gA = I.slots + I.dev_off[A] + (long long)slot * I.slot_elems;
+        gB = I.slots + I.dev_off[B] + (long long)slot * I.slot_elems;
+      }
+    }
+    const bool keep = fused && !second;   // the second pass reads the first pass's values
     double part[MAXR];
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
     if constexpr (NT == TB) {
-      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x);
-      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x);
+      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x, gA, keep);
+      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x, gB, keep);
     } else if (threadIdx.x < TB) {   // warp-uniform
-      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x);
+      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x, gA, keep);
     } else {
-      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x - TB);
+      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x - TB, gB, keep);
     }
     if (!ADJ && A == 0 && L.partial != nullptr && tt.pslot >= 0) {   // block-uniform
       // A's threads (the first TB) hold the partials: the same reduction as batch_tma_kernel's
@@ -374,33 +383,22 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
         L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
       }
     }
-    __syncthreads();   // both target boxes hold the new values
-    if (threadIdx.x == 0) {
-      int slot = -1;
-      if (ADJ) slot = 0;
-      else if (!fused) slot = sub_slots(tt, L.mode, L.j, L.sub, L.K).out;
-      else if (second || state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
-        slot = slot_index(tt.ns, tt.n_full, tt.n_ck, second ? L.j - 1 : L.j, L.K, segment);
-      if (slot >= 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        if (Ord<N>::n(A) > 0) par_store<N, ADJ>(L, tt, A, st + LY::OWNA, slot);
-        if (Ord<N>::n(B) > 0) par_store<N, ADJ>(L, tt, B, st + LY::OWNB, slot);
-        bulk_commit();
-      }
-    }
+    // the next pass's ghosts read the target boxes and rewrite the neighbour boxes; after the
+    // last pass the stage may be refilled
+    __syncthreads();
   }
   (void)F1; (void)F2;
 }
 
-template <int N, bool ADJ, int NT, class Pre>
+template <int N, bool ADJ, int NT>
 __device__ __forceinline__ void par_tile(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[TB / 32][MAXR], Pre& pre) {
-  if (tt.cls == 0) par_tile_p<N, 0, ADJ, NT>(L, tt, st, red, pre);
-  else par_tile_p<N, 1, ADJ, NT>(L, tt, st, red, pre);
+                                         double (&red)[TB / 32][MAXR]) {
+  if (tt.cls == 0) par_tile_p<N, 0, ADJ, NT>(L, tt, st, red);
+  else par_tile_p<N, 1, ADJ, NT>(L, tt, st, red);
 }
 
 // Persistent CTAs over a launch's parity tiles, two stages each: the next tile's loads are issued
-// into the other stage once the current tile's ghosts are formed, so that they land while the
+// into the other stage as soon as the current tile's have landed, so that they land while the
 // current tile is updated.  2 TB threads: one per target point of a tile.  The dynamic shared
 // memory holds the two stages (its size / 2 each, a multiple of 128 bytes).
 constexpr int PAR_NT = 2 * TB;
@@ -443,18 +441,15 @@ __global__ void __launch_bounds__(PAR_NT, PN_PAR_MINB) batch_par_kernel(const __
       __syncthreads();
       return;
     }
-    const TTile& tt = *reinterpret_cast<const TTile*>(st + ParLayout<N>::TIL);
+    // the other stage's last readers (tile k - 1) are past its final barrier
     const int tn = (int)blockIdx.x + (k + 1) * G;
-    auto pre = [&]() {
-      if (tn < L.n_tiles) {
-        bulk_wait_read();   // the previous tile's stores have read the other stage
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        par_issue<N, ADJ>(L, L.tiles[tn], smem + (s ^ 1) * SB, &full[s ^ 1]);
-      }
-    };
-    par_tile<N, ADJ, PAR_NT>(L, tt, st, red, pre);
+    if (threadIdx.x == 0 && tn < L.n_tiles) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      par_issue<N, ADJ>(L, L.tiles[tn], smem + (s ^ 1) * SB, &full[s ^ 1]);
+    }
+    const TTile& tt = *reinterpret_cast<const TTile*>(st + ParLayout<N>::TIL);
+    par_tile<N, ADJ, PAR_NT>(L, tt, st, red);
   }
-  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 }  // namespace pn
