@@ -263,7 +263,7 @@ enum pn_batch_flags {
   PN_BATCH_SWEEP_LAUNCH = 16,
   /* FP32 2D groups: one TMA tile per target class (a 32 x 4 box, a 40 x 4 x-neighbour box and a
      32 x 5 y-neighbour box) instead of parity tiles (both targets of a parity at one 32 x 4
-     position, one 36 x 5 box per neighbour class, two stages per CTA).  Identical results */
+     position, one 36 x 5 box per neighbour class).  Identical results */
   PN_BATCH_CLASS_TILES = 32,
   /* bits 8..11: resident CTAs per SM of the persistent TMA tile kernels, 1..15 (0: as many as the
      shared memory and registers allow); fewer CTAs each walk more tiles.  One of the autotuner's

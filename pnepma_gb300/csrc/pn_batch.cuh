@@ -645,8 +645,7 @@ class BatchGroup : public BatchGroupBase {
   int* done_d = nullptr;            // [step][solve] completed tiles, zeroed before every sweep
   int sweep_grid = 0;
   int tma_grid[2] = {0, 0};        // persistent CTAs of the forward / adjoint TMA kernel
-  // 2D groups update both target classes of a parity per tile (pn_batch_par.cuh) when two stages
-  // of the group's parity tiles fit in shared memory
+  // 2D groups update both target classes of a parity per tile (pn_batch_par.cuh)
   static constexpr bool kPar = DIMS == 3 && PPT == 1;
   bool par = false;
   int par_stage = 0;               // shared memory of one parity-tile stage (the group's elements)
@@ -976,14 +975,14 @@ class BatchGroup : public BatchGroupBase {
         int ne_max = 1;
         for (int q = 0; q < n; ++q) ne_max = std::max(ne_max, hinst[q].ne);
         par_stage = (ParLayout<N>::smem(ne_max) + 127) / 128 * 128;
-        if (2 * par_stage + 2048 <= smem_optin && !class_tiles) {
+        if (par_stage + 2048 <= smem_optin && !class_tiles) {
           PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       2 * par_stage));
+                                       par_stage));
           PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       2 * par_stage));
+                                       par_stage));
           int pf = 0, pa = 0;
-          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, batch_par_kernel<N, false>, PAR_NT, 2 * par_stage));
-          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, batch_par_kernel<N, true>, PAR_NT, 2 * par_stage));
+          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, batch_par_kernel<N, false>, TB, par_stage));
+          PN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, batch_par_kernel<N, true>, TB, par_stage));
           if (pf >= 1 && pa >= 1) {
             par = true;
             occ_f = pf;
@@ -1533,9 +1532,9 @@ class BatchGroup : public BatchGroupBase {
         if (par) {
           if constexpr (kPar) {
             if (adj)
-              batch_par_kernel<N, true><<<grid, PAR_NT, 2 * par_stage, ls>>>(a);
+              batch_par_kernel<N, true><<<grid, TB, par_stage, ls>>>(a);
             else
-              batch_par_kernel<N, false><<<grid, PAR_NT, 2 * par_stage, ls>>>(a);
+              batch_par_kernel<N, false><<<grid, TB, par_stage, ls>>>(a);
           }
         } else {
           if (adj)

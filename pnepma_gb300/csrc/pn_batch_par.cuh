@@ -15,10 +15,9 @@
 
 namespace pn {
 
-// resident CTAs per SM the two-stage parity-tile kernel is compiled for (P11: shared memory
-// allows two)
+// resident CTAs per SM the parity-tile kernel is compiled for (shared memory allows four)
 #ifndef PN_PAR_MINB
-#define PN_PAR_MINB 2
+#define PN_PAR_MINB 4
 #endif
 
 constexpr int NBW = 36;            // neighbour box width: x0 - 4 .. x0 + 31, or x0 .. x0 + 35
@@ -59,8 +58,10 @@ struct ParLayout {
   static constexpr int smem(int ne) { return RHOA + 2 * ne * PLO * 4; }
 };
 
-// Issue a parity tile's loads (one thread); `tt` is the tile record in global memory.
-template <int N, bool ADJ>
+// Issue a parity tile's loads (one thread); `tt` is the tile record in global memory.  PART 0:
+// all of them; 1: all but the target boxes (and the barrier's byte count for all); 2: the target
+// boxes only.
+template <int N, bool ADJ, int PART = 0>
 __device__ __forceinline__ void par_issue(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
                                           unsigned long long* bar) {
   using LY = ParLayout<N>;
@@ -90,18 +91,24 @@ __device__ __forceinline__ void par_issue(const TLaunch<N>& L, const TTile& tt, 
   }
   const unsigned bytes = 4u * (unsigned)(PLO * (nA + nB) + PLN * (n1 + n2) + 2 * PLO * tt.ne) +
                          (unsigned)(n_rows * sizeof(ArgRow<N>) + sizeof(TTile) + sizeof(TSolve));
-  mbar_expect_tx(bar, bytes);
   const CUtensorMap* mp = L.maps + (long long)tt.inst * 8 * TM_KINDS;
+  if (PART != 2) mbar_expect_tx(bar, bytes);   // before any of the copies it counts
+  if (PART != 1) {
+    if (ADJ) {
+      if (nA > 0) tma_load_4d(st + LY::OWNA, mp + A * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
+      if (nB > 0) tma_load_4d(st + LY::OWNB, mp + B * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
+    } else {
+      if (nA > 0) tma_load_5d(st + LY::OWNA, mp + A * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
+      if (nB > 0) tma_load_5d(st + LY::OWNB, mp + B * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
+    }
+  }
+  if (PART == 2) return;
   const int x1 = tt.x0 + nb_dx(F1), y1 = tt.y0 + nb_dy(F1);
   const int x2 = tt.x0 + nb_dx(F2), y2 = tt.y0 + nb_dy(F2);
   if (ADJ) {
-    if (nA > 0) tma_load_4d(st + LY::OWNA, mp + A * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
-    if (nB > 0) tma_load_4d(st + LY::OWNB, mp + B * TM_KINDS + TM_LAM_T, tt.x0, tt.y0, tt.z, 0, bar);
     if (n1 > 0) tma_load_4d(st + LY::NB1, mp + F1 * TM_KINDS + TM_LAM_N, x1, y1, tt.z, 0, bar);
     if (n2 > 0) tma_load_4d(st + LY::NB2, mp + F2 * TM_KINDS + TM_LAM_N, x2, y2, tt.z, 0, bar);
   } else {
-    if (nA > 0) tma_load_5d(st + LY::OWNA, mp + A * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
-    if (nB > 0) tma_load_5d(st + LY::OWNB, mp + B * TM_KINDS + TM_ST_T, tt.x0, tt.y0, tt.z, 0, sl.own, bar);
     if (n1 > 0) tma_load_5d(st + LY::NB1, mp + F1 * TM_KINDS + TM_ST_N, x1, y1, tt.z, 0, sl.from, bar);
     if (n2 > 0) tma_load_5d(st + LY::NB2, mp + F2 * TM_KINDS + TM_ST_N, x2, y2, tt.z, 0, sl.from, bar);
   }
@@ -115,7 +122,7 @@ __device__ __forceinline__ void par_issue(const TLaunch<N>& L, const TTile& tt, 
 // The single-axis ghost points target C reads, computed into the shared neighbour boxes
 // (ghost_fill's arithmetic, as tile_ghosts).  own: C's target box; fx / fy: the boxes of C ^ 4 and
 // C ^ 2.  All threads call this; the caller syncs before reading.
-template <int N, int C, int KIND, int NT>
+template <int N, int C, int KIND>
 __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& S, const TTile& tt, int ext,
                                            const float* own, float* fx, float* fy, double bc) {
   constexpr bool ADJ = KIND == 1;
@@ -138,7 +145,7 @@ __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& 
         const int icol = left ? 1 : ncx - 1 - tt.x0;      // its box starts at x0)
         const bool src = !ADJ && !left;
         const int nrow = yhi - ylo;
-        for (int w = threadIdx.x; w < nrow * nf; w += NT) {
+        for (int w = threadIdx.x; w < nrow * nf; w += TB) {
           const int ty = ylo + w / nf, r = w % nf;
           float bv = 0.0f;
 #pragma unroll
@@ -167,7 +174,7 @@ __device__ __forceinline__ void par_ghosts(const BInst<float>& I, const TSolve& 
         const int crow = left ? 0 : ncy - 1 - tt.y0;       // the face cells' row in the target box
         const int grow = left ? 0 : ncy - tt.y0;           // F's ghost and first interior row (F odd in y:
         const int irow = left ? 1 : ncy - 1 - tt.y0;       // its box starts at y0)
-        for (int w = threadIdx.x; w < nx * nf; w += NT) {
+        for (int w = threadIdx.x; w < nx * nf; w += TB) {
           const int tx = xv0 + w % nx, r = w / nx;
           float bv = 0.0f;
 #pragma unroll
@@ -221,17 +228,15 @@ __device__ __forceinline__ void par_advection(float* acc, const float* fx, const
   }
 }
 
-// One point of target C (tma_update's arithmetic).  The new values go to memory at `dst` (C's
-// state slot or adjoint state; none if null), one coalesced store per moment, and with `keep`
-// also replace the old ones in C's target box (read again by the second pass of a fused launch).
-// Intensity partials (eee, forward) accumulate into part.
+// One point of target C (tma_update's arithmetic): the new values replace the old ones in C's
+// target box.  Intensity partials (eee, forward) accumulate into part.
 template <int N, int C, bool ADJ>
 __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, int ext, float* own, const float* fx,
                                           const float* fy, const float* rh, const TSolve& I, const ArgRow<N>& ar,
-                                          float dt, double* part, int pt, float* dst, bool keep) {
+                                          float dt, double* part) {
   constexpr int n = Ord<N>::n(C);
   if constexpr (n > 0) {
-    const int tx = pt % TX, ty = pt / TX;
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int xv0 = ext & 255, xv1 = (ext >> 8) & 255, ylo = (ext >> 16) & 255, yhi = (ext >> 24) & 255;
     if (!(tx >= xv0 && tx < xv1 && ty >= ylo && ty < yhi)) return;
     const bool want_part = !ADJ && C == 0 && L.partial != nullptr;
@@ -265,8 +270,6 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
       rr[e] = e < tt.ne ? rh[e * PLO + lo] : 0.0f;
       S = fmaf(rr[e], ar.s[e], S);
     }
-    float* const gp = dst == nullptr ? nullptr : dst + (long long)j * I.px[C] + i;
-    const long long gms = I.ms[C];
     const float invS = recip(S);
     const float dts = dt * invS;
     constexpr unsigned mask = Ord<N>::deg_mask(C);
@@ -290,8 +293,7 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
       const float q = (m == 0) ? q0 : 0.0f;
       const float num = fmaf(-Cl[l], u, q - acc[m]);   // (q - A u) - C_l u
       const float unew = fmaf(num, gl[l], u);
-      if (keep) own[m * PLO + lo] = unew;
-      if (gp != nullptr) gp[m * gms] = unew;
+      own[m * PLO + lo] = unew;
       if constexpr (C == 0 && !ADJ) {
         if (m == 0 && want_part) {
 #pragma unroll
@@ -303,15 +305,24 @@ __device__ __forceinline__ void par_point(const TLaunch<N>& L, const TTile& tt, 
   }
 }
 
-// One parity tile: one sub-step, or the two of a fused launch, on both targets.  With NT = TB
-// threads each thread updates one point of each target; with NT = 2 TB warps 0-3 update A and
-// warps 4-7 update B.  The threads store their points' new values themselves (no tensor store
-// reads the stage afterwards, so the stage can be refilled once the tile's threads are past its
-// last barrier).
-template <int N, int P, bool ADJ, int NT>
+// store target class C's box from `box` (thread 0): the adjoint state, or state slot `slot`
+template <int N, bool ADJ>
+__device__ __forceinline__ void par_store(const TLaunch<N>& L, int inst, int x0, int y0, int z, int C,
+                                          const unsigned char* box, int slot) {
+  const CUtensorMap* mp = L.maps + ((long long)inst * 8 + C) * TM_KINDS;
+  if (ADJ)
+    tma_store_4d(mp + TM_LAM_T, x0, y0, z, 0, box);
+  else
+    tma_store_5d(mp + TM_ST_T, x0, y0, z, 0, slot, box);
+}
+
+// One parity tile: one sub-step, or the two of a fused launch, on both targets.  With `next`,
+// thread 0 issues that tile's loads other than its target boxes (par_issue part 1) once the last
+// pass has finished with the stage, before this tile's stores.
+template <int N, int P, bool ADJ>
 __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                           double (&red)[TB / 32][MAXR]) {
-  static_assert(NT == TB || NT == 2 * TB, "one or two threads per tile position");
+                                           double (&red)[TB / 32][MAXR], const TTile* next,
+                                           unsigned long long* bar) {
   using LY = ParLayout<N>;
   constexpr int A = par_a(P), B = par_b(P), F1 = A ^ 4, F2 = A ^ 2;
   const TSolve& I = *reinterpret_cast<const TSolve*>(st + LY::SOL);
@@ -335,46 +346,21 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
     const ArgRow<N>& ar = rows[pass];
     const float dt = L.sub == 2 ? I.dE : half;
     // ghosts: A reads F1 along x and F2 along y, B reads F2 along x and F1 along y
-    par_ghosts<N, A, ADJ ? 1 : 0, NT>(inst, I, tt, extA, ownA, nb1, nb2, ADJ ? 0.0 : ar.bc);
-    par_ghosts<N, B, ADJ ? 1 : 0, NT>(inst, I, tt, extB, ownB, nb2, nb1, ADJ ? 0.0 : ar.bc);
+    par_ghosts<N, A, ADJ ? 1 : 0>(inst, I, tt, extA, ownA, nb1, nb2, ADJ ? 0.0 : ar.bc);
+    par_ghosts<N, B, ADJ ? 1 : 0>(inst, I, tt, extB, ownB, nb2, nb1, ADJ ? 0.0 : ar.bc);
+    if (second && threadIdx.x == 0) bulk_wait_read();   // the first pass's stores have read the boxes
     __syncthreads();
-    // where the new values go: the adjoint state, or the state slot this pass writes (if any)
-    float* gA = nullptr;
-    float* gB = nullptr;
-    if (ADJ) {
-      gA = I.lam + I.dev_off[A];
-      gB = I.lam + I.dev_off[B];
-    } else {
-      int slot = -1;
-      if (!fused) slot = sub_slots(tt, L.mode, L.j, L.sub, L.K).out;
-      else if (second || state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
-        slot = slot_index(tt.ns, tt.n_full, tt.n_ck, second ? L.j - 1 : L.j, L.K, segment);
-      if (slot >= 0) {
-        gA = I.slots + I.dev_off[A] + (long long)slot * I.slot_elems;
-        gB = I.slots + I.dev_off[B] + (long long)slot * I.slot_elems;
-      }
-    }
-    const bool keep = fused && !second;   // the second pass reads the first pass's values
     double part[MAXR];
 #pragma unroll
     for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
-    if constexpr (NT == TB) {
-      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x, gA, keep);
-      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x, gB, keep);
-    } else if (threadIdx.x < TB) {   // warp-uniform
-      par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part, threadIdx.x, gA, keep);
-    } else {
-      par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part, threadIdx.x - TB, gB, keep);
-    }
+    par_point<N, A, ADJ>(L, tt, extA, ownA, nb1, nb2, rhA, I, ar, dt, part);
+    par_point<N, B, ADJ>(L, tt, extB, ownB, nb2, nb1, rhB, I, ar, dt, part);
     if (!ADJ && A == 0 && L.partial != nullptr && tt.pslot >= 0) {   // block-uniform
-      // A's threads (the first TB) hold the partials: the same reduction as batch_tma_kernel's
-      if (threadIdx.x < TB) {   // warp-uniform
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        if (L.pr <= 1) warp_partials<1>(part, lane, w, L.pr, red);
-        else if (L.pr <= 2) warp_partials<2>(part, lane, w, L.pr, red);
-        else if (L.pr <= 4) warp_partials<4>(part, lane, w, L.pr, red);
-        else warp_partials<8>(part, lane, w, L.pr, red);
-      }
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      if (L.pr <= 1) warp_partials<1>(part, lane, w, L.pr, red);
+      else if (L.pr <= 2) warp_partials<2>(part, lane, w, L.pr, red);
+      else if (L.pr <= 4) warp_partials<4>(part, lane, w, L.pr, red);
+      else warp_partials<8>(part, lane, w, L.pr, red);
       __syncthreads();
       if (threadIdx.x < L.pr) {
         double v = 0.0;
@@ -383,73 +369,82 @@ __device__ __forceinline__ void par_tile_p(const TLaunch<N>& L, const TTile& tt,
         L.partial[(long long)tt.pslot * L.pr + threadIdx.x] = v;
       }
     }
-    // the next pass's ghosts read the target boxes and rewrite the neighbour boxes; after the
-    // last pass the stage may be refilled
-    __syncthreads();
+    __syncthreads();   // both target boxes hold the new values
+    if (threadIdx.x == 0) {
+      int slot = -1;
+      if (ADJ) slot = 0;
+      else if (!fused) slot = sub_slots(tt, L.mode, L.j, L.sub, L.K).out;
+      else if (second || state_kept(tt.ns, tt.n_full, L.j, L.K, segment))
+        slot = slot_index(tt.ns, tt.n_full, tt.n_ck, second ? L.j - 1 : L.j, L.K, segment);
+      // the tile record is overwritten by the next tile's issue
+      const int inst = tt.inst, x0 = tt.x0, y0 = tt.y0, z = tt.z;
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (next != nullptr && pass == p1 - 1) par_issue<N, ADJ, 1>(L, *next, st, bar);
+      if (slot >= 0) {
+        if (Ord<N>::n(A) > 0) par_store<N, ADJ>(L, inst, x0, y0, z, A, st + LY::OWNA, slot);
+        if (Ord<N>::n(B) > 0) par_store<N, ADJ>(L, inst, x0, y0, z, B, st + LY::OWNB, slot);
+        bulk_commit();
+      }
+    }
   }
   (void)F1; (void)F2;
 }
 
-template <int N, bool ADJ, int NT>
+template <int N, bool ADJ>
 __device__ __forceinline__ void par_tile(const TLaunch<N>& L, const TTile& tt, unsigned char* st,
-                                         double (&red)[TB / 32][MAXR]) {
-  if (tt.cls == 0) par_tile_p<N, 0, ADJ, NT>(L, tt, st, red);
-  else par_tile_p<N, 1, ADJ, NT>(L, tt, st, red);
+                                         double (&red)[TB / 32][MAXR], const TTile* next = nullptr,
+                                         unsigned long long* bar = nullptr) {
+  if (tt.cls == 0) par_tile_p<N, 0, ADJ>(L, tt, st, red, next, bar);
+  else par_tile_p<N, 1, ADJ>(L, tt, st, red, next, bar);
 }
 
-// Persistent CTAs over a launch's parity tiles, two stages each: the next tile's loads are issued
-// into the other stage as soon as the current tile's have landed, so that they land while the
-// current tile is updated.  2 TB threads: one per target point of a tile.  The dynamic shared
-// memory holds the two stages (its size / 2 each, a multiple of 128 bytes).
-constexpr int PAR_NT = 2 * TB;
-
+// Persistent CTAs over a launch's parity tiles (batch_tma_kernel's structure; 2D groups).
 template <int N, bool ADJ>
-__global__ void __launch_bounds__(PAR_NT, PN_PAR_MINB) batch_par_kernel(const __grid_constant__ TLaunch<N> L) {
+__global__ void __launch_bounds__(TB, PN_PAR_MINB) batch_par_kernel(const __grid_constant__ TLaunch<N> L) {
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) unsigned long long full[2];
+  __shared__ __align__(8) unsigned long long full[1];
   __shared__ double red[TB / 32][MAXR];
-  unsigned dyn;
-  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
-  const unsigned SB = dyn / 2;
-  if ((smem_u32(smem) & 127u) != 0u || (SB & 127u) != 0u) {
+  if ((smem_u32(smem) & 127u) != 0u) {
     if (threadIdx.x == 0) atomicExch(L.status, (int)PN_ERR_INVALID);
     return;
   }
   if (threadIdx.x == 0) {
     mbar_init(&full[0], 1);
-    mbar_init(&full[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   const int G = gridDim.x;
-  if (threadIdx.x == 0 && (int)blockIdx.x < L.n_tiles) par_issue<N, ADJ>(L, L.tiles[blockIdx.x], smem, &full[0]);
+  unsigned phase = 0;
   for (int k = 0; (int)blockIdx.x + k * G < L.n_tiles; ++k) {
-    // tile k lives in stage k & 1, use k >> 1 of its barrier; no other loads are in flight
-    const int s = k & 1;
-    const unsigned phase = (unsigned)(k >> 1) & 1u;
-    unsigned char* st = smem + s * SB;
-    bool ok = mbar_wait_bounded(&full[s], phase);
+    const int t = blockIdx.x + k * G;
+    if (threadIdx.x == 0) {
+      if (k == 0) {
+        par_issue<N, ADJ, 0>(L, L.tiles[t], smem, &full[0]);
+      } else {   // the rest of the tile's loads went out before the previous tile's stores
+        bulk_wait_read();   // those stores have read the target boxes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        par_issue<N, ADJ, 2>(L, L.tiles[t], smem, &full[0]);
+      }
+    }
+    bool ok = mbar_wait_bounded(&full[0], phase);
     if (L.test_expire != nullptr && k == 0 && threadIdx.x == 0 && ok && *(volatile int*)L.test_expire > 0 &&
         atomicSub(L.test_expire, 1) > 0)
       ok = false;   // test hook: report a completed wait as run out (see batch_tma_kernel)
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) {
         atomicExch(L.status, (int)PN_ERR_TIMEOUT);
-        mbar_wait_bounded(&full[s], phase);   // let the copies in flight land
+        mbar_wait_bounded(&full[0], phase);   // let the copies in flight land
         bulk_wait_all();
       }
       __syncthreads();
       return;
     }
-    // the other stage's last readers (tile k - 1) are past its final barrier
-    const int tn = (int)blockIdx.x + (k + 1) * G;
-    if (threadIdx.x == 0 && tn < L.n_tiles) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      par_issue<N, ADJ>(L, L.tiles[tn], smem + (s ^ 1) * SB, &full[s ^ 1]);
-    }
-    const TTile& tt = *reinterpret_cast<const TTile*>(st + ParLayout<N>::TIL);
-    par_tile<N, ADJ, PAR_NT>(L, tt, st, red);
+    phase ^= 1u;
+    const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
+    const TTile* next = t + G < L.n_tiles ? L.tiles + t + G : nullptr;
+    par_tile<N, ADJ>(L, tt, smem, red, next, &full[0]);
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 }  // namespace pn

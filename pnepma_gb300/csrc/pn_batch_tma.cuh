@@ -1283,8 +1283,8 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
     } else if (PAR_OK && S.par) {
       if constexpr (PAR_OK) {
         const TTile& tt = *reinterpret_cast<const TTile*>(smem + ParLayout<N>::TIL);
-        if (kind == TS_ADJ) par_tile<N, true, NTS>(L, tt, smem, red);
-        else par_tile<N, false, NTS>(L, tt, smem, red);
+        if (kind == TS_ADJ) par_tile<N, true>(L, tt, smem, red);
+        else par_tile<N, false>(L, tt, smem, red);
       }
     } else {
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + LY::TIL);
@@ -1297,7 +1297,7 @@ __global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_sweep_kernel(const __g
       const int til = kind == TS_INT ? LI::TIL : (PAR_OK && S.par) ? ParLayout<N>::TIL : LY::TIL;
       const TTile& tt = *reinterpret_cast<const TTile*>(smem + til);
       pend = (long long)k * S.n_solves + tt.inst;
-      pend_generic = kind == TS_INT || (PAR_OK && S.par);   // parity tiles store from their threads
+      pend_generic = kind == TS_INT;
     }
     __syncthreads();   // the stage's tile record is not read again before the next issue
   }
