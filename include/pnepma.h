@@ -261,10 +261,12 @@ enum pn_batch_flags {
      slower on the 2D P11 workload (each tile waits for its stores to land before it releases
      its counter), so off by default and one of the autotuner's choices */
   PN_BATCH_SWEEP_LAUNCH = 16,
-  /* FP32 2D groups: one TMA tile per target class (a 32 x 4 box, a 40 x 4 x-neighbour box and a
-     32 x 5 y-neighbour box) instead of parity tiles (both targets of a parity at one 32 x 4
-     position, one 36 x 5 box per neighbour class).  Identical results */
-  PN_BATCH_CLASS_TILES = 32,
+  /* FP32 2D groups: parity tiles (both target classes of a parity at one 32 x 4 position, one
+     36 x 5 box per neighbour class: a third less shared memory per target point) instead of one
+     TMA tile per target class (a 32 x 4 box, a 40 x 4 x-neighbour box and a 32 x 5 y-neighbour
+     box).  Identical results; measured as fast as the class tiles on the 2D P11 workload, so off
+     by default and one of the autotuner's choices */
+  PN_BATCH_PARITY_TILES = 32,
   /* bits 8..11: resident CTAs per SM of the persistent TMA tile kernels, 1..15 (0: as many as the
      shared memory and registers allow); fewer CTAs each walk more tiles.  One of the autotuner's
      choices (tiles per CTA) */

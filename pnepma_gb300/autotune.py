@@ -11,7 +11,9 @@ The configurations are the batch engine's own runtime choices:
   persistent cooperative launch (``PN_BATCH_SWEEP_LAUNCH``);
 * the tape schedule: the automatic choice within the memory budget, or a fixed checkpoint stride;
 * the persistent grid of the TMA tile kernels: resident CTAs per SM (``PN_BATCH_CTAS_PER_SM_SHIFT``
-  bits of the flags), i.e. how many tiles each CTA walks.
+  bits of the flags), i.e. how many tiles each CTA walks;
+* the 2D tile shape: one tile per target class, the default, or parity tiles that update both
+  target classes of a parity at one position (``PN_BATCH_PARITY_TILES``).
 
 The tile box (32 x 4 points) and the points per thread are compile-time constants of the TMA
 kernels (``PN_TMA_TY``, ``PN_TMA_PPT``) and are not among the runtime choices.  A configuration
@@ -30,6 +32,7 @@ import numpy as np
 PN_BATCH_GENERIC_KERNELS = 1
 PN_BATCH_DIRECT_LAUNCH = 2
 PN_BATCH_SWEEP_LAUNCH = 16
+PN_BATCH_PARITY_TILES = 32
 PN_BATCH_CTAS_PER_SM_SHIFT = 8
 PN_FP32 = 1
 
@@ -45,6 +48,8 @@ class Config:
 
     def label(self) -> str:
         kern = "generic" if self.flags & PN_BATCH_GENERIC_KERNELS else "tma"
+        if self.flags & PN_BATCH_PARITY_TILES:
+            kern += "-parity"
         launch = ("direct" if self.flags & PN_BATCH_DIRECT_LAUNCH else
                   "sweep" if self.flags & PN_BATCH_SWEEP_LAUNCH else "graphs")
         tape = f"K={self.checkpoint_stride}" if self.checkpoint_stride else "K=auto"
@@ -61,6 +66,7 @@ DEFAULT_CANDIDATES = (
     Config(PN_BATCH_SWEEP_LAUNCH, 0),
     Config(3 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
     Config(4 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
+    Config(PN_BATCH_PARITY_TILES, 0),
 )
 
 
@@ -79,6 +85,8 @@ def batch_key(descs) -> str:
 def applies(cfg: Config, descs) -> bool:
     """False when the configuration runs the batch exactly as the default does."""
     tiles = any(d.precision == PN_FP32 and sum(d.n_points[k] > 1 for k in range(3)) >= 2 for d in descs)
+    if cfg.flags & PN_BATCH_PARITY_TILES:
+        return any(d.precision == PN_FP32 and sum(d.n_points[k] > 1 for k in range(3)) == 2 for d in descs)
     if cfg.flags & (PN_BATCH_GENERIC_KERNELS | PN_BATCH_SWEEP_LAUNCH) or cfg.ctas_per_sm:
         return tiles
     return True

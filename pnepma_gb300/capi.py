@@ -31,7 +31,7 @@ PN_BATCH_GENERIC_KERNELS = 1
 PN_BATCH_DIRECT_LAUNCH = 2
 PN_BATCH_TEST_EXPIRE_WAIT = 4
 PN_BATCH_SWEEP_LAUNCH = 16
-PN_BATCH_CLASS_TILES = 32
+PN_BATCH_PARITY_TILES = 32
 PN_BATCH_CTAS_PER_SM_SHIFT = 8
 
 

@@ -629,7 +629,7 @@ class BatchGroup : public BatchGroupBase {
   int* dstatus = nullptr;          // [0] status of the latest calls, [1] test expiries left
   bool test_expire = false;         // PN_BATCH_TEST_EXPIRE_WAIT
   int cta_cap = 0;                  // resident CTAs per SM of the tile kernels (0: occupancy)
-  bool class_tiles = false;         // PN_BATCH_CLASS_TILES
+  bool parity_tiles = false;        // PN_BATCH_PARITY_TILES
   // one persistent launch per sweep (TMA groups replayed as graphs, see batch_sweep_kernel): the
   // steps of each sweep are planned once before the graphs are captured
   bool sweep = false;
@@ -902,7 +902,7 @@ class BatchGroup : public BatchGroupBase {
     if constexpr (std::is_same<T, float>::value && (DIMS == 3 || DIMS == 7)) {
       test_expire = (flags & PN_BATCH_TEST_EXPIRE_WAIT) != 0;
       cta_cap = (flags >> PN_BATCH_CTAS_PER_SM_SHIFT) & 15;
-      class_tiles = (flags & PN_BATCH_CLASS_TILES) != 0;
+      parity_tiles = (flags & PN_BATCH_PARITY_TILES) != 0;
       if (!(flags & PN_BATCH_GENERIC_KERNELS))
         if ((rc = build_tma())) return rc;
     } else {
@@ -975,7 +975,7 @@ class BatchGroup : public BatchGroupBase {
         int ne_max = 1;
         for (int q = 0; q < n; ++q) ne_max = std::max(ne_max, hinst[q].ne);
         par_stage = (ParLayout<N>::smem(ne_max) + 127) / 128 * 128;
-        if (par_stage + 2048 <= smem_optin && !class_tiles) {
+        if (par_stage + 2048 <= smem_optin && parity_tiles) {
           PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        par_stage));
           PN_CUDA(cudaFuncSetAttribute(batch_par_kernel<N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -32,6 +32,16 @@ def test_generic_kernels_only_matter_for_fp32_2d_and_3d():
     assert autotune.applies(autotune.Config(autotune.PN_BATCH_DIRECT_LAUNCH, 0), [d2])
 
 
+def test_parity_tiles_only_matter_for_fp32_2d():
+    p = autotune.Config(autotune.PN_BATCH_PARITY_TILES, 0)
+    d2, k2 = _descs(dims=2, N=3, shape=(8, 7), precision=PN_FP32)
+    d3, k3 = _descs(dims=3, N=3, shape=(8, 7, 5), precision=PN_FP32)
+    d64, k64 = _descs(dims=2, N=3, shape=(8, 7))
+    assert autotune.applies(p, [d2]) and autotune.applies(p, [d3, d2])
+    assert not autotune.applies(p, [d3]) and not autotune.applies(p, [d64])
+    assert p.label() == "tma-parity/graphs/K=auto"
+
+
 def test_tune_keeps_the_fastest_and_remembers_it(tmp_path):
     d, k = _descs(dims=2, N=3, shape=(8, 7), precision=PN_FP32)
     times = {c: 1.0 + i for i, c in enumerate(autotune.DEFAULT_CANDIDATES)}

@@ -229,15 +229,15 @@ def test_sweep_launch_matches_step_launches(gpu_lib):
 
 
 def test_parity_tiles_match_the_class_tiles(gpu_lib):
-    """2D: parity tiles (both targets of a parity at one 32 x 4 position, the default) against one
-    tile per target class (PN_BATCH_CLASS_TILES).  Every point runs the same arithmetic, and the
+    """2D: parity tiles (both targets of a parity at one 32 x 4 position, PN_BATCH_PARITY_TILES)
+    against one tile per target class (the default).  Every point runs the same arithmetic, and the
     intensity partials are reduced over the same 32 x 4 eee positions in the same order, so
     intensities, states and gradients agree bit for bit; also with the sweep launch."""
     torch = pytest.importorskip("torch")
     solves = tma_solves()
     for K, extra in ((1, 0), (3, 0), (3, capi.PN_BATCH_SWEEP_LAUNCH)):
-        ref = run_batch(torch, solves, K=K, flags=capi.PN_BATCH_CLASS_TILES | extra)
-        got = run_batch(torch, solves, K=K, ibar=ref[1], flags=extra)
+        ref = run_batch(torch, solves, K=K, flags=extra)
+        got = run_batch(torch, solves, K=K, ibar=ref[1], flags=capi.PN_BATCH_PARITY_TILES | extra)
         assert got[5].tma_groups == ref[5].tma_groups == ref[5].n_groups
         for a, b in zip(got[:5], ref[:5]):
             for x, y in zip(a, b):
