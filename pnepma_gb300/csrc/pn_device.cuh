@@ -16,6 +16,10 @@
 // computes it, with no other thread reading or writing it during the launch.  Ghosts along two or
 // more axes are read by no stencil and are not maintained.
 //
+// The plain path (one solve per launch) runs these sub-steps and the density integral with two
+// threads per target cell (substep_split_kernel, integrate_split_kernel), each updating the
+// moments of half of the cell's degrees, with the same arithmetic per moment.
+//
 // The adjoint density kernel (integrate_adjoint_densities!, pn_solver/pn_intensities.jl:129-164)
 // evaluates du of a tape state for every class (plain right-hand side, no exponential factor) and
 // accumulates rho_bar[e] += sum_m lambda_m (s_e du_m + c_{e,l(m)} u_m) dvol dE w, plus the eee
@@ -206,6 +210,7 @@ __device__ __forceinline__ float phi1_ref(float c) {
 
 template <class T>
 __device__ __forceinline__ T recip(T x) { return T(1) / x; }
+
 
 // minimum resident blocks per SM the plain sub-step kernel is compiled for: 5 keeps the FP64 P11
 // instances within 96 registers (5 x 4 warps per SM to feed the FP64 pipe, instead of 4 x 4)
@@ -727,6 +732,230 @@ __global__ void __launch_bounds__(PBLOCK, PN_PLAIN_MINB * (BLOCK / PBLOCK)) subs
 }
 
 // --------------------------------------------------------------------------------------------
+// plain sub-step with two threads per cell
+// --------------------------------------------------------------------------------------------
+// One solve's sub-step launch holds about 14 warps per SM (one thread per target cell), and they
+// leave the FP64 pipe idle while they wait for their neighbour values.  This form gives every
+// target cell two threads in two different warps: half h updates the moments [M0, M1) of its cell
+// (h = 0 the lower degrees, h = 1 the rest, split at the degree boundary nearest to half the
+// moments), forms the factors of those degrees only, and loads only the neighbour moments that its
+// rows couple to.  Each row receives the same products in the same order as in substep_cell, so
+// the results are bit-identical to substep_kernel's.
+
+// first moment of the upper half of class C (n when the class has a single degree: the lower
+// half then does all of it, so moment 0, with the intensity partials and the adjoint source, is
+// always in the lower half)
+template <int N, int C>
+__host__ __device__ constexpr int split_moment() {
+  const int n = Ord<N>::n(C);
+  int best = 0, bd = 1 << 30;
+  for (int m = 1; m < n; ++m) {
+    if (degree_of<N, C>(m) == degree_of<N, C>(m - 1)) continue;
+    const int d = 2 * m > n ? 2 * m - n : n - 2 * m;
+    if (d < bd) {
+      bd = d;
+      best = m;
+    }
+  }
+  return best > 0 ? best : n;
+}
+
+// degrees of the moments [M0, M1) of class C
+template <int N, int C, int M0, int M1>
+__host__ __device__ constexpr unsigned range_deg_mask() {
+  unsigned msk = 0u;
+  for (int m = M0; m < M1; ++m) msk |= 1u << degree_of<N, C>(m);
+  return msk;
+}
+
+// Accumulators of rows [M0, M1); the other rows go to a sink that nothing reads, so the compiler
+// drops their products, and the differences and loads that only they use.
+template <class T, int M0, int M1>
+struct RowAcc {
+  T v[M1 > M0 ? M1 - M0 : 1];
+  T sink;
+  __device__ __forceinline__ T& operator[](int m) { return (m >= M0 && m < M1) ? v[m - M0] : sink; }
+};
+
+// stencil_axis (table coefficients, runtime active axes) over a row range
+template <class T, int N, int C, int D, bool NEG, class Acc>
+__device__ __forceinline__ void stencil_axis_rows(Acc& acc, T* const* rd, const Geom* g, int i, int j, int k,
+                                                  const T* tab) {
+  constexpr int F = C ^ (4 >> D);
+  constexpr int nf = Ord<N>::n(F);
+  if constexpr (nf == 0 || Ord<N>::n(C) == 0) {
+    return;
+  } else {
+    const Geom& gf = g[F];
+    int r3[3] = {i, j, k};
+    int l3[3] = {i, j, k};
+    if ((C >> (2 - D)) & 1) l3[D] -= 1;
+    else r3[D] += 1;
+    const T* fr = rd[F] + lin(gf, r3[0], r3[1], r3[2]);
+    const T* fl = rd[F] + lin(gf, l3[0], l3[1], l3[2]);
+    const long long ms = gf.ms;
+    auto diff = [&](int q) -> T {
+      const T x = fr[q * ms];
+      const T y = fl[q * ms];
+      return NEG ? (y - x) : (x - y);
+    };
+    constexpr int off = Ord<N>::off(C, D);
+    auto coef = [&](int kk, double lit) -> T {
+      (void)lit;
+      return tab[off + kk];
+    };
+    Adv<N, C, D>::template apply<T>(acc, diff, coef);
+  }
+}
+
+template <class T, int N, int C, bool ADJ, int H>
+__device__ __forceinline__ void substep_cell_half(const SubArgs<T, N>& a, int i, int j, int k, double* part) {
+  constexpr int n = Ord<N>::n(C);
+  constexpr int MS = split_moment<N, C>();
+  constexpr int M0 = H == 0 ? 0 : MS;
+  constexpr int M1 = H == 0 ? MS : n;
+  if constexpr (n == 0 || M1 <= M0) {
+    (void)a; (void)i; (void)j; (void)k; (void)part;
+  } else {
+    const Geom& gt = a.g[C];
+    const long long p = lin(gt, i, j, k);
+    RowAcc<T, M0, M1> acc;
+#pragma unroll
+    for (int m = 0; m < M1 - M0; ++m) acc.v[m] = T(0);
+    acc.sink = T(0);
+    if (a.act[0]) stencil_axis_rows<T, N, C, 0, ADJ>(acc, a.rd, a.g, i, j, k, a.tab);
+    if (a.act[1]) stencil_axis_rows<T, N, C, 1, ADJ>(acc, a.rd, a.g, i, j, k, a.tab);
+    if (a.act[2]) stencil_axis_rows<T, N, C, 2, ADJ>(acc, a.rd, a.g, i, j, k, a.tab);
+
+    constexpr unsigned mask = range_deg_mask<N, C, M0, M1>();
+    T Cl[N + 1];
+    T gl[N + 1];
+    if (a.cache_mode == 2) {
+      const T* cp = a.cache[C] + p;
+#pragma unroll
+      for (int l = 0; l <= N; ++l) {
+        Cl[l] = ((mask >> l) & 1u) ? cp[l * gt.ms] : T(0);
+        gl[l] = ((mask >> l) & 1u) ? cp[(1 + N + l) * gt.ms] : T(0);
+      }
+    } else {
+      const T* rho = a.rho[C] + p;
+      T rr[MAXE];
+      T S = T(0);
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
+        S = fma(rr[e], a.s[e], S);
+      }
+      const T invS = recip(S);
+      const T dts = a.dt * invS;
+      cl_sums<T, N, mask>(rr, a.c, a.ne, Cl);
+#pragma unroll
+      for (int l = 0; l <= N; ++l) gl[l] = ((mask >> l) & 1u) ? dts * phi1(-(Cl[l] * dts)) : T(0);
+      if (a.cache_mode == 1) {
+        T* cp = a.cache[C] + p;
+#pragma unroll
+        for (int l = 0; l <= N; ++l)
+          if ((mask >> l) & 1u) {
+            cp[l * gt.ms] = Cl[l];
+            cp[(1 + N + l) * gt.ms] = gl[l];
+          }
+      }
+    }
+    const T* uo = a.rd[C] + p;
+    T* un = a.wr[C] + p;
+    T q0 = T(0);
+    if constexpr (ADJ && C == 0 && M0 == 0) {
+      if (a.adjoint_source) {
+        const long long ce = eee_cell(gt, i, j, k);
+        double q = 0.0;
+        for (int r = 0; r < a.nr; ++r)
+          q = q - a.sig_src[r] * a.acs[ce * a.nr + r] * a.noa[ce * a.ne + a.xel[r]] * a.ibar[r];
+        q0 = T(q);
+      }
+    }
+#pragma unroll
+    for (int m = M0; m < M1; ++m) {
+      const int l = degree_of<N, C>(m);
+      const T u = uo[m * gt.ms];
+      const T q = (m == 0) ? q0 : T(0);
+      const T num = fma(-Cl[l], u, q - acc.v[m - M0]);   // (q - A u) - C_l u
+      const T unew = fma(num, gl[l], u);
+      un[m * gt.ms] = unew;
+      if constexpr (C == 0 && !ADJ && M0 == 0) {
+        if (m == 0 && part != nullptr) {
+          const long long ce = eee_cell(gt, i, j, k);
+#pragma unroll
+          for (int r = 0; r < MAXR; ++r)
+            if (r < a.nr) part[r] += a.wint[ce * a.nr + r] * double(unew);
+        }
+      }
+    }
+  }
+}
+
+template <class T, int N, bool ADJ, int H>
+__device__ __forceinline__ void substep_half_of(const SubArgs<T, N>& a, int cls, int i, int j, int k, double* part) {
+  switch (cls) {
+    case 0: substep_cell_half<T, N, 0, ADJ, H>(a, i, j, k, part); break;
+    case 1: substep_cell_half<T, N, 1, ADJ, H>(a, i, j, k, part); break;
+    case 2: substep_cell_half<T, N, 2, ADJ, H>(a, i, j, k, part); break;
+    case 3: substep_cell_half<T, N, 3, ADJ, H>(a, i, j, k, part); break;
+    case 4: substep_cell_half<T, N, 4, ADJ, H>(a, i, j, k, part); break;
+    case 5: substep_cell_half<T, N, 5, ADJ, H>(a, i, j, k, part); break;
+    case 6: substep_cell_half<T, N, 6, ADJ, H>(a, i, j, k, part); break;
+    default: substep_cell_half<T, N, 7, ADJ, H>(a, i, j, k, part); break;
+  }
+}
+
+// resident blocks of 2 x PBLOCK threads per SM the split kernel is compiled for (its register cap)
+#ifndef PN_SPLIT_MINB
+#define PN_SPLIT_MINB 7
+#endif
+
+// Same work segments and partial-sum slots as substep_kernel (PBLOCK cells per block); threads
+// [0, PBLOCK) are the lower halves of the block's cells, [PBLOCK, 2 PBLOCK) the upper halves.  The
+// face ghosts must have been written by ghost_kernel before the launch.
+template <class T, int N, bool ADJ>
+__global__ void __launch_bounds__(2 * PBLOCK, PN_SPLIT_MINB) substep_split_kernel(const __grid_constant__ SubArgs<T, N> a) {
+  const int h = threadIdx.x >= PBLOCK ? 1 : 0;   // warp-uniform
+  const int tid = threadIdx.x - h * PBLOCK;
+  int s, i, j, k;
+  const bool ok = locate<PBLOCK>(a.seg, a.nseg, blockIdx.x, tid, s, i, j, k);
+  const int cls = a.seg[s].cls;
+  double part[MAXR];
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) part[r] = 0.0;
+  double* pp = (a.partial != nullptr) ? part : nullptr;
+  if (ok) {
+    if (h == 0) substep_half_of<T, N, ADJ, 0>(a, cls, i, j, k, pp);
+    else substep_half_of<T, N, ADJ, 1>(a, cls, i, j, k, pp);
+  }
+  if (a.partial != nullptr) {
+    // moment 0 is in the lower half: the lower warps' sums, in substep_kernel's order
+    __shared__ double red[PBLOCK / 32][MAXR];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (h == 0) {
+#pragma unroll
+      for (int r = 0; r < MAXR; ++r) {
+        if (r < a.nr) {
+          double v = part[r];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+          if (lane == 0) red[w][r] = v;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < a.nr) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < PBLOCK / 32; ++q) v += red[q][threadIdx.x];
+      a.partial[(long long)blockIdx.x * a.nr + threadIdx.x] = v;
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------------
 // adjoint density kernel
 // --------------------------------------------------------------------------------------------
 template <class T, int N, int C, bool LIT, class A, int DIMS = 0>
@@ -818,22 +1047,146 @@ __device__ __forceinline__ void integrate_cell(const A& a, int i, int j, int k, 
   }
 }
 
+// The density integral with two threads per cell (the plain path's form, as
+// substep_split_kernel): half h forms du for the moments [M0, M1) of its cell and the sums
+// R_l of its degrees.  P = sum_m lambda_m du_m is one FMA chain in moment order: the lower half
+// runs it over its moments and hands the partial chain, with its R_l, to the upper half through
+// shared memory; the upper half continues the chain over its moments and writes rho_bar.  Every
+// sum is formed in integrate_cell's order, so rho_bar is bit-identical to a one-thread-per-cell
+// evaluation of integrate_cell.
 template <class T, int N>
-__global__ void __launch_bounds__(PBLOCK) integrate_kernel(const __grid_constant__ IntArgs<T, N> a) {
-  int s, i, j, k;
-  if (!locate<PBLOCK>(a.seg, a.nseg, blockIdx.x, threadIdx.x, s, i, j, k)) return;
-  const int cls = a.seg[s].cls;
-  const bool face = a.seg[s].kind == 1;
-  switch (cls) {
-    case 0: integrate_cell<T, N, 0, false>(a, i, j, k, face); break;
-    case 1: integrate_cell<T, N, 1, false>(a, i, j, k, face); break;
-    case 2: integrate_cell<T, N, 2, false>(a, i, j, k, face); break;
-    case 3: integrate_cell<T, N, 3, false>(a, i, j, k, face); break;
-    case 4: integrate_cell<T, N, 4, false>(a, i, j, k, face); break;
-    case 5: integrate_cell<T, N, 5, false>(a, i, j, k, face); break;
-    case 6: integrate_cell<T, N, 6, false>(a, i, j, k, face); break;
-    default: integrate_cell<T, N, 7, false>(a, i, j, k, face); break;
+struct IntXchg {
+  T P[PBLOCK];
+  T R[N + 1][PBLOCK];
+};
+
+template <class T, int N, int C, int H>
+__device__ __forceinline__ void integrate_cell_half(const IntArgs<T, N>& a, bool ok, int i, int j, int k, int tid,
+                                                    IntXchg<T, N>& x) {
+  constexpr int n = Ord<N>::n(C);
+  constexpr int MS = split_moment<N, C>();
+  constexpr int M0 = H == 0 ? 0 : MS;
+  constexpr int M1 = H == 0 ? MS : n;
+  constexpr bool alone = MS >= n;   // one degree: the lower half does all of it
+  if constexpr (n == 0 || M1 <= M0) {
+    __syncthreads();
+  } else {
+    const Geom& gt = a.g[C];
+    const long long p = ok ? lin(gt, i, j, k) : 0;
+    constexpr unsigned mask = range_deg_mask<N, C, M0, M1>();
+    constexpr unsigned cmask = Ord<N>::deg_mask(C);
+    T P = T(0);
+    T R[N + 1];
+#pragma unroll
+    for (int l = 0; l <= N; ++l) R[l] = T(0);
+    T tm[M1 - M0], lmv[M1 - M0];
+    T invS = T(1);
+    if (ok) {
+      RowAcc<T, M0, M1> acc;
+#pragma unroll
+      for (int m = 0; m < M1 - M0; ++m) acc.v[m] = T(0);
+      acc.sink = T(0);
+      if (a.act[0]) stencil_axis_rows<T, N, C, 0, false>(acc, a.u, a.g, i, j, k, a.tab);
+      if (a.act[1]) stencil_axis_rows<T, N, C, 1, false>(acc, a.u, a.g, i, j, k, a.tab);
+      if (a.act[2]) stencil_axis_rows<T, N, C, 2, false>(acc, a.u, a.g, i, j, k, a.tab);
+      const T* rho = a.rho[C] + p;
+      T rr[MAXE];
+      T S = T(0);
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        rr[e] = e < a.ne ? rho[e * gt.ms] : T(0);
+        S = fma(rr[e], a.s[e], S);
+      }
+      invS = recip(S);
+      T Cl[N + 1];
+      cl_sums<T, N, mask>(rr, a.c, a.ne, Cl);
+      const T* uu = a.u[C] + p;
+      const T* la = a.lam[C] + p;
+#pragma unroll
+      for (int m = M0; m < M1; ++m) {
+        const int l = degree_of<N, C>(m);
+        const T u = uu[m * gt.ms];
+        const T lm = la[m * gt.ms];
+        tm[m - M0] = fma(-Cl[l], u, -acc.v[m - M0]);
+        lmv[m - M0] = lm;
+        R[l] = fma(lm, u, R[l]);
+      }
+      if constexpr (H == 0) {
+#pragma unroll
+        for (int m = 0; m < M1; ++m) P = fma(lmv[m], tm[m], P);
+        if constexpr (!alone) {
+          x.P[tid] = P;
+#pragma unroll
+          for (int l = 0; l <= N; ++l)
+            if ((mask >> l) & 1u) x.R[l][tid] = R[l];
+        }
+      }
+      if constexpr (C == 0 && H == 0) {
+        const long long ce = eee_cell(gt, i, j, k);
+        const double u0 = double(uu[0]);
+        for (int r = 0; r < a.nr; ++r) {
+          const double cr = a.coef[r] * a.ibar[r];
+          const int el = a.xel[r];
+          a.acs_bar[ce * a.nr + r] += a.noa[ce * a.ne + el] * u0 * cr;
+          a.noa_bar[ce * a.ne + el] += a.acs[ce * a.nr + r] * u0 * cr;
+        }
+      }
+    }
+    __syncthreads();
+    // the half that finishes: the upper one, or the lower one of a single-degree class
+    if (ok && (H == 1 || alone)) {
+      if constexpr (H == 1) {
+        P = x.P[tid];
+#pragma unroll
+        for (int m = M0; m < M1; ++m) P = fma(lmv[m - M0], tm[m - M0], P);
+#pragma unroll
+        for (int l = 0; l <= N; ++l)
+          if (((cmask & ~mask) >> l) & 1u) R[l] = x.R[l][tid];
+      }
+      P *= invS;
+      double* rb = a.rbar[C] + p;
+#pragma unroll
+      for (int e = 0; e < MAXE; ++e) {
+        if (e < a.ne) {
+          T v = a.s[e] * P;
+#pragma unroll
+          for (int l = 0; l <= N; ++l)
+            if ((cmask >> l) & 1u) v = fma(T(a.c[e][l]), R[l], v);
+          rb[e * gt.ms] = fma(double(v), a.wfac, rb[e * gt.ms]);
+        }
+      }
+    }
   }
+}
+
+template <class T, int N, int H>
+__device__ __forceinline__ void integrate_half_of(const IntArgs<T, N>& a, int cls, bool ok, int i, int j, int k,
+                                                  int tid, IntXchg<T, N>& x) {
+  switch (cls) {
+    case 0: integrate_cell_half<T, N, 0, H>(a, ok, i, j, k, tid, x); break;
+    case 1: integrate_cell_half<T, N, 1, H>(a, ok, i, j, k, tid, x); break;
+    case 2: integrate_cell_half<T, N, 2, H>(a, ok, i, j, k, tid, x); break;
+    case 3: integrate_cell_half<T, N, 3, H>(a, ok, i, j, k, tid, x); break;
+    case 4: integrate_cell_half<T, N, 4, H>(a, ok, i, j, k, tid, x); break;
+    case 5: integrate_cell_half<T, N, 5, H>(a, ok, i, j, k, tid, x); break;
+    case 6: integrate_cell_half<T, N, 6, H>(a, ok, i, j, k, tid, x); break;
+    default: integrate_cell_half<T, N, 7, H>(a, ok, i, j, k, tid, x); break;
+  }
+}
+
+// PBLOCK cells per block, one class per block (the plain path's segments); the face
+// ghosts must have been written by ghost_kernel before the launch.  Every thread reaches the one
+// __syncthreads of its class's path.
+template <class T, int N>
+__global__ void __launch_bounds__(2 * PBLOCK, PN_SPLIT_MINB) integrate_split_kernel(const __grid_constant__ IntArgs<T, N> a) {
+  __shared__ IntXchg<T, N> x;
+  const int h = threadIdx.x >= PBLOCK ? 1 : 0;   // warp-uniform
+  const int tid = threadIdx.x - h * PBLOCK;
+  int s, i, j, k;
+  const bool ok = locate<PBLOCK>(a.seg, a.nseg, blockIdx.x, tid, s, i, j, k);
+  const int cls = a.seg[s].cls;   // block-uniform
+  if (h == 0) integrate_half_of<T, N, 0>(a, cls, ok, i, j, k, tid, x);
+  else integrate_half_of<T, N, 1>(a, cls, ok, i, j, k, tid, x);
 }
 
 }  // namespace pn

@@ -24,8 +24,6 @@
 
 namespace pn {
 
-
-
 // final intensities in step order: I_r = sum_i (((dE dvol) sigma_{i,r}) integral_{i,r}) w_i
 static __global__ void final_intensity_kernel(const double* __restrict__ integral, const double* __restrict__ sigma,
                                        const double* __restrict__ weight, double* __restrict__ I, int ns1,
@@ -642,10 +640,11 @@ class Solver : public SolverBase {
     if ((rc = launch_ghosts(a.rd, adj, bc, gl_off[par], gl_n[par], stream))) return rc;
     a.pre_ghosts = 1;
     const int nb = nblk_par[par];
+    // two threads per cell (substep_split_kernel): the same segments, 2 x PBLOCK threads a block
     if (adj)
-      substep_kernel<T, N, true><<<nb, PBLOCK, 0, stream>>>(a);
+      substep_split_kernel<T, N, true><<<nb, 2 * PBLOCK, 0, stream>>>(a);
     else
-      substep_kernel<T, N, false><<<nb, PBLOCK, 0, stream>>>(a);
+      substep_split_kernel<T, N, false><<<nb, 2 * PBLOCK, 0, stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
     return PN_OK;
@@ -696,7 +695,7 @@ class Solver : public SolverBase {
     const int gn = par < 0 ? gl_n[0] + gl_n[1] : gl_n[par];
     if ((rc = launch_ghosts(a.u, false, a.bc, goff, gn, st ? st : stream))) return rc;
     a.pre_ghosts = 1;
-    integrate_kernel<T, N><<<par < 0 ? nblk_all : nblk_par[par], PBLOCK, 0, st ? st : stream>>>(a);
+    integrate_split_kernel<T, N><<<par < 0 ? nblk_all : nblk_par[par], 2 * PBLOCK, 0, st ? st : stream>>>(a);
     PN_CUDA(cudaGetLastError());
     ++n_launch;
     return PN_OK;
