@@ -479,6 +479,10 @@ const char* pn_last_error(const pn_handle* h);
    (no counterpart in the reference): evaluates it and the expm1f(c) / c form for n arguments. */
 int pn_selftest_phi1(int32_t n, const float* x, float* phi1_fast, float* phi1_ref);
 
+/* Self-test of the FP64 exponential factor phi1(c) = (e^c - 1) / c of the FP64 kernels (no
+   counterpart in the reference): evaluates it on the device for n arguments. */
+int pn_selftest_phi1_f64(int32_t n, const double* x, double* phi1);
+
 /* FP64 throughput probe (diagnostic; no counterpart in the reference): launches `blocks` blocks of
    256 threads, each thread running 8 independent FP64 FMA chains for `iters` iterations
    (blocks * 256 * iters * 16 flops) on `stream`; `out` is a device buffer of `blocks` doubles.

@@ -138,6 +138,8 @@ def lib():
         L.pn_server_destroy.restype = None
         L.pn_selftest_phi1.argtypes = [ctypes.c_int32, P, P, P]
         L.pn_selftest_phi1.restype = ctypes.c_int
+        L.pn_selftest_phi1_f64.argtypes = [ctypes.c_int32, P, P]
+        L.pn_selftest_phi1_f64.restype = ctypes.c_int
         L.pn_probe_fp64_fma.argtypes = [ctypes.c_int32, ctypes.c_int32, P, P]
         L.pn_probe_fp64_fma.restype = ctypes.c_int
         L.pn_material_create.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int64)]

@@ -143,29 +143,38 @@ struct IntArgs {
 // --------------------------------------------------------------------------------------------
 // small helpers
 // --------------------------------------------------------------------------------------------
+// 1 / n! as the double nearest to it (n! is exact in a double for n <= 18)
+__host__ __device__ constexpr double inv_fact(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; ++i) f *= i;
+  return 1.0 / f;
+}
+
+// sum_{k=0..K} c^k / (k+1)! in Horner form (K FMAs)
+template <int K>
+__device__ __forceinline__ double phi1_series(double c) {
+  double t = inv_fact(K + 1);
+#pragma unroll
+  for (int k = K - 1; k >= 0; --k) t = fma(t, c, inv_fact(k + 1));
+  return t;
+}
+
 // FP64 phi1(c) = (e^c - 1) / c, expm1div of solver_core.jl:38-44.  |c| <= 2e-4: the reference's
-// own Taylor form.  2e-4 < |c| <= 0.3 (every factor of the 2D/3D workloads: |c| = |C_l| dt / S
-// stays below ~0.27 on half steps): the series sum_k c^k / (k+1)! to k = 10 in Horner form.  Its
-// truncation is below 4.3e-15 relative at |c| = 0.3 and 2e-20 at 0.1, the same order as the
-// cancellation error of the reference's (e^c - 1) / c (~1e-15 at |c| = 0.1, growing as |c|
-// shrinks), and costs 11 FMAs instead of an exponential and a division on this GPU's scarce FP64
-// pipe.  Beyond: (exp(c) - 1) / c as the reference.
+// own Taylor form.  Above, the series sum_k c^k / (k+1)! truncated after the term K that keeps its
+// truncation below ~5e-16 relative on the range of |c| (the same order as the cancellation error
+// of the reference's (e^c - 1) / c there): K = 6 below 0.03, 8 below 0.1, 10 below 0.3 (4.3e-15 at
+// 0.3), 14 below 0.7; beyond, (exp(c) - 1) / c as the reference.  The factors of the 2D workloads
+// reach |c| = 0.27 on half steps and 0.62 on full steps (the high degrees), which before the K = 14
+// range paid an FP64 exponential and a division on this GPU's scarce FP64 pipe.  The range is
+// chosen on the integer pipe from the high word of c (monotone in |c|; each bound rounds down to
+// its high word, by less than 2^-20 relative).
 __device__ __forceinline__ double phi1(double c) {
   if (fabs(c) <= 0.0002) return 1.0 + 0.5 * c + 1.0 / 6.0 * (c * c);
-  if (fabs(c) <= 0.3) {
-    // 1/(k+1)! for k = 10 .. 1, then 1
-    double t = 1.0 / 39916800.0;
-    t = fma(t, c, 1.0 / 3628800.0);
-    t = fma(t, c, 1.0 / 362880.0);
-    t = fma(t, c, 1.0 / 40320.0);
-    t = fma(t, c, 1.0 / 5040.0);
-    t = fma(t, c, 1.0 / 720.0);
-    t = fma(t, c, 1.0 / 120.0);
-    t = fma(t, c, 1.0 / 24.0);
-    t = fma(t, c, 1.0 / 6.0);
-    t = fma(t, c, 0.5);
-    return fma(t, c, 1.0);
-  }
+  const unsigned hi = (unsigned)__double2hiint(c) & 0x7fffffffu;
+  if (hi < 0x3f9eb851u) return phi1_series<6>(c);    // |c| < 0.03
+  if (hi < 0x3fb99999u) return phi1_series<8>(c);    // |c| < 0.1
+  if (hi < 0x3fd33333u) return phi1_series<10>(c);   // |c| < 0.3
+  if (hi < 0x3fe66666u) return phi1_series<14>(c);   // |c| < 0.7
   return (exp(c) - 1.0) / c;
 }
 

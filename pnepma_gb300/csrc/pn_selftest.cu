@@ -46,6 +46,37 @@ extern "C" int pn_selftest_phi1(int32_t n, const float* x, float* phi1_fast, flo
   return PN_OK;
 }
 
+static __global__ void phi1_f64_kernel(const double* x, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = pn::phi1(x[i]);
+}
+
+extern "C" int pn_selftest_phi1_f64(int32_t n, const double* x, double* phi1) {
+  if (n < 0 || (n > 0 && (!x || !phi1))) {
+    pn::set_last_error("NULL argument");
+    return PN_ERR_INVALID;
+  }
+  if (n == 0) return PN_OK;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * 2 * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    pn::set_last_error("device allocation failed");
+    return PN_ERR_NO_MEMORY;
+  }
+  cudaError_t e = cudaMemcpy(d, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    phi1_f64_kernel<<<(n + 255) / 256, 256>>>(d, d + n, n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(phi1, d + n, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    pn::set_last_error(std::string("self-test failed: ") + cudaGetErrorString(e));
+    return PN_ERR_CUDA;
+  }
+  return PN_OK;
+}
+
 // FP64 fused multiply-add throughput probe: every thread runs 8 independent FMA chains for `iters`
 // iterations (16 flops per iteration), so the FP64 pipe, not latency, bounds it.  The chains
 // converge to y / (1 - x) and stay finite; their sum is written so nothing is optimised away.
