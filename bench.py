@@ -80,8 +80,9 @@ def parse():
                          "finite-difference check of the mass-fraction gradient on 32 cells; prints its own line")
     ap.add_argument("--fd-cells", type=int, default=32)
     ap.add_argument("--autotune", action="store_true",
-                    help="measure the batch configurations (kernel family, launch mode, tape schedule) on the FP32 "
-                         "batch of the 60-solve 2D workload, keep the fastest in the autotuner table and print it")
+                    help="measure the batch configurations (kernel family, launch mode, tape schedule, tile shape, "
+                         "CTAs per SM) on the FP32 batch of the 60-solve 2D workload and on one request of each "
+                         "served kind, keep the fastest per key in the autotuner table and print them")
     ap.add_argument("--autotune-table", default=os.path.join(HERE, "pnepma_gb300", "_build", "autotune.json"))
     ap.add_argument("--material", action="store_true",
                     help="device material fields and pullbacks on the 3D 96x96x64 per-cell boxed material "
@@ -1118,35 +1119,43 @@ def material_gradient(s, rho_bar, noa_bar, acs_bar, acs):
 
 
 def run_autotune(args):
-    """The autotuner on the FP32 batch of the 2D workload: every applicable configuration timed
-    (forward + adjoint of the 60 solves, inputs resident), the fastest kept in the table."""
+    """The autotuner on four batch keys: the FP32 batch of the 60-solve 2D workload (256x128 P11)
+    and one request of each kind of the served stream (2D 128x64 P11, 3D 64x64x48 P5, 1D 200
+    cells P7; 32 solves each).  Every applicable configuration is timed (forward + adjoint of the
+    batch, inputs resident, CUDA events) and the fastest kept in the table; one JSON line per key."""
     import torch
-    from pnepma_gb300 import autotune
+    from pnepma_gb300 import autotune, workloads
     from pnepma_gb300.problem import PN_FP32, PN_FP64
     torch.cuda.set_device(0)
-    solves = workload(args.positions)
-    inputs = [solves[0].inputs()] * len(solves)        # one material: the solves share the inputs
-    descs, keep = [], []
-    for s in solves:
-        s.problem.precision = PN_FP32
-        d, k = s.problem.descriptor(s.x_rays)
-        descs.append(d)
-        keep.append(k)
-        s.problem.precision = PN_FP64
-    ibars = [np.ones(len(s.x_rays)) for s in solves]
-    torch.cuda.empty_cache()
-    free_b, _tot = torch.cuda.mem_get_info()
+    batches = [("2D 256x128 P11 workload, 60 solves", workload(args.positions))]
+    for q, kind in enumerate(("2d", "3d", "1d")):
+        batches.append((f"served {kind} request, 32 solves", workloads.config5_kind(kind, 5000 + q, precision=PN_FP32)))
     os.makedirs(os.path.dirname(args.autotune_table), exist_ok=True)
     tuner = autotune.Autotuner(args.autotune_table)
-    key = autotune.batch_key(descs)
-    tuner.table.pop(key, None)                          # measure afresh
-    best = tuner.tune(descs, autotune.batch_timer(descs, keep, inputs, ibars, memory_budget=int(0.8 * free_b)))
-    entry = tuner.table[key]
-    line = {"metric": "autotuned FP32 batch: forward+adjoint seconds per configuration (60-solve 2D workload)",
-            "value": entry["seconds"], "unit": "s", "higher_is_better": False, "best": best.label(),
-            "measured": {m["label"]: m["seconds"] for m in entry["measured"]}, "key": key,
-            "table": args.autotune_table}
-    print(json.dumps(line), flush=True)
+    for label, solves in batches:
+        shared = solves[0].inputs()                      # one material per batch: the solves share it
+        inputs = [shared] * len(solves)
+        descs, keep = [], []
+        for s in solves:
+            prec = s.problem.precision
+            s.problem.precision = PN_FP32
+            d, k = s.problem.descriptor(s.x_rays)
+            descs.append(d)
+            keep.append(k)
+            s.problem.precision = prec
+        ibars = [np.ones(len(s.x_rays)) for s in solves]
+        torch.cuda.empty_cache()
+        free_b, _tot = torch.cuda.mem_get_info()
+        key = autotune.batch_key(descs)
+        tuner.table.pop(key, None)                      # measure afresh
+        best = tuner.tune(descs, autotune.batch_timer(descs, keep, inputs, ibars, memory_budget=int(0.8 * free_b)))
+        entry = tuner.table[key]
+        line = {"metric": f"autotuned FP32 batch: forward+adjoint seconds per configuration ({label})",
+                "value": entry["seconds"], "unit": "s", "higher_is_better": False, "best": best.label(),
+                "measured": {m["label"]: m["seconds"] for m in entry["measured"]}, "key": key,
+                "table": args.autotune_table}
+        print(json.dumps(line), flush=True)
+        del descs, keep, inputs
 
 
 def run_material(args):

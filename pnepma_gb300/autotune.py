@@ -16,7 +16,9 @@ The configurations are the batch engine's own runtime choices:
   target classes of a parity at one position (``PN_BATCH_PARITY_TILES``).
 
 The tile box (32 x 4 points) and the points per thread are compile-time constants of the TMA
-kernels (``PN_TMA_TY``, ``PN_TMA_PPT``) and are not among the runtime choices.  A configuration
+kernels (``PN_TMA_TY``, ``PN_TMA_PPT``) and are not among the runtime choices.  ``options_for``
+returns the tuned configuration of a batch's key from the table; the reconstruction driver's
+batches (``reconstruct.BatchBackend``) are built with it.  A configuration
 that does not change anything for a batch is skipped: the kernel family and the CTA count only
 matter for FP32 groups with two or three active axes.
 """
@@ -68,6 +70,26 @@ DEFAULT_CANDIDATES = (
     Config(4 << PN_BATCH_CTAS_PER_SM_SHIFT, 0),
     Config(PN_BATCH_PARITY_TILES, 0),
 )
+
+
+# the table `bench.py --autotune` writes and the library's batch users read
+DEFAULT_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
+
+
+def options_for(descs, path: str | None = DEFAULT_TABLE) -> dict:
+    """``capi.Batch`` keyword arguments (flags, checkpoint_stride) of the configuration the table
+    holds for the batch's key, or {} (the engine's defaults) when the table or the key is absent."""
+    if not path or not os.path.exists(path):
+        return {}
+    try:
+        with open(path) as f:
+            entry = json.load(f).get(batch_key(descs))
+    except (OSError, ValueError):
+        return {}
+    if not entry:
+        return {}
+    cfg = Config(**entry["config"])
+    return {"flags": cfg.flags, "checkpoint_stride": cfg.checkpoint_stride}
 
 
 def key_of(desc) -> str:

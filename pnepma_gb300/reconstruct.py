@@ -48,11 +48,12 @@ class BatchBackend:
 
     def __init__(self, descs, keep, memory_budget: int = 0, device: int = 0):
         import torch
-        from . import capi
+        from . import autotune, capi
         self.torch = torch
         self.dev = torch.device("cuda", device)
         torch.cuda.set_device(self.dev)
-        self.batch = capi.Batch(descs, keep, memory_budget=memory_budget)
+        # the autotuner's configuration for this batch's key, when its table has one
+        self.batch = capi.Batch(descs, keep, memory_budget=memory_budget, **autotune.options_for(descs))
         self.sizes = [capi.query_sizes(d) for d in descs]
         self.nr = [d.n_xrays for d in descs]
         self._inputs = None

@@ -78,3 +78,18 @@ def test_tune_without_any_measurable_configuration_is_an_error():
     d, k = _descs(dims=1, N=3, shape=(12,))
     with pytest.raises(RuntimeError):
         autotune.Autotuner().tune([d], lambda c: None)
+
+
+def test_options_for_reads_the_tuned_configuration(tmp_path):
+    """The batch users' view of the table: the tuned flags and stride of the batch's key, nothing
+    (the engine's defaults) for a key the table does not hold or when there is no table."""
+    d, k = _descs(dims=2, N=5, shape=(8, 7), precision=PN_FP32)
+    path = str(tmp_path / "table.json")
+    assert autotune.options_for([d], path) == {}
+    tuner = autotune.Autotuner(path)
+    best = autotune.Config(4 << autotune.PN_BATCH_CTAS_PER_SM_SHIFT, 0)
+    tuner.tune([d], lambda cfg: 0.5 if cfg == best else 1.0)
+    assert autotune.options_for([d], path) == {"flags": best.flags, "checkpoint_stride": 0}
+    other, k2 = _descs(dims=2, N=3, shape=(8, 7), precision=PN_FP32)
+    assert autotune.options_for([other], path) == {}
+    assert autotune.options_for([d], None) == {}
