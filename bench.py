@@ -495,6 +495,90 @@ def run_ours(args):
     step_ms = max_over_ranks(step_ms, dist, dev)
     value = whole_job_rate(world, nsol, step_ms)
 
+    # FP64 gradients of one solve per energy, for the FP32 batch's accuracy check below
+    g64_of = {}
+    for i in range(0, nsol, max(1, nsol // 3)):
+        with torch.cuda.stream(stream):
+            solve64(i)
+        stream.synchronize()
+        g64_of[i] = rb[0].cpu().numpy()
+    I64 = outI.cpu().numpy()
+
+    # ---------------- e2e through the host-pointer ABI with pinned buffers, every timed step
+    p_rho = torch.from_numpy(rho).pin_memory()
+    p_noa = torch.from_numpy(noa).pin_memory()
+    p_acs = torch.from_numpy(acs).pin_memory()
+    p_I = torch.zeros(nr, dtype=torch.float64).pin_memory()
+    p_ibar = d_ibar.cpu().pin_memory()
+    p_rb = torch.zeros(sz.n_rho, dtype=torch.float64).pin_memory()
+    p_nb = torch.zeros(sz.n_noa, dtype=torch.float64).pin_memory()
+    p_ab = torch.zeros(max(sz.n_acs, 1), dtype=torch.float64).pin_memory()
+    L = capi.lib()
+    P = capi._ptr
+
+    def e2e_step():
+        for i in range(nsol):
+            h = handles64[i]
+            h._check(L.pn_forward(h._h, P(p_rho.data_ptr()), P(p_noa.data_ptr()), P(p_acs.data_ptr()),
+                                  P(p_I.data_ptr())))
+            h._check(L.pn_adjoint(h._h, P(p_ibar[i].data_ptr()), P(p_rb.data_ptr()), P(p_nb.data_ptr()),
+                                  P(p_ab.data_ptr())))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(float(np.mean(e2e_times)), dist, dev)
+    h2d = nsol * (rho.nbytes + noa.nbytes + acs.nbytes + 8 * nr)
+    d2h = nsol * (8 * nr + 8 * (sz.n_rho + sz.n_noa + sz.n_acs))
+
+    # ---------------- roofline of the sub-step kernel (timed via the forward graph)
+    fwd_ms = []
+    for i in (0, nsol // 2, nsol - 1):
+        h = handles64[i]
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            h.forward_device(d_rho.data_ptr(), d_noa.data_ptr(), d_acs.data_ptr(), outI[i].data_ptr(), sp)
+            b.record(stream)
+        stream.synchronize()
+        fwd_ms.append((a.elapsed_time(b), solves[i].problem.N_steps))
+    bytes_step, m_active = algorithmic_bytes_per_step(solves[0], 8)
+    launches = sum(3 * n for _t, n in fwd_ms)
+    t_launch = sum(t for t, _n in fwd_ms) / launches * 1e-3
+    achieved = (bytes_step / 3) / t_launch / 1e9
+    flops_launch = fp64_flops_per_launch(solves[0])
+    fp64_achieved = flops_launch / t_launch / 1e12
+    fp64_peak = fp64_peak_tflops(dev, stream)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_source = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(HERE, "profiles", "substep_fp64_traffic.json")))
+        traffic = prof.get("dram_bytes_per_launch")
+    except Exception:
+        pass
+    # every FP64 measurement is done: release the handles, and with them the device's shared tape
+    # buffer, so that the FP32 batch's tapes can hold every state
+    gpu_launches = args.steps * sum(h.info().forward_kernels + h.info().adjoint_kernels for h in handles64)
+    for h in handles64:
+        h.close()
+    handles64 = []
+    torch.cuda.synchronize()
+
     # ---------------- FP32 batched: all 60 solves in one batch (one launch per sub-step)
     descs32, keep32 = [], []
     for s in solves:
@@ -551,52 +635,23 @@ def run_ours(args):
     binfo = batch.info()
 
     # accuracy of the FP32 batch against the FP64 plain results (same inputs)
-    I64 = outI.cpu().numpy()
     I32 = outI32.cpu().numpy()
     k_err = float(np.max(np.abs(I32 - I64) / np.abs(I64)))
     # gradient error on one solve of each energy
     g_err = 0.0
     for i in range(0, nsol, max(1, nsol // 3)):
-        with torch.cuda.stream(stream):
-            solve64(i)
-        stream.synchronize()
-        g64 = rb[0].cpu().numpy()
+        g64 = g64_of[i]
         g32 = rb32[i].cpu().numpy()
         g_err = max(g_err, float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64))))
 
-    # ---------------- e2e through the host-pointer ABI with pinned buffers, every timed step
-    p_rho = torch.from_numpy(rho).pin_memory()
-    p_noa = torch.from_numpy(noa).pin_memory()
-    p_acs = torch.from_numpy(acs).pin_memory()
-    p_I = torch.zeros(nr, dtype=torch.float64).pin_memory()
-    p_ibar = d_ibar.cpu().pin_memory()
-    p_rb = torch.zeros(sz.n_rho, dtype=torch.float64).pin_memory()
-    p_nb = torch.zeros(sz.n_noa, dtype=torch.float64).pin_memory()
-    p_ab = torch.zeros(max(sz.n_acs, 1), dtype=torch.float64).pin_memory()
-    L = capi.lib()
-    P = capi._ptr
+    # the FP32 adjoint sweep: fused sub-steps of the adjoint state, the density integral and the
+    # forward steps the tape recomputes, over the adjoint time of the batch
+    adj_bytes = sum(s.problem.N_steps * algorithmic_bytes_adjoint_step(s, 4) for s in solves)
+    adj_bytes += binfo.recomputed_steps * bytes32_step
+    adj_ms = float(np.mean(b_ms)) - float(np.mean(b_fwd))
+    fp32_adj_gbs = adj_bytes / (adj_ms / 1e3) / 1e9
 
-    def e2e_step():
-        for i in range(nsol):
-            h = handles64[i]
-            h._check(L.pn_forward(h._h, P(p_rho.data_ptr()), P(p_noa.data_ptr()), P(p_acs.data_ptr()),
-                                  P(p_I.data_ptr())))
-            h._check(L.pn_adjoint(h._h, P(p_ibar[i].data_ptr()), P(p_rb.data_ptr()), P(p_nb.data_ptr()),
-                                  P(p_ab.data_ptr())))
-
-    e2e_step()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    e2e_times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        e2e_step()
-        torch.cuda.synchronize()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_s = max_over_ranks(float(np.mean(e2e_times)), dist, dev)
-    h2d = nsol * (rho.nbytes + noa.nbytes + acs.nbytes + 8 * nr)
-    d2h = nsol * (8 * nr + 8 * (sz.n_rho + sz.n_noa + sz.n_acs))
+    mcu = sum(2 * s.problem.N_steps for s in solves) * m_active
 
     # ---------------- FP32 batched e2e: the 60 solves as one request through the server's host-buffer ABI
     served = None
@@ -630,49 +685,6 @@ def run_ours(args):
     # ---------------- served stream (config 5), bounded: 48 requests at 200 requests/s, then at 90 % of capacity
     if rank == 0 and not args.no_serve:
         served = served_summary(args)
-
-    # ---------------- roofline of the sub-step kernel (timed via the forward graph)
-    fwd_ms = []
-    for i in (0, nsol // 2, nsol - 1):
-        h = handles64[i]
-        with torch.cuda.stream(stream):
-            flush.fill_(1.0)
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            h.forward_device(d_rho.data_ptr(), d_noa.data_ptr(), d_acs.data_ptr(), outI[i].data_ptr(), sp)
-            b.record(stream)
-        stream.synchronize()
-        fwd_ms.append((a.elapsed_time(b), solves[i].problem.N_steps))
-    bytes_step, m_active = algorithmic_bytes_per_step(solves[0], 8)
-    launches = sum(3 * n for _t, n in fwd_ms)
-    t_launch = sum(t for t, _n in fwd_ms) / launches * 1e-3
-    achieved = (bytes_step / 3) / t_launch / 1e9
-    flops_launch = fp64_flops_per_launch(solves[0])
-    fp64_achieved = flops_launch / t_launch / 1e12
-    fp64_peak = fp64_peak_tflops(dev, stream)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    peak_source = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
-    traffic = None
-    try:
-        prof = json.load(open(os.path.join(HERE, "profiles", "substep_fp64_traffic.json")))
-        traffic = prof.get("dram_bytes_per_launch")
-    except Exception:
-        pass
-    # the FP32 adjoint sweep: fused sub-steps of the adjoint state, the density integral and the
-    # forward steps the tape recomputes, over the adjoint time of the batch
-    adj_bytes = sum(s.problem.N_steps * algorithmic_bytes_adjoint_step(s, 4) for s in solves)
-    adj_bytes += binfo.recomputed_steps * bytes32_step
-    adj_ms = float(np.mean(b_ms)) - float(np.mean(b_fwd))
-    fp32_adj_gbs = adj_bytes / (adj_ms / 1e3) / 1e9
-
-    gpu_launches = args.steps * sum(h.info().forward_kernels + h.info().adjoint_kernels for h in handles64)
-    mcu = sum(2 * s.problem.N_steps for s in solves) * m_active
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
