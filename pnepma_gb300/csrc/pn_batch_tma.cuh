@@ -190,6 +190,16 @@ struct TmaLayout {
   static constexpr int SMEM = TSTAGES * STAGE;
 };
 
+// Resident CTAs per SM the sub-step and density-integral tile kernels of an order are compiled for,
+// i.e. their register cap (65536 / (128 x CTAs)): as many as a tile stage's shared memory allows,
+// at most 8 (64 registers), at least PN_TMA_MINB.  The P11 2D stage (40.8 KB) allows 5; small
+// orders stage little (P5 3D: 20 KB) and were held to 5-6 CTAs per SM by their registers alone.
+template <int N, int DIMS>
+struct TmaMinBlocks {
+  static constexpr int by_smem = (228 * 1024) / (TmaLayout<N, DIMS>::SMEM + 1024);
+  static constexpr int value = by_smem > 8 ? 8 : (by_smem < PN_TMA_MINB ? PN_TMA_MINB : by_smem);
+};
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
@@ -778,7 +788,7 @@ __device__ __forceinline__ void tma_cell_of(const TLaunch<N>& L, const TTile& tt
 }
 
 template <int N, bool ADJ, int DIMS>
-__global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
+__global__ void __launch_bounds__(NTS, (TmaMinBlocks<N, DIMS>::value)) batch_tma_kernel(const __grid_constant__ TLaunch<N> L) {
   using LY = TmaLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
@@ -1034,7 +1044,7 @@ __device__ __forceinline__ void tma_int_cell_of(const TILaunch<N>& L, const TTil
 }
 
 template <int N, int DIMS>
-__global__ void __launch_bounds__(NTS, PN_TMA_MINB) batch_tma_int_kernel(const __grid_constant__ TILaunch<N> L) {
+__global__ void __launch_bounds__(NTS, (TmaMinBlocks<N, DIMS>::value)) batch_tma_int_kernel(const __grid_constant__ TILaunch<N> L) {
   using LY = TmaIntLayout<N, DIMS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long full[TSTAGES];
