@@ -200,9 +200,10 @@ def fp64_flops_per_launch(solve):
     energy step), counted from the compiled stencil: per target cell, per active axis one
     difference per neighbour moment and one FMA (2 flops) per coupling coefficient; per moment the
     update u + g_l ((q - A u) - C_l u) (5 flops); per cell and degree present in the class the
-    factors, S = sum_e rho_e s_e (2 n_e), C_l (2 n_e), g_l = dt/S phi1(-C_l dt/S) with the degree-10
-    series (22) -- computed in sub-steps 1 and 2 and reused by sub-step 3; per ghost point of a face
-    the boundary product B v (2 n_odd n_even)."""
+    factors, S = sum_e rho_e s_e (2 n_e), C_l (2 n_e), g_l = dt/S phi1(-C_l dt/S) counted as an
+    11-term series (22; the kernel evaluates 7 to 15 terms by the range of |c|, about 11 on
+    average over the degrees of the 2D workload) -- computed in sub-steps 1 and 2 and reused by
+    sub-step 3; per ghost point of a face the boundary product B v (2 n_odd n_even)."""
     from pnepma_gb300 import codegen
     from pnepma_gb300.moments import class_moments, parity, switch, class_bits
     N = solve.problem.N
