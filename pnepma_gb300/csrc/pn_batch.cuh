@@ -592,6 +592,21 @@ namespace pn {
 // ----------------------------------------------------------------------------------------------
 
 
+// A chunk of a call's solve pointers, carried to the device in kernel parameters (at most
+// IoChunk::MAX solves per launch; 25.6 KB of parameters).
+struct IoChunk {
+  static constexpr int MAX = 400;
+  BIo* dst;
+  int n;
+  int pad_;
+  BIo v[MAX];
+};
+static_assert(sizeof(IoChunk) < 32000, "IoChunk must fit the kernel parameter space");
+
+static __global__ void batch_put_io_kernel(const __grid_constant__ IoChunk c) {
+  for (int i = threadIdx.x; i < c.n; i += blockDim.x) c.dst[i] = c.v[i];
+}
+
 template <class T, int N, int DIMS>
 class BatchGroup : public BatchGroupBase {
  public:
@@ -678,8 +693,9 @@ class BatchGroup : public BatchGroupBase {
     }
   }
   long long device_bytes() const override { return bytes; }
-  long long launches_forward() const override { return nl_f + 2; }
-  long long launches_adjoint() const override { return nl_a + 2; }
+  // the recorded launches plus the call's own: the pointer upload, load / prep and store kernels
+  long long launches_forward() const override { return nl_f + 2 + (n + IoChunk::MAX - 1) / IoChunk::MAX; }
+  long long launches_adjoint() const override { return nl_a + 3 + (n + IoChunk::MAX - 1) / IoChunk::MAX; }
   int stride() const override { return K; }
   long long recomputed_steps() const override { return recomputed; }
   bool tma() const override { return use_tma; }
@@ -923,6 +939,12 @@ class BatchGroup : public BatchGroupBase {
     if (!direct) {
       if ((rc = capture(gf, true))) return rc;
       if ((rc = capture(ga, false))) return rc;
+      // upload both graphs now, on the idle upload stream: left to its first launch, the adjoint
+      // graph's upload queued behind the forward on the caller's stream and held the adjoint call
+      // on the host until the forward had finished on the device
+      PN_CUDA(cudaGraphUpload(gf, up));
+      PN_CUDA(cudaGraphUpload(ga, up));
+      PN_CUDA(cudaEventRecord(ev_up, up));
     } else {
       // count the launches of one sweep without issuing them
       nl = 0;
@@ -1798,10 +1820,18 @@ class BatchGroup : public BatchGroupBase {
     return PN_OK;
   }
 
+  // The call's solve pointers go to the device in the parameters of a small kernel: parameters
+  // are captured at launch, so the call does not wait for the stream (a copy from pageable host
+  // memory may wait for it to drain).
   int put_io(const BIo* io_host, cudaStream_t s) {
-    std::vector<BIo> v(n);
-    for (int q = 0; q < n; ++q) v[q] = io_host[members[q]];
-    PN_CUDA(cudaMemcpyAsync(dio, v.data(), sizeof(BIo) * n, cudaMemcpyHostToDevice, s));
+    IoChunk c;
+    for (int q0 = 0; q0 < n; q0 += IoChunk::MAX) {
+      c.dst = dio + q0;
+      c.n = std::min(IoChunk::MAX, n - q0);
+      for (int q = 0; q < c.n; ++q) c.v[q] = io_host[members[q0 + q]];
+      batch_put_io_kernel<<<1, 128, 0, s>>>(c);
+      PN_CUDA(cudaGetLastError());
+    }
     return PN_OK;
   }
 

@@ -77,6 +77,7 @@ struct Wave {
   std::vector<const double*> rho, noa, acs, ibar;
   std::vector<double*> I, rho_bar, noa_bar, acs_bar;
   int adjoint = 0;
+  bool alone = false;          // no other wave on the GPU and no request waiting at admission
   int rc = PN_OK;
   std::string err;
 };
@@ -225,9 +226,13 @@ int pn_server::launch_wave(Wave* w) {
   // tapes: first a fair share of what is free among the wave slots still open.  "Does not fit"
   // from the stride search wants a larger budget, a full arena (tables and tiles come on top of
   // the tapes) a smaller one, i.e. a longer checkpoint stride.
+  // A wave alone on the server (nothing else running or waiting) first tries half of the free
+  // memory, so that its tape keeps more states (a fair share among the wave slots made the adjoint
+  // of a lone 60-solve request recompute most of its forward); the other half stays for requests
+  // that arrive meanwhile (three quarters starved a served stream's later arrivals).
   const long long free_now = (long long)arena->free_bytes();
   const int open = std::max(1, max_waves - in_flight);
-  std::vector<long long> tries = {free_now / open};
+  std::vector<long long> tries = {w->alone ? free_now / 2 : free_now / open};
   for (long long b : {free_now * 3 / 4, free_now / 2, free_now / 4, free_now / 8})
     if (b != tries[0]) tries.push_back(b);
   int rc = PN_ERR_NO_MEMORY;
@@ -246,9 +251,15 @@ int pn_server::launch_wave(Wave* w) {
     release();
     return rc;
   }
-  if ((rc = pn_batch_forward(w->b, w->rho.data(), w->noa.data(), w->acs.data(), w->I.data(), w->st)) ||
-      (w->adjoint &&
-       (rc = pn_batch_adjoint(w->b, w->ibar.data(), w->rho_bar.data(), w->noa_bar.data(), w->acs_bar.data(), w->st)))) {
+  const auto t_built = Clock::now();
+  rc = pn_batch_forward(w->b, w->rho.data(), w->noa.data(), w->acs.data(), w->I.data(), w->st);
+  const auto t_fwd = Clock::now();
+  if (rc == PN_OK && w->adjoint)
+    rc = pn_batch_adjoint(w->b, w->ibar.data(), w->rho_bar.data(), w->noa_bar.data(), w->acs_bar.data(), w->st);
+  if (trace)
+    std::fprintf(stderr, "[pn] wave %d: forward launched in %.1f ms, adjoint in %.1f ms\n", w->id,
+                 ms_between(t_built, t_fwd), ms_between(t_fwd, Clock::now()));
+  if (rc) {
     w->err = pn_last_error(nullptr);
     // a group that failed part-way is not joined to the wave's stream: wait for all its work
     cudaDeviceSynchronize();
@@ -378,6 +389,7 @@ void pn_server::run() {
         it = pending.erase(it);
       }
       ++in_flight;
+      w->alone = in_flight == 1 && pending.empty();
       lk.unlock();
       const auto t = Clock::now();
       int rc = launch_wave(w);
