@@ -77,7 +77,6 @@ struct Wave {
   std::vector<const double*> rho, noa, acs, ibar;
   std::vector<double*> I, rho_bar, noa_bar, acs_bar;
   int adjoint = 0;
-  bool alone = false;          // no other wave on the GPU and no request waiting at admission
   int rc = PN_OK;
   std::string err;
 };
@@ -226,13 +225,9 @@ int pn_server::launch_wave(Wave* w) {
   // tapes: first a fair share of what is free among the wave slots still open.  "Does not fit"
   // from the stride search wants a larger budget, a full arena (tables and tiles come on top of
   // the tapes) a smaller one, i.e. a longer checkpoint stride.
-  // A wave alone on the server (nothing else running or waiting) first tries half of the free
-  // memory, so that its tape keeps more states (a fair share among the wave slots made the adjoint
-  // of a lone 60-solve request recompute most of its forward); the other half stays for requests
-  // that arrive meanwhile (three quarters starved a served stream's later arrivals).
   const long long free_now = (long long)arena->free_bytes();
   const int open = std::max(1, max_waves - in_flight);
-  std::vector<long long> tries = {w->alone ? free_now / 2 : free_now / open};
+  std::vector<long long> tries = {free_now / open};
   for (long long b : {free_now * 3 / 4, free_now / 2, free_now / 4, free_now / 8})
     if (b != tries[0]) tries.push_back(b);
   int rc = PN_ERR_NO_MEMORY;
@@ -389,7 +384,6 @@ void pn_server::run() {
         it = pending.erase(it);
       }
       ++in_flight;
-      w->alone = in_flight == 1 && pending.empty();
       lk.unlock();
       const auto t = Clock::now();
       int rc = launch_wave(w);
