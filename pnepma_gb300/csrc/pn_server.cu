@@ -222,14 +222,21 @@ int pn_server::launch_wave(Wave* w) {
       }
     }
   const auto t_io = Clock::now();
-  // tapes: first a fair share of what is free among the wave slots still open.  "Does not fit"
-  // from the stride search wants a larger budget, a full arena (tables and tiles come on top of
-  // the tapes) a smaller one, i.e. a longer checkpoint stride.
+  // tapes: a fair share of what is free among the wave slots still open or, for a wave whose every
+  // state would not fit that share, up to half of what is free (its adjoint then recomputes fewer
+  // forward steps; a batch takes only what its tape needs).  "Does not fit" from the stride search
+  // wants a larger budget, a full arena (tables and tiles come on top of the tapes) a smaller one,
+  // i.e. a longer checkpoint stride.
   const long long free_now = (long long)arena->free_bytes();
   const int open = std::max(1, max_waves - in_flight);
-  std::vector<long long> tries = {free_now / open};
-  for (long long b : {free_now * 3 / 4, free_now / 2, free_now / 4, free_now / 8})
-    if (b != tries[0]) tries.push_back(b);
+  long long need = 0;   // every state of every solve (the device layout's padding estimated)
+  for (int q = 0; q < n; ++q)
+    need += (long long)(descs[q]->n_steps + 1) * w->sizes[q].n_state * (descs[q]->precision == PN_FP32 ? 4 : 8);
+  need += need / 16;
+  const long long fair = free_now / open;
+  std::vector<long long> tries = {std::max(fair, std::min(need, free_now / 2))};
+  for (long long b : {fair, free_now * 3 / 4, free_now / 2, free_now / 4, free_now / 8})
+    if (std::find(tries.begin(), tries.end(), b) == tries.end()) tries.push_back(b);
   int rc = PN_ERR_NO_MEMORY;
   for (long long budget : tries) {
     std::string err;
