@@ -45,7 +45,7 @@ extern "C" {
 typedef enum pn_status {
   PN_OK = 0,
   PN_ERR_INVALID = -1,       /* malformed descriptor or argument */
-  PN_ERR_UNSUPPORTED = -2,   /* P_N order or layout not compiled into this build */
+  PN_ERR_UNSUPPORTED = -2,   /* P_N order or layout not compiled into the library */
   PN_ERR_CFL = -3,           /* energy step above the stability estimate (only with PN_FLAG_CHECK_CFL) */
   PN_ERR_NO_MEMORY = -4,     /* device allocation failed or memory budget exceeded */
   PN_ERR_DIVERGED = -5,      /* a non-finite value appeared in the solution */

@@ -102,7 +102,7 @@ int batch_create(const pn_desc* const* descs, int n, long long budget, int K, in
       BatchGroupBase* g = make_group(kv.first.first, precision, kv.first.second);
       if (!g) {
         delete b;
-        err = "P_N order " + std::to_string(kv.first.first) + " is not compiled into this build";
+        err = "P_N order " + std::to_string(kv.first.first) + " is not compiled into the library";
         return PN_ERR_UNSUPPORTED;
       }
       g->arena = arena;

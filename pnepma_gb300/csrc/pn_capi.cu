@@ -140,7 +140,7 @@ int pn_create(const pn_desc* desc, pn_handle** out) {
       return fail("no CUDA device is available", PN_ERR_NO_DEVICE);
     }
     pn::SolverBase* s = pn::make_solver(desc->order, desc->precision);
-    if (!s) return fail("P_N order " + std::to_string(desc->order) + " is not compiled into this build", PN_ERR_UNSUPPORTED);
+    if (!s) return fail("P_N order " + std::to_string(desc->order) + " is not compiled into the library", PN_ERR_UNSUPPORTED);
     rc = s->create(desc);
     if (rc) {
       std::string m = s->err;

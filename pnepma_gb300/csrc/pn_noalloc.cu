@@ -97,7 +97,7 @@ extern "C" int pn_forward_noalloc(const pn_desc* desc, const double* rho, const 
 #undef PN_CASE
       default:
         rc = PN_ERR_UNSUPPORTED;
-        err = "P_N order not compiled into this build";
+        err = "P_N order not compiled into the library";
     }
     if (rc) pn::set_last_error(err);
     return rc;
