@@ -743,7 +743,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s, "steps": args.steps},
             "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": fp64_achieved / fp64_peak, "traffic": traffic,
-                         "kernel": "substep_kernel<double,11> (forward)",
+                         "kernel": "substep_split_kernel<double,11> (forward)",
                          "algorithmic_flops_per_launch": flops_launch,
                          "peak_source": "measured in this run: pn_probe_fp64_fma (independent FP64 FMA chains)",
                          "launch_us": t_launch * 1e6,
